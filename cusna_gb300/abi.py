@@ -1,0 +1,177 @@
+"""ctypes mirror of the libcusna C ABI (include/libcusna.h).
+
+The struct layouts follow the reference header src/libcusna.h:90-208 field for
+field; `tests/test_abi.py` checks every offset against a C compiler. This module
+also loads the GB300 library (libcusna_gb300.so). There is no CPU fallback: if
+the library is missing, `load_library()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+ABI_VERSION = 1
+MAXEFF, MAXBEFF, MAXRATE, MAXNET, MAX_N = 24, 6, 4, 4, 8192
+
+STATUS = {0: "CUSNA_OK", 1: "CUSNA_ERR_NULL_ARG", 2: "CUSNA_ERR_SHAPE",
+          3: "CUSNA_ERR_NO_CUDA", 4: "CUSNA_ERR_CUDA", 5: "CUSNA_ERR_UNSUPPORTED",
+          6: "CUSNA_ERR_INTERNAL"}
+OK, ERR_NULL_ARG, ERR_SHAPE, ERR_NO_CUDA, ERR_CUDA, ERR_UNSUPPORTED, ERR_INTERNAL = range(7)
+
+_p = C.c_void_p
+_PROBLEM_FIELDS = [
+    ("struct_version", C.c_int32),
+    ("n", C.c_int32), ("W", C.c_int32), ("k", C.c_int32), ("M", C.c_int32),
+    ("threads", C.c_int32),
+    ("x0_out", _p), ("x0_in", _p), ("sim_out", _p), ("sim_in", _p),
+    ("lam", _p), ("theta", _p),
+    ("type_ids", _p), ("etypes", _p), ("wtab", _p), ("p1", _p), ("p2", _p),
+    ("vmat", _p), ("vmiss", _p), ("dyc_idx", _p), ("dyc", _p),
+    ("int0", _p), ("int1", _p), ("int2", _p), ("dyn_flags", _p),
+    ("kdist", _p), ("keep_out", _p), ("keep_in", _p), ("force_out", _p),
+    ("force_in", _p), ("perm", _p),
+    ("od0", _p), ("id0", _p),
+    ("maxdegree", C.c_int32), ("need_mask", C.c_int32), ("conditional", C.c_int32),
+    ("target_dist", C.c_int32), ("symflag", C.c_int32),
+    ("seed", C.c_uint64),
+    ("has_comp", C.c_int32), ("nact", C.c_int32), ("act", _p), ("inactw", _p),
+    ("kb", C.c_int32), ("lamb", _p), ("thetab", _p), ("bty", _p), ("z0", _p),
+    ("vb", _p), ("bkdist", _p),
+    ("zmin", C.c_int32), ("zmax", C.c_int32),
+    ("zbar", C.c_float), ("brange", C.c_float), ("bsimmean", C.c_float),
+    ("nrate", C.c_int32), ("rkind", _p), ("ralpha", _p), ("ru", _p),
+    ("vmat64", _p), ("wtab64", _p), ("vb64", _p), ("p1_64", _p), ("p2_64", _p),
+]
+
+
+class SaomProblem(C.Structure):
+    """cusna_saom_problem (src/libcusna.h:90-180)."""
+    _fields_ = _PROBLEM_FIELDS
+
+
+class SaomResult(C.Structure):
+    """cusna_saom_result (src/libcusna.h:185-208)."""
+    _fields_ = [
+        ("struct_version", C.c_int32),
+        ("stats", _p), ("ntim", _p), ("scores", _p),
+        ("dist", _p), ("dist_stat", _p), ("steps", _p),
+        ("bdist", _p), ("bscores", _p), ("z_end", _p),
+        ("rscores", _p), ("actor_dist", _p),
+        ("want_end_nets", C.c_int32), ("a_ends", _p),
+    ]
+
+
+class GpuOptions(C.Structure):
+    """cusna_gpu_options (extension, include/libcusna.h)."""
+    _fields_ = [
+        ("struct_version", C.c_int32), ("device_ptrs", C.c_int32),
+        ("chain_offset", C.c_uint32), ("warps_per_chain", C.c_int32),
+        ("chains_per_cta", C.c_int32), ("reserved0", C.c_int32),
+        ("stream", _p), ("elapsed_ms", C.c_double), ("ministeps", C.c_int64),
+    ]
+
+
+def _here() -> str:
+    return os.path.dirname(os.path.abspath(__file__))
+
+
+LIB_PATH = os.path.join(_here(), "_lib", "libcusna_gb300.so")
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libcusna_gb300.so and declare its symbols. Raises if it is absent:
+    the simulator has no CPU path."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"libcusna_gb300.so not found at {p}; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (no CPU fallback)")
+    lib = C.CDLL(p)
+    i32, u32 = C.c_int32, C.c_uint32
+    P = C.POINTER
+    lib.cusna_saom_simulate_period.argtypes = [P(SaomProblem), P(SaomResult)]
+    lib.cusna_saom_simulate_period.restype = i32
+    lib.cusna_saom_simulate_period_ex.argtypes = [P(SaomProblem), P(SaomResult), P(GpuOptions)]
+    lib.cusna_saom_simulate_period_ex.restype = i32
+    lib.cusna_saom_simulate_batch.argtypes = [P(SaomProblem), P(SaomResult), i32, P(GpuOptions)]
+    lib.cusna_saom_simulate_batch.restype = i32
+    lib.cusna_pack_bits.argtypes = [_p, i32, _p, _p, P(i32)]
+    lib.cusna_pack_bits.restype = i32
+    lib.cusna_philox4x32.argtypes = [P(u32), P(u32), P(u32)]
+    lib.cusna_philox4x32.restype = i32
+    lib.cusna_abi_version.restype = i32
+    lib.cusna_version_string.restype = C.c_char_p
+    lib.cusna_has_cuda.restype = i32
+    lib.cusna_last_error.restype = C.c_char_p
+    lib.cusna_network_stats_gpu.argtypes = [_p, i32, i32, i32, _p, _p, _p, _p, _p, _p,
+                                            _p, _p, _p, _p, i32, _p]
+    lib.cusna_network_stats_gpu.restype = i32
+    lib.cusna_behavior_stats_gpu.argtypes = [_p, i32, i32, i32, _p, _p, _p,
+                                             C.c_double, C.c_double, C.c_double, _p]
+    lib.cusna_behavior_stats_gpu.restype = i32
+    if path is None:
+        _lib = lib
+    return lib
+
+
+# Symbols include/libcusna.h declares; tests check the library exports each one.
+EXPORTED_SYMBOLS = [
+    "cusna_saom_simulate_period", "cusna_pack_bits", "cusna_philox4x32",
+    "cusna_abi_version", "cusna_version_string", "cusna_has_cuda", "cusna_last_error",
+    "cusna_saom_simulate_period_ex", "cusna_saom_simulate_batch",
+    "cusna_network_stats_gpu", "cusna_behavior_stats_gpu",
+]
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array (None for None)."""
+    if a is None:
+        return None
+    return a.ctypes.data
+
+
+class CudaError(RuntimeError):
+    pass
+
+
+def check(status: int, what: str, lib=None) -> None:
+    if status != OK:
+        detail = ""
+        if lib is not None:
+            try:
+                detail = (lib.cusna_last_error() or b"").decode()
+            except Exception:  # pragma: no cover - best effort
+                detail = ""
+        raise CudaError(f"{what} failed: {STATUS.get(status, status)}"
+                        + (f" ({detail})" if detail else ""))
+
+
+def pack_rows(dense: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Dense n*n 0/1 matrix -> (out rows, in rows), n*W uint32 each, bit (j&31)
+    of word (j>>5); the packing of src/cusna_saom_glue.cpp:22-32."""
+    d = np.ascontiguousarray(dense != 0)
+    n = d.shape[0]
+    W = (n + 31) // 32
+
+    def rows(m):
+        padded = np.zeros((n, W * 32), dtype=np.uint8)
+        padded[:, :n] = m
+        by = np.packbits(padded, axis=1, bitorder="little")
+        return np.ascontiguousarray(by).view(np.uint32).reshape(n, W).copy()
+
+    return rows(d), rows(d.T)
+
+
+def unpack_rows(rows: np.ndarray, n: int) -> np.ndarray:
+    """Inverse of pack_rows for one set of rows -> dense uint8 n*n."""
+    W = (n + 31) // 32
+    by = np.ascontiguousarray(rows.reshape(n, W).astype(np.uint32)).view(np.uint8)
+    bits = np.unpackbits(by, axis=1, bitorder="little")
+    return bits[:, :n].astype(np.uint8)

@@ -1,0 +1,256 @@
+/* ==========================================================================
+ * libcusna.h -- C ABI of the GB300 (sm_103a) SAOM period simulator.
+ *
+ * This header is the drop-in boundary of cusna's period simulator. The first
+ * part declares the same POD structs (field for field, byte-identical layout),
+ * status codes, capacity limits and entry points as the reference header
+ * src/libcusna.h of cran/cusna 0.1.1. A caller written against that header (the
+ * cpp11 glue src/cusna_saom_glue.cpp:57-189) compiles and links against
+ * libcusna_gb300.so unchanged. The second part (marked EXTENSION) adds new
+ * entry points. They have no counterpart in the reference, so nothing existing
+ * has to change for them.
+ *
+ * Conventions (src/libcusna.h:28-35):
+ *   - extern "C", fixed-width integer types, caller-allocated buffers, and NULL
+ *     skips an optional output;
+ *   - every struct starts with struct_version == CUSNA_ABI_VERSION;
+ *   - matrices are row-major. A "packed bit row" holds W = ceil(n/32) uint32
+ *     words per actor. Bit (j & 31) of word (j >> 5) is the tie to actor j.
+ *
+ * Every entry point is synchronous: its outputs are final when it returns.
+ * The library keeps no caller pointer after returning.
+ * ========================================================================== */
+#ifndef LIBCUSNA_H
+#define LIBCUSNA_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#  ifdef LIBCUSNA_BUILD
+#    define CUSNA_API __declspec(dllexport)
+#  else
+#    define CUSNA_API __declspec(dllimport)
+#  endif
+#else
+#  define CUSNA_API __attribute__((visibility("default")))
+#endif
+
+/* Capacity limits (src/libcusna.h:61-65). */
+#define CUSNA_MAXEFF  24  /* network effects per model            */
+#define CUSNA_MAXBEFF 6   /* behaviour effects per model          */
+#define CUSNA_MAXRATE 4   /* non-basic rate effects               */
+#define CUSNA_MAXNET  4   /* co-evolving networks (multi-net ABI) */
+#define CUSNA_MAX_N   8192
+
+#define CUSNA_ABI_VERSION 1  /* src/libcusna.h:69 */
+
+/* Status codes (src/libcusna.h:72-80). */
+typedef enum cusna_status {
+    CUSNA_OK              = 0,
+    CUSNA_ERR_NULL_ARG    = 1,  /* a required pointer is NULL                  */
+    CUSNA_ERR_SHAPE       = 2,  /* n/W/k/M out of range or inconsistent        */
+    CUSNA_ERR_NO_CUDA     = 3,  /* no usable CUDA device                       */
+    CUSNA_ERR_CUDA        = 4,  /* a CUDA call failed; see cusna_last_error()  */
+    CUSNA_ERR_UNSUPPORTED = 5,  /* option this build does not implement        */
+    CUSNA_ERR_INTERNAL    = 6   /* e.g. a chain hit the step cap               */
+} cusna_status;
+
+/* --------------------------------------------------------------------------
+ * One SAOM period, M chains (src/libcusna.h:90-180). n actors, W words per
+ * actor, k network effects, M chains.
+ * -------------------------------------------------------------------------- */
+typedef struct cusna_saom_problem {
+    int32_t struct_version;   /* CUSNA_ABI_VERSION                            */
+
+    int32_t n;                /* actors, 1..CUSNA_MAX_N                       */
+    int32_t W;                /* (n + 31) / 32                                */
+    int32_t k;                /* network effects, 1..CUSNA_MAXEFF             */
+    int32_t M;                /* chains                                       */
+    int32_t threads;          /* ignored here: launch shape is autotuned      */
+
+    const uint32_t *x0_out;   /* n*W out-ties of the period's start network   */
+    const uint32_t *x0_in;    /* n*W in-ties (transposed rows); not read      */
+    const uint32_t *sim_out;  /* [opt] simulation start rows (else x0_out)    */
+    const uint32_t *sim_in;   /* [opt] not read                               */
+
+    const float *lam;         /* M basic rates (chain c reads lam[c])         */
+    const float *theta;       /* M*k evaluation parameters (row c = chain c)  */
+
+    const int32_t *type_ids;  /* k effect type ids 0..32                      */
+    const int32_t *etypes;    /* [opt] k: 0 eval, 1 creation, 2 endowment     */
+    const float   *wtab;      /* [opt] k*(n+1) gwesp/gwdsp weights            */
+    const float   *p1;        /* [opt] k effect parameter 1                   */
+    const float   *p2;        /* [opt] k effect parameter 2                   */
+    const float   *vmat;      /* [opt] k*n covariate values                   */
+    const uint8_t *vmiss;     /* [opt] k*n covariate-missing flags (stats)    */
+    const int32_t *dyc_idx;   /* [opt] k dyadic covariate index or -1         */
+    const float   *dyc;       /* [opt] not read (the CPU engine zero-fills)   */
+    const int32_t *int0;      /* [opt] k interaction component 0 or -1        */
+    const int32_t *int1;      /* [opt] k interaction component 1 or -1        */
+    const int32_t *int2;      /* [opt] k interaction component 2 or -1        */
+    const int32_t *dyn_flags; /* [opt] k: covariate is the behaviour (0/1)    */
+
+    const uint32_t *kdist;    /* [opt] n*W dyads counted in the distance      */
+    const uint32_t *keep_out; /* [opt] n*W statistic net = (A & keep) | force */
+    const uint32_t *keep_in;  /* [opt] not read                               */
+    const uint32_t *force_out;/* [opt] n*W                                    */
+    const uint32_t *force_in; /* [opt] not read                               */
+    const uint32_t *perm;     /* [opt] n*W toggleable dyads                   */
+
+    const int32_t *od0;       /* [opt] n start out-degrees (degree stats)     */
+    const int32_t *id0;       /* [opt] n start in-degrees                     */
+
+    int32_t maxdegree;        /* > 0 forbids new ties at the bound            */
+    int32_t need_mask;        /* not read                                     */
+    int32_t conditional;      /* 1: stop at target_dist (internal rate)       */
+    int32_t target_dist;      /* conditional stopping distance                */
+    int32_t symflag;          /* symmetric network: paired toggles            */
+    uint64_t seed;            /* Philox key: low word k0, high word k1        */
+
+    int32_t has_comp;         /* restore inactive actors at the period end    */
+    int32_t nact;             /* active actors (read when act != NULL)        */
+    const int32_t  *act;      /* [opt] n: active actor ids first              */
+    const uint32_t *inactw;   /* [opt] W: inactive-actor bitmask              */
+
+    int32_t kb;               /* behaviour effects 0..CUSNA_MAXBEFF           */
+    const float   *lamb;      /* [opt] M behaviour rates                      */
+    const float   *thetab;    /* [opt] M*kb behaviour parameters              */
+    const int32_t *bty;       /* [opt] kb behaviour type ids 0..4             */
+    const int32_t *z0;        /* [opt] n start behaviour values               */
+    const float   *vb;        /* [opt] n centred start behaviour              */
+    const int32_t *bkdist;    /* [opt] n: actor counted in behaviour distance */
+    int32_t zmin, zmax;
+    float   zbar, brange, bsimmean;
+
+    int32_t nrate;            /* non-basic rate effects 0..CUSNA_MAXRATE      */
+    const int32_t *rkind;     /* [opt] nrate: 0 RateX, 1 outRate, 2 inRate    */
+    const float   *ralpha;    /* [opt] nrate rate parameters                  */
+    const float   *ru;        /* [opt] nrate*n RateX covariate values         */
+
+    /* float64 descriptors. When non-NULL they take precedence over the float
+     * fields above, as in the CPU engine (src/libcusna_saom_cpu.cpp:337-350).
+     * The cpp11 glue sets only these (src/cusna_saom_glue.cpp:101-103). */
+    const double *vmat64;     /* [opt] k*n                                    */
+    const double *wtab64;     /* [opt] k*(n+1)                                */
+    const double *vb64;       /* [opt] n                                      */
+    const double *p1_64;      /* [opt] k                                      */
+    const double *p2_64;      /* [opt] k                                      */
+} cusna_saom_problem;
+
+/* Outputs, caller-allocated; NULL skips one (src/libcusna.h:185-208). */
+typedef struct cusna_saom_result {
+    int32_t struct_version;
+
+    double  *stats;      /* [M*k]      statistics of the masked end network   */
+    double  *ntim;       /* [M]        simulated time                         */
+    float   *scores;     /* [M*(k+1)]  column 0 rate score, then k effects    */
+    int32_t *dist;       /* [M]        signed distance walked vs x0           */
+    int32_t *dist_stat;  /* [M]        |x_end xor x0| over kdist              */
+    int32_t *steps;      /* [M]        ministeps taken                        */
+
+    int32_t *bdist;      /* [opt] [M]          (kb > 0)                       */
+    float   *bscores;    /* [opt] [M*(kb+1)]   (kb > 0)                       */
+    int32_t *z_end;      /* [opt] [M*n]        (kb > 0)                       */
+
+    float   *rscores;    /* [opt] [M*nrate]    (nrate > 0)                    */
+    int32_t *actor_dist; /* [opt] [M*n]        (nrate > 0)                    */
+
+    int32_t  want_end_nets;
+    uint8_t *a_ends;     /* [opt] [M*n*n] dense end networks, row-major       */
+} cusna_saom_result;
+
+/* Run M chains of one period on the GPU (src/libcusna.h:210-213; the
+ * reference declares it but ships no definition). Chain c draws from Philox
+ * counters (msteps, c, 0, 0) and (msteps, c, 1, j) under key `seed`, as
+ * src/libcusna_saom_cpu.cpp:167,266 do, so trajectories equal the CPU
+ * engine's for the same seed. Returns CUSNA_ERR_NO_CUDA without a device. */
+CUSNA_API cusna_status cusna_saom_simulate_period(
+    const cusna_saom_problem *problem, cusna_saom_result *result);
+
+/* --------------------------------------------------------------------------
+ * Utilities (src/libcusna.h:297-305, :527-530).
+ * -------------------------------------------------------------------------- */
+
+/* Pack a dense row-major uint8 n*n adjacency into out rows and in rows (n*W
+ * words each, caller-allocated); *W_out = W (src/libcusna.h:299-301). */
+CUSNA_API cusna_status cusna_pack_bits(
+    const uint8_t *dense, int32_t n,
+    uint32_t *out_rows, uint32_t *in_rows, int32_t *W_out);
+
+/* One Philox4x32-10 block, the generator of the simulator (src/libcusna.h:
+ * 304-305; the round function is src/libcusna_saom_cpu.cpp:32-45). */
+CUSNA_API cusna_status cusna_philox4x32(
+    const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
+
+CUSNA_API int32_t     cusna_abi_version(void);     /* CUSNA_ABI_VERSION      */
+CUSNA_API const char *cusna_version_string(void);  /* build description      */
+CUSNA_API int32_t     cusna_has_cuda(void);        /* 1 if a device is usable */
+CUSNA_API const char *cusna_last_error(void);      /* per-thread error detail */
+
+/* ==========================================================================
+ * EXTENSION: GB300 entry points. None of these exists in the reference; the
+ * reference-facing symbols above do not depend on them.
+ * ========================================================================== */
+
+/* Launch and memory options for the _ex entry points. Zero-initialise and set
+ * struct_version; zero in every other field means "default". */
+typedef struct cusna_gpu_options {
+    int32_t  struct_version;   /* CUSNA_ABI_VERSION                           */
+    int32_t  device_ptrs;      /* 1: every problem/result pointer except the
+                                  struct itself is a device pointer            */
+    uint32_t chain_offset;     /* global index of chain 0 (Philox counter word
+                                  1), so M chains can be split across calls or
+                                  GPUs with identical results                  */
+    int32_t  warps_per_chain;  /* 0 = autotuned                               */
+    int32_t  chains_per_cta;   /* 0 = autotuned                               */
+    int32_t  reserved0;
+    void    *stream;           /* cudaStream_t to run on (NULL = the library's
+                                  own per-thread stream)                       */
+    double   elapsed_ms;       /* out: device time of the simulation kernels  */
+    int64_t  ministeps;        /* out: ministeps summed over all chains       */
+} cusna_gpu_options;
+
+/* cusna_saom_simulate_period with options (device-resident buffers, chain
+ * offset, stream) and device timing written back into *opts. */
+CUSNA_API cusna_status cusna_saom_simulate_period_ex(
+    const cusna_saom_problem *problem, cusna_saom_result *result,
+    cusna_gpu_options *opts);
+
+/* Run `count` independent problems (periods, groups, parameter points) in one
+ * persistent launch. Problems may have different n, k, M and effects; chains of
+ * all problems share one work queue. Each result is the same as a separate
+ * cusna_saom_simulate_period call on that problem. */
+CUSNA_API cusna_status cusna_saom_simulate_batch(
+    const cusna_saom_problem *problems, cusna_saom_result *results,
+    int32_t count, cusna_gpu_options *opts);
+
+/* Evaluation statistics of M end networks on the GPU: the batched device
+ * counterpart of the reference's host cusna_network_stats
+ * (src/libcusna_saom_cpu.cpp:619-689). `a_batch` is M*n*n dense uint8 (the
+ * statistic network per chain); the descriptors are those of
+ * cusna_network_stats. Fills out[M*k]. */
+CUSNA_API cusna_status cusna_network_stats_gpu(
+    const uint8_t *a_batch, int32_t n, int32_t M, int32_t k,
+    const int32_t *type_ids, const double *p1, const double *p2,
+    const double *vmat, const uint8_t *vmiss, const int32_t *dyn_flags,
+    const double *vb, const int32_t *od0, const int32_t *id0,
+    const double *wtab, int32_t symflag, double *out);
+
+/* Behaviour statistics of M end behaviour vectors on the GPU, the device
+ * counterpart of cusna_behavior_stats (src/libcusna_saom_cpu.cpp:768-817).
+ * Same arguments; fills out[M*kb]. */
+CUSNA_API cusna_status cusna_behavior_stats_gpu(
+    const int32_t *z_batch, int32_t n, int32_t M, int32_t kb,
+    const int32_t *bty, const uint8_t *xnet, const int32_t *bkdist,
+    double zbar, double brange, double bsimmean, double *out);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* LIBCUSNA_H */

@@ -1,0 +1,121 @@
+"""CPU ORACLE for the SAOM period simulator -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+package; the product (cusna_gb300) never does. Two CPU engines sit behind the
+same interface:
+
+  * Oracle("port") -- oracle/cusna_oracle.c, a C restatement of the reference
+    engine (src/libcusna_saom_cpu.cpp), built by `make -C oracle`;
+  * Oracle("reference") -- the reference engine itself compiled from its own
+    sources into oracle/_ref/ (`make -C oracle ref`). It only exists where the
+    reference sources are present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libcusna_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libcusna_ref.so")
+REF_SRC = os.environ.get("CUSNA_REFERENCE_DIR", "/root/reference")
+
+
+def build(ref: bool = True) -> None:
+    """Compile the oracle (and the reference engine when its sources exist)."""
+    subprocess.check_call(["make", "-s", "-C", HERE])
+    if ref and os.path.exists(os.path.join(REF_SRC, "src", "libcusna_saom_cpu.cpp")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"])
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+class Oracle:
+    """ctypes front end to one CPU engine ("port" or "reference")."""
+
+    def __init__(self, kind: str = "port"):
+        from cusna_gb300.abi import SaomProblem, SaomResult
+        self.kind = kind
+        path = PORT_SO if kind == "port" else REF_SO
+        if not os.path.exists(path):
+            if kind == "port":
+                build(ref=False)
+            else:
+                raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        pre = "oracle_" if kind == "port" else "cusna_"
+        sim = "oracle_simulate_period" if kind == "port" else "cusna_saom_simulate_period_cpu"
+        self._sim = getattr(self.lib, sim)
+        self._sim.argtypes = [C.POINTER(SaomProblem), C.POINTER(SaomResult)]
+        self._sim.restype = C.c_int32
+        vp, i32 = C.c_void_p, C.c_int32
+        self._ns = getattr(self.lib, pre + "network_stats")
+        self._ns.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp]
+        self._ns.restype = i32
+        self._bs = getattr(self.lib, pre + "behavior_stats")
+        self._bs.argtypes = [vp, i32, i32, i32, vp, vp, vp, C.c_double, C.c_double,
+                             C.c_double, vp]
+        self._bs.restype = i32
+        if kind == "port":
+            self._ph = self.lib.oracle_philox4x32
+            self._ph.argtypes = [vp, vp, vp]
+            self._ph.restype = i32
+            self.lib.oracle_max_threads.restype = i32
+
+    def max_threads(self) -> int:
+        if self.kind == "port":
+            return int(self.lib.oracle_max_threads())
+        return os.cpu_count() or 1
+
+    def simulate(self, m, threads: int = 0) -> dict:
+        """Run a marshalled period (cusna_gb300.glue.Marshalled); returns the
+        output arrays by name."""
+        from cusna_gb300.glue import result_dict
+        m.problem.threads = int(threads)
+        st = self._sim(C.byref(m.problem), C.byref(m.result))
+        if st != 0:
+            raise RuntimeError(f"{self.kind} simulate_period status {st}")
+        return result_dict(m)
+
+    def network_stats(self, a, n, k, type_ids, p1, p2, vmat, vmiss, dyn_flags, vb, od0, id0,
+                      wtab, symflag) -> np.ndarray:
+        def c(x, dt):
+            return None if x is None else np.ascontiguousarray(np.asarray(x, dtype=dt))
+        arrs = [c(np.asarray(a) != 0, np.uint8), c(type_ids, np.int32), c(p1, np.float64),
+                c(p2, np.float64), c(vmat, np.float64),
+                None if vmiss is None else c(np.asarray(vmiss) != 0, np.uint8),
+                c(dyn_flags, np.int32), c(vb, np.float64), c(od0, np.int32), c(id0, np.int32),
+                c(wtab, np.float64)]
+        out = np.zeros(k)
+        P = [None if x is None else x.ctypes.data for x in arrs]
+        st = self._ns(P[0], n, k, P[1], P[2], P[3], P[4], P[5], P[6], P[7], P[8], P[9], P[10],
+                      int(symflag), out.ctypes.data)
+        if st != 0:
+            raise RuntimeError(f"network_stats status {st}")
+        return out
+
+    def behavior_stats(self, z_batch, bty, xnet, bkdist, zbar, brange, bsimmean) -> np.ndarray:
+        z = np.ascontiguousarray(np.atleast_2d(np.asarray(z_batch, dtype=np.int32)))
+        M, n = z.shape
+        b = np.ascontiguousarray(np.asarray(bty, dtype=np.int32))
+        x = np.ascontiguousarray(np.asarray(xnet) != 0, dtype=np.uint8)
+        bk = None if bkdist is None else np.ascontiguousarray(np.asarray(bkdist, dtype=np.int32))
+        out = np.zeros((M, len(b)))
+        st = self._bs(z.ctypes.data, n, M, len(b), b.ctypes.data, x.ctypes.data,
+                      None if bk is None else bk.ctypes.data, float(zbar), float(brange),
+                      float(bsimmean), out.ctypes.data)
+        if st != 0:
+            raise RuntimeError(f"behavior_stats status {st}")
+        return out
+
+    def philox(self, counter, key) -> np.ndarray:
+        ctr = np.ascontiguousarray(np.asarray(counter, dtype=np.uint32))
+        ky = np.ascontiguousarray(np.asarray(key, dtype=np.uint32))
+        out = np.zeros(4, dtype=np.uint32)
+        self._ph(ctr.ctypes.data, ky.ctypes.data, out.ctypes.data)
+        return out
