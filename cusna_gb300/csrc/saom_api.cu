@@ -1,0 +1,786 @@
+// saom_api.cu -- host side of libcusna_gb300: argument validation with the
+// reference's status codes, a per-thread device arena and stream, input
+// preparation, the launch-shape autotuner, and the C ABI of include/libcusna.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "libcusna.h"
+#include "saom_launch.h"
+#include "saom_stats.cuh"
+
+namespace cusna {
+namespace {
+
+thread_local std::string g_err;
+
+void set_err(const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+
+#define CU(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return CUSNA_ERR_CUDA;                                                            \
+    }                                                                                   \
+  } while (0)
+
+// Per-thread device state: stream, growable device arena, device properties.
+struct Ctx {
+  int device = -1;
+  int sms = 0;
+  int smem_sm = 0, smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  void *arena = nullptr;
+  size_t cap = 0;
+  ~Ctx() {
+    // the CUDA runtime may already be torn down at thread exit; free best-effort
+    if (arena) cudaFree(arena);
+  }
+};
+thread_local Ctx g_ctx;
+
+cusna_status ensure_ctx() {
+  Ctx &c = g_ctx;
+  if (c.device >= 0) return CUSNA_OK;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count < 1) {
+    cudaGetLastError();
+    set_err("no CUDA device");
+    return CUSNA_ERR_NO_CUDA;
+  }
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  CU(cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev));
+  CU(cudaDeviceGetAttribute(&c.smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  CU(cudaDeviceGetAttribute(&c.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CU(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  CU(cudaEventCreate(&c.ev0));
+  CU(cudaEventCreate(&c.ev1));
+  c.device = dev;
+  return CUSNA_OK;
+}
+
+cusna_status ensure_arena(size_t bytes) {
+  Ctx &c = g_ctx;
+  if (bytes <= c.cap) return CUSNA_OK;
+  if (c.arena) {
+    CU(cudaStreamSynchronize(c.stream));
+    CU(cudaFree(c.arena));
+    c.arena = nullptr;
+    c.cap = 0;
+  }
+  size_t want = std::max(bytes, (size_t)64 << 20);
+  want = std::max(want, bytes + bytes / 4);
+  CU(cudaMalloc(&c.arena, want));
+  c.cap = want;
+  return CUSNA_OK;
+}
+
+// Bump planner over the arena: first pass records sizes, then pointers.
+struct Planner {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    const size_t o = off;
+    off = (off + bytes + 255) & ~(size_t)255;
+    return o;
+  }
+};
+
+template <class T>
+T *at(size_t off) {
+  return reinterpret_cast<T *>(static_cast<char *>(g_ctx.arena) + off);
+}
+
+
+// Per-problem host-side facts read during validation.
+struct Facts {
+  std::vector<int> tid, i0, i1, i2, rk;
+  int flags = 0;
+};
+
+cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, bool dev,
+                      Facts &F) {
+  if (!p || !r) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
+  if (p->struct_version != CUSNA_ABI_VERSION) {
+    set_err("struct_version %d != %d", p->struct_version, CUSNA_ABI_VERSION);
+    return CUSNA_ERR_SHAPE;
+  }
+  const int n = p->n, k = p->k;
+  if (n < 1 || n > CUSNA_MAX_N || p->W != (n + 31) / 32 || k < 1 || p->M < 1) {
+    set_err("bad shape n=%d W=%d k=%d M=%d", n, p->W, k, p->M);
+    return CUSNA_ERR_SHAPE;
+  }
+  if (k > CUSNA_MAXEFF || p->kb < 0 || p->kb > CUSNA_MAXBEFF || p->nrate < 0 ||
+      p->nrate > CUSNA_MAXRATE) {
+    set_err("capacity exceeded k=%d kb=%d nrate=%d", k, p->kb, p->nrate);
+    return CUSNA_ERR_SHAPE;
+  }
+  if (!p->x0_out || !p->theta || !p->lam || !p->type_ids) {
+    set_err("x0_out, theta, lam and type_ids are required");
+    return CUSNA_ERR_NULL_ARG;
+  }
+  if (p->kb > 0 && !p->bty) { set_err("bty is required when kb > 0"); return CUSNA_ERR_NULL_ARG; }
+  if (p->nrate > 0 && (!p->rkind || !p->ralpha || !p->ru)) {
+    set_err("rkind, ralpha and ru are required when nrate > 0");
+    return CUSNA_ERR_NULL_ARG;
+  }
+  if (p->act && (p->nact < 1 || p->nact > n)) { set_err("nact %d out of range", p->nact); return CUSNA_ERR_SHAPE; }
+  auto fetch = [&](const int32_t *src, int cnt, std::vector<int> &dst, int def) -> cusna_status {
+    dst.assign(cnt, def);
+    if (!src || cnt == 0) return CUSNA_OK;
+    if (dev) CU(cudaMemcpy(dst.data(), src, cnt * sizeof(int), cudaMemcpyDeviceToHost));
+    else std::memcpy(dst.data(), src, cnt * sizeof(int));
+    return CUSNA_OK;
+  };
+  cusna_status s;
+  if ((s = fetch(p->type_ids, k, F.tid, 0)) != CUSNA_OK) return s;
+  if ((s = fetch(p->int0, k, F.i0, -1)) != CUSNA_OK) return s;
+  if ((s = fetch(p->int1, k, F.i1, -1)) != CUSNA_OK) return s;
+  if ((s = fetch(p->int2, k, F.i2, -1)) != CUSNA_OK) return s;
+  if ((s = fetch(p->rkind, p->nrate, F.rk, 0)) != CUSNA_OK) return s;
+  if (p->act) {
+    std::vector<int> act;
+    if ((s = fetch(p->act, p->nact, act, 0)) != CUSNA_OK) return s;
+    for (int v : act)
+      if (v < 0 || v >= n) { set_err("act entry %d out of range", v); return CUSNA_ERR_SHAPE; }
+  }
+  int fl = 0;
+  for (int e = 0; e < k; ++e) {
+    const int t = F.tid[e];
+    switch (t) {
+      case 2: fl |= F_PC_RI_CJ | F_PC_RI_RJ; break;
+      case 3: case 23: fl |= F_PC_RJ_CI; break;
+      case 5: fl |= F_NEED_TP; break;
+      case 6: fl |= F_PC_RI_CJ | F_PC_RICIRJ; break;
+      case 19: fl |= F_NEED_RDEG; break;
+      case 24: fl |= F_PC_RI_CJ; break;
+      case 26: fl |= F_PC_RI_RJ; break;
+      case 27: fl |= F_PC_CI_CJ; break;
+      case 28: fl |= F_PC_CI_RJ; break;
+      case 29: fl |= F_NEED_GW29; break;
+      case 30: fl |= F_NEED_GW30; break;
+      case 32:
+        fl |= F_HAS_INTER;
+        if (F.i0[e] < 0 || F.i0[e] >= e || F.i1[e] < 0 || F.i1[e] >= e || F.i2[e] >= e) {
+          set_err("interaction %d: components must be earlier effects", e);
+          return CUSNA_ERR_SHAPE;
+        }
+        break;
+      default: break;
+    }
+  }
+  F.flags = fl;
+  // gwdsp change statistics index the weight table at p+1 with p <= n-2 on a
+  // network without self-ties; a self-tie in the start network could push p to
+  // n and read past the table, so such problems are rejected
+  if (fl & (F_NEED_GW29 | F_NEED_GW30)) {
+    const int W = p->W;
+    std::vector<uint32_t> rows((size_t)n * W);
+    for (const uint32_t *src : {p->x0_out, p->sim_out}) {
+      if (!src) continue;
+      if (dev) CU(cudaMemcpy(rows.data(), src, rows.size() * 4, cudaMemcpyDeviceToHost));
+      else std::memcpy(rows.data(), src, rows.size() * 4);
+      for (int i = 0; i < n; ++i)
+        if ((rows[(size_t)i * W + (i >> 5)] >> (i & 31)) & 1u) {
+          set_err("gwdsp effects need a start network without self-ties (actor %d)", i);
+          return CUSNA_ERR_SHAPE;
+        }
+    }
+  }
+  return CUSNA_OK;
+}
+
+// Sizes of the arrays a problem points at (for host -> device copies).
+struct RawSizes {
+  size_t rows, theta, lam, lamb, thetab, k4, k8, kn8, kn4f, kn1, wt8, wt4, n4, n8, n4f, W4, ru8,
+      ru4f, r4, rf;
+};
+
+// Device layout of one prepared problem.
+struct ProbBufs {
+  size_t x0T, x0cT, simT, simcT, kdistT, permT, keepT, forceT, keepcT, forcecT;
+  size_t vmat, wtab, p1, p2, vb, ralpha, ru;
+  size_t etypes, dyn, i0, i1, i2, act, z0, bkdist, inact, vmiss;
+  // raw copies (host mode)
+  size_t r_x0, r_sim, r_kd, r_pm, r_keep, r_force, r_theta, r_lam, r_lamb, r_thetab, r_tid,
+      r_ety, r_dyn, r_i0, r_i1, r_i2, r_vmat64, r_vmat32, r_wtab64, r_wtab32, r_p164, r_p132,
+      r_p264, r_p232, r_vb64, r_vb32, r_vmiss, r_od0, r_id0, r_act, r_inact, r_z0, r_bkd, r_bty,
+      r_rk, r_ra, r_ru;
+  // outputs (host mode)
+  size_t o_stats, o_ntim, o_scores, o_dist, o_dstat, o_steps, o_bdist, o_bscores, o_zend,
+      o_rscores, o_adist, o_aends;
+};
+
+const size_t NONE = ~(size_t)0;
+
+struct Job {
+  const cusna_saom_problem *p;
+  cusna_saom_result *r;
+  Facts F;
+  ProbBufs B;
+};
+
+size_t maybe(Planner &pl, const void *ptr, size_t bytes) {
+  return ptr ? pl.take(bytes) : NONE;
+}
+
+void plan_problem(Planner &pl, Job &J, bool dev) {
+  const cusna_saom_problem *p = J.p;
+  const cusna_saom_result *r = J.r;
+  const size_t n = p->n, W = p->W, k = p->k, M = p->M, kb = p->kb, nr = p->nrate;
+  const size_t bits = W * n * 4;
+  ProbBufs &B = J.B;
+  B.x0T = pl.take(bits); B.x0cT = pl.take(bits); B.simT = pl.take(bits); B.simcT = pl.take(bits);
+  B.kdistT = pl.take(bits); B.permT = pl.take(bits); B.keepT = pl.take(bits);
+  B.forceT = pl.take(bits); B.keepcT = pl.take(bits); B.forcecT = pl.take(bits);
+  B.vmat = pl.take(k * n * 8); B.wtab = pl.take(k * (n + 1) * 8);
+  B.p1 = pl.take(k * 8); B.p2 = pl.take(k * 8); B.vb = pl.take(n * 8);
+  B.ralpha = pl.take((nr + 1) * 8); B.ru = pl.take((nr + 1) * n * 8);
+  B.etypes = pl.take(k * 4); B.dyn = pl.take(k * 4); B.i0 = pl.take(k * 4);
+  B.i1 = pl.take(k * 4); B.i2 = pl.take(k * 4); B.act = pl.take(n * 4);
+  B.z0 = pl.take(n * 4); B.bkdist = pl.take(n * 4); B.inact = pl.take(W * 4);
+  B.vmiss = NONE;
+  if (!dev) {
+    B.r_x0 = pl.take(n * W * 4);
+    B.r_sim = maybe(pl, p->sim_out, n * W * 4);
+    B.r_kd = maybe(pl, p->kdist, n * W * 4);
+    B.r_pm = maybe(pl, p->perm, n * W * 4);
+    B.r_keep = maybe(pl, p->keep_out, n * W * 4);
+    B.r_force = maybe(pl, p->force_out, n * W * 4);
+    B.r_theta = pl.take(M * k * 4);
+    B.r_lam = pl.take(M * 4);
+    B.r_lamb = maybe(pl, p->lamb, M * 4);
+    B.r_thetab = maybe(pl, p->thetab, M * kb * 4);
+    B.r_tid = pl.take(k * 4);
+    B.r_ety = maybe(pl, p->etypes, k * 4);
+    B.r_dyn = maybe(pl, p->dyn_flags, k * 4);
+    B.r_i0 = maybe(pl, p->int0, k * 4);
+    B.r_i1 = maybe(pl, p->int1, k * 4);
+    B.r_i2 = maybe(pl, p->int2, k * 4);
+    B.r_vmat64 = maybe(pl, p->vmat64, k * n * 8);
+    B.r_vmat32 = p->vmat64 ? NONE : maybe(pl, p->vmat, k * n * 4);
+    B.r_wtab64 = maybe(pl, p->wtab64, k * (n + 1) * 8);
+    B.r_wtab32 = p->wtab64 ? NONE : maybe(pl, p->wtab, k * (n + 1) * 4);
+    B.r_p164 = maybe(pl, p->p1_64, k * 8);
+    B.r_p132 = p->p1_64 ? NONE : maybe(pl, p->p1, k * 4);
+    B.r_p264 = maybe(pl, p->p2_64, k * 8);
+    B.r_p232 = p->p2_64 ? NONE : maybe(pl, p->p2, k * 4);
+    B.r_vb64 = maybe(pl, p->vb64, n * 8);
+    B.r_vb32 = p->vb64 ? NONE : maybe(pl, p->vb, n * 4);
+    B.r_vmiss = maybe(pl, p->vmiss, k * n);
+    B.r_od0 = maybe(pl, p->od0, n * 4);
+    B.r_id0 = maybe(pl, p->id0, n * 4);
+    B.r_act = maybe(pl, p->act, n * 4);
+    B.r_inact = (p->has_comp && p->inactw) ? pl.take(W * 4) : NONE;
+    B.r_z0 = maybe(pl, p->z0, n * 4);
+    B.r_bkd = maybe(pl, p->bkdist, n * 4);
+    B.r_bty = kb ? pl.take(kb * 4) : NONE;
+    B.r_rk = nr ? pl.take(nr * 4) : NONE;
+    B.r_ra = nr ? pl.take(nr * 4) : NONE;
+    B.r_ru = nr ? pl.take(nr * n * 4) : NONE;
+    B.o_stats = maybe(pl, r->stats, M * k * 8);
+    B.o_ntim = maybe(pl, r->ntim, M * 8);
+    B.o_scores = maybe(pl, r->scores, M * (k + 1) * 4);
+    B.o_dist = maybe(pl, r->dist, M * 4);
+    B.o_dstat = maybe(pl, r->dist_stat, M * 4);
+    B.o_steps = maybe(pl, r->steps, M * 4);
+    B.o_bdist = kb ? maybe(pl, r->bdist, M * 4) : NONE;
+    B.o_bscores = kb ? maybe(pl, r->bscores, M * (kb + 1) * 4) : NONE;
+    B.o_zend = kb ? maybe(pl, r->z_end, M * n * 4) : NONE;
+    B.o_rscores = nr ? maybe(pl, r->rscores, M * nr * 4) : NONE;
+    B.o_adist = nr ? maybe(pl, r->actor_dist, M * n * 4) : NONE;
+    B.o_aends = (r->want_end_nets && r->a_ends) ? pl.take(M * n * n) : NONE;
+  }
+}
+
+// Host -> device copy of one raw array into its arena slot; returns its device
+// pointer (or the caller's device pointer in device mode).
+template <class T>
+const T *stage(const T *src, size_t off, size_t bytes, bool dev, cudaStream_t st, cusna_status &s) {
+  if (!src) return nullptr;
+  if (dev) return src;
+  if (off == NONE) return nullptr;
+  cudaError_t e = cudaMemcpyAsync(at<char>(off), src, bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) {
+    set_err("H2D copy failed: %s", cudaGetErrorString(e));
+    s = CUSNA_ERR_CUDA;
+  }
+  return at<T>(off);
+}
+
+cusna_status prepare(Job &J, bool dev, DevProblem &D, uint32_t chain_offset) {
+  const cusna_saom_problem *p = J.p;
+  cusna_saom_result *r = J.r;
+  const ProbBufs &B = J.B;
+  cudaStream_t st = g_ctx.stream;
+  const int n = p->n, W = p->W, k = p->k, M = p->M, kb = p->kb, nr = p->nrate;
+  cusna_status s = CUSNA_OK;
+  const size_t bitsz = (size_t)n * W * 4;
+
+  const uint32_t *x0 = stage(p->x0_out, B.r_x0, bitsz, dev, st, s);
+  const uint32_t *sim = stage(p->sim_out, B.r_sim, bitsz, dev, st, s);
+  const uint32_t *kd = stage(p->kdist, B.r_kd, bitsz, dev, st, s);
+  const uint32_t *pm = stage(p->perm, B.r_pm, bitsz, dev, st, s);
+  const uint32_t *kp = stage(p->keep_out, B.r_keep, bitsz, dev, st, s);
+  const uint32_t *fo = stage(p->force_out, B.r_force, bitsz, dev, st, s);
+  const float *theta = stage(p->theta, B.r_theta, (size_t)M * k * 4, dev, st, s);
+  const float *lam = stage(p->lam, B.r_lam, (size_t)M * 4, dev, st, s);
+  const float *lamb = stage(p->lamb, B.r_lamb, (size_t)M * 4, dev, st, s);
+  const float *thetab = kb ? stage(p->thetab, B.r_thetab, (size_t)M * kb * 4, dev, st, s) : nullptr;
+  const int *tid = stage(p->type_ids, B.r_tid, (size_t)k * 4, dev, st, s);
+  const int *ety = stage(p->etypes, B.r_ety, (size_t)k * 4, dev, st, s);
+  const int *dyn = stage(p->dyn_flags, B.r_dyn, (size_t)k * 4, dev, st, s);
+  const int *ri0 = stage(p->int0, B.r_i0, (size_t)k * 4, dev, st, s);
+  const int *ri1 = stage(p->int1, B.r_i1, (size_t)k * 4, dev, st, s);
+  const int *ri2 = stage(p->int2, B.r_i2, (size_t)k * 4, dev, st, s);
+  const double *vm64 = stage(p->vmat64, B.r_vmat64, (size_t)k * n * 8, dev, st, s);
+  const float *vm32 = p->vmat64 ? nullptr : stage(p->vmat, B.r_vmat32, (size_t)k * n * 4, dev, st, s);
+  const double *wt64 = stage(p->wtab64, B.r_wtab64, (size_t)k * (n + 1) * 8, dev, st, s);
+  const float *wt32 = p->wtab64 ? nullptr : stage(p->wtab, B.r_wtab32, (size_t)k * (n + 1) * 4, dev, st, s);
+  const double *p164 = stage(p->p1_64, B.r_p164, (size_t)k * 8, dev, st, s);
+  const float *p132 = p->p1_64 ? nullptr : stage(p->p1, B.r_p132, (size_t)k * 4, dev, st, s);
+  const double *p264 = stage(p->p2_64, B.r_p264, (size_t)k * 8, dev, st, s);
+  const float *p232 = p->p2_64 ? nullptr : stage(p->p2, B.r_p232, (size_t)k * 4, dev, st, s);
+  const double *vb64 = stage(p->vb64, B.r_vb64, (size_t)n * 8, dev, st, s);
+  const float *vb32 = p->vb64 ? nullptr : stage(p->vb, B.r_vb32, (size_t)n * 4, dev, st, s);
+  const uint8_t *vmiss = stage(p->vmiss, B.r_vmiss, (size_t)k * n, dev, st, s);
+  const int *od0 = stage(p->od0, B.r_od0, (size_t)n * 4, dev, st, s);
+  const int *id0 = stage(p->id0, B.r_id0, (size_t)n * 4, dev, st, s);
+  const int *act = stage(p->act, B.r_act, (size_t)n * 4, dev, st, s);
+  const uint32_t *inact = (p->has_comp && p->inactw) ? stage(p->inactw, B.r_inact, (size_t)W * 4, dev, st, s) : nullptr;
+  const int *z0 = stage(p->z0, B.r_z0, (size_t)n * 4, dev, st, s);
+  const int *bkd = stage(p->bkdist, B.r_bkd, (size_t)n * 4, dev, st, s);
+  const int *bty = kb ? stage(p->bty, B.r_bty, (size_t)kb * 4, dev, st, s) : nullptr;
+  const int *rk = nr ? stage(p->rkind, B.r_rk, (size_t)nr * 4, dev, st, s) : nullptr;
+  const float *ra = nr ? stage(p->ralpha, B.r_ra, (size_t)nr * 4, dev, st, s) : nullptr;
+  const float *ru = nr ? stage(p->ru, B.r_ru, (size_t)nr * n * 4, dev, st, s) : nullptr;
+  if (s != CUSNA_OK) return s;
+
+  // canonical word-major networks
+  CU(launch_prep_bits(x0, n, W, at<uint32_t>(B.x0T), at<uint32_t>(B.x0cT), 0, st));
+  CU(launch_prep_bits(sim ? sim : x0, n, W, at<uint32_t>(B.simT), at<uint32_t>(B.simcT), 0, st));
+  CU(launch_prep_bits(kd, n, W, at<uint32_t>(B.kdistT), nullptr, 1, st));
+  CU(launch_prep_bits(pm, n, W, at<uint32_t>(B.permT), nullptr, 1, st));
+  CU(launch_prep_bits(kp, n, W, at<uint32_t>(B.keepT), at<uint32_t>(B.keepcT), 1, st));
+  CU(launch_prep_bits(fo, n, W, at<uint32_t>(B.forceT), at<uint32_t>(B.forcecT), 2, st));
+  // float64 descriptors
+  CU(launch_prep_desc(vm64, vm32, (size_t)k * n, at<double>(B.vmat), st));
+  CU(launch_prep_desc(wt64, wt32, (size_t)k * (n + 1), at<double>(B.wtab), st));
+  CU(launch_prep_desc(p164, p132, (size_t)k, at<double>(B.p1), st));
+  CU(launch_prep_desc(p264, p232, (size_t)k, at<double>(B.p2), st));
+  CU(launch_prep_desc(vb64, vb32, (size_t)n, at<double>(B.vb), st));
+  if (nr) {
+    CU(launch_prep_desc(nullptr, ra, (size_t)nr, at<double>(B.ralpha), st));
+    CU(launch_prep_desc(nullptr, ru, (size_t)nr * n, at<double>(B.ru), st));
+  }
+  // integer descriptors with the CPU engine's defaults
+  auto icopy = [&](const int *src, size_t off, size_t cnt, int mode, int def) -> cusna_status {
+    if (src) CU(cudaMemcpyAsync(at<int>(off), src, cnt * 4, cudaMemcpyDeviceToDevice, st));
+    else CU(launch_fill_int(at<int>(off), cnt, mode, def, st));
+    return CUSNA_OK;
+  };
+  if ((s = icopy(ety, B.etypes, k, 0, 0)) != CUSNA_OK) return s;
+  if ((s = icopy(dyn, B.dyn, k, 0, 0)) != CUSNA_OK) return s;
+  if ((s = icopy(ri0, B.i0, k, 0, -1)) != CUSNA_OK) return s;
+  if ((s = icopy(ri1, B.i1, k, 0, -1)) != CUSNA_OK) return s;
+  if ((s = icopy(ri2, B.i2, k, 0, -1)) != CUSNA_OK) return s;
+  if ((s = icopy(z0, B.z0, n, 0, 0)) != CUSNA_OK) return s;
+  if ((s = icopy(bkd, B.bkdist, n, 0, 1)) != CUSNA_OK) return s;
+  if (act) {
+    CU(cudaMemcpyAsync(at<int>(B.act), act, (size_t)p->nact * 4, cudaMemcpyDeviceToDevice, st));
+  } else {
+    CU(launch_fill_int(at<int>(B.act), n, 1, 0, st));
+  }
+  if (inact) CU(cudaMemcpyAsync(at<uint32_t>(B.inact), inact, (size_t)W * 4, cudaMemcpyDeviceToDevice, st));
+  else CU(cudaMemsetAsync(at<uint32_t>(B.inact), 0, (size_t)W * 4, st));
+
+  std::memset(&D, 0, sizeof D);
+  D.n = n; D.W = W; D.k = k; D.kb = kb; D.nrate = nr; D.M = M;
+  D.chain_offset = chain_offset;
+  D.cond = p->conditional; D.target_dist = p->target_dist; D.symflag = p->symflag;
+  D.maxdeg = p->maxdegree; D.has_comp = p->has_comp && p->inactw; D.nact = p->act ? p->nact : n;
+  D.k0 = (uint32_t)(p->seed & 0xFFFFFFFFu);
+  D.k1 = (uint32_t)(p->seed >> 32);
+  D.flags = J.F.flags | ((r->want_end_nets && r->a_ends) ? F_WANT_ENDS : 0);
+  D.zmin = p->zmin; D.zmax = p->zmax;
+  D.zbar = (double)p->zbar; D.brange = (double)p->brange; D.bsimmean = (double)p->bsimmean;
+  D.type_ids = tid; D.etypes = at<int>(B.etypes); D.dyn = at<int>(B.dyn);
+  D.int0 = at<int>(B.i0); D.int1 = at<int>(B.i1); D.int2 = at<int>(B.i2);
+  D.p1 = at<double>(B.p1); D.p2 = at<double>(B.p2); D.vmat = at<double>(B.vmat);
+  D.wtab = at<double>(B.wtab); D.vmiss = vmiss; D.vb = at<double>(B.vb);
+  D.od0 = od0; D.id0 = id0; D.bty = bty; D.rkind = rk;
+  D.ralpha = at<double>(B.ralpha); D.ru = at<double>(B.ru);
+  D.act = at<int>(B.act); D.inact = at<uint32_t>(B.inact);
+  D.z0 = at<int>(B.z0); D.bkdist = at<int>(B.bkdist);
+  D.x0T = at<uint32_t>(B.x0T); D.x0cT = at<uint32_t>(B.x0cT);
+  D.simT = at<uint32_t>(B.simT); D.simcT = at<uint32_t>(B.simcT);
+  D.kdistT = at<uint32_t>(B.kdistT); D.permT = at<uint32_t>(B.permT);
+  D.keepT = at<uint32_t>(B.keepT); D.forceT = at<uint32_t>(B.forceT);
+  D.keepcT = at<uint32_t>(B.keepcT); D.forcecT = at<uint32_t>(B.forcecT);
+  D.lam = lam; D.theta = theta; D.lamb = lamb; D.thetab = thetab;
+  auto out = [&](void *user, size_t off) -> void * {
+    if (!user) return nullptr;
+    return dev ? user : (off == NONE ? nullptr : at<char>(off));
+  };
+  D.stats = (double *)out(r->stats, B.o_stats);
+  D.ntim = (double *)out(r->ntim, B.o_ntim);
+  D.scores = (float *)out(r->scores, B.o_scores);
+  D.dist = (int *)out(r->dist, B.o_dist);
+  D.dist_stat = (int *)out(r->dist_stat, B.o_dstat);
+  D.steps = (int *)out(r->steps, B.o_steps);
+  if (kb) {
+    D.bdist = (int *)out(r->bdist, B.o_bdist);
+    D.bscores = (float *)out(r->bscores, B.o_bscores);
+    D.z_end = (int *)out(r->z_end, B.o_zend);
+  }
+  if (nr) {
+    D.rscores = (float *)out(r->rscores, B.o_rscores);
+    D.actor_dist = (int *)out(r->actor_dist, B.o_adist);
+  }
+  D.a_ends = (r->want_end_nets && r->a_ends) ? (uint8_t *)out(r->a_ends, B.o_aends) : nullptr;
+  return CUSNA_OK;
+}
+
+cusna_status fetch_outputs(Job &J) {
+  const cusna_saom_problem *p = J.p;
+  cusna_saom_result *r = J.r;
+  const ProbBufs &B = J.B;
+  cudaStream_t st = g_ctx.stream;
+  const size_t n = p->n, k = p->k, M = p->M, kb = p->kb, nr = p->nrate;
+  auto get = [&](void *dst, size_t off, size_t bytes) -> cusna_status {
+    if (!dst || off == NONE) return CUSNA_OK;
+    CU(cudaMemcpyAsync(dst, at<char>(off), bytes, cudaMemcpyDeviceToHost, st));
+    return CUSNA_OK;
+  };
+  cusna_status s;
+  if ((s = get(r->stats, B.o_stats, M * k * 8)) != CUSNA_OK) return s;
+  if ((s = get(r->ntim, B.o_ntim, M * 8)) != CUSNA_OK) return s;
+  if ((s = get(r->scores, B.o_scores, M * (k + 1) * 4)) != CUSNA_OK) return s;
+  if ((s = get(r->dist, B.o_dist, M * 4)) != CUSNA_OK) return s;
+  if ((s = get(r->dist_stat, B.o_dstat, M * 4)) != CUSNA_OK) return s;
+  if ((s = get(r->steps, B.o_steps, M * 4)) != CUSNA_OK) return s;
+  if (kb) {
+    if ((s = get(r->bdist, B.o_bdist, M * 4)) != CUSNA_OK) return s;
+    if ((s = get(r->bscores, B.o_bscores, M * (kb + 1) * 4)) != CUSNA_OK) return s;
+    if ((s = get(r->z_end, B.o_zend, M * n * 4)) != CUSNA_OK) return s;
+  }
+  if (nr) {
+    if ((s = get(r->rscores, B.o_rscores, M * nr * 4)) != CUSNA_OK) return s;
+    if ((s = get(r->actor_dist, B.o_adist, M * n * 4)) != CUSNA_OK) return s;
+  }
+  if (r->want_end_nets && r->a_ends)
+    if ((s = get(r->a_ends, B.o_aends, M * n * n)) != CUSNA_OK) return s;
+  return CUSNA_OK;
+}
+
+// ---- launch-shape autotuner ---------------------------------------------------
+// The simulator is float64-bound on GB300, so the shape only has to keep every
+// SM sub-partition issuing float64 work: at least two warps per sub-partition
+// (8 per SM) with the chain state in shared memory. Among the shapes that fit,
+// prefer the fewest warps per chain (no team barriers) and many chains per SM.
+LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bool gw,
+                         bool tq, long long total_units, int force_G, int force_tpc) {
+  const Ctx &c = g_ctx;
+  LaunchShape best{};
+  best.G = 0;
+  const int Gs[5] = {1, 2, 4, 8, 16};
+  double best_score = -1.0;
+  for (int gi = 0; gi < 5; ++gi) {
+    const int G = Gs[gi];
+    if (force_G && G != force_G) continue;
+    for (int cols_smem = 1; cols_smem >= 0; --cols_smem) {
+      LaunchShape sh{};
+      sh.G = G;
+      sh.cols_in_smem = cols_smem;
+      sh.lay = make_layout(nmax, Wmax, kmax, kbmax, nrmax, G, cols_smem, tp, gw, tq);
+      if (sh.lay.bytes > (size_t)c.smem_optin) continue;
+      int tpc = 1;
+      if (G == 1) {
+        tpc = (int)std::min<size_t>(8, (size_t)c.smem_optin / sh.lay.bytes);
+        tpc = std::max(1, tpc);
+      }
+      if (force_tpc) {
+        tpc = force_tpc;
+        if (sh.lay.bytes * tpc > (size_t)c.smem_optin) continue;
+      }
+      if (G > 1 && tpc > 15) continue;
+      sh.teams_per_cta = tpc;
+      const size_t dyn = sh.lay.bytes * tpc;
+      int per_sm = period_blocks_per_sm(32 * G * tpc, dyn);
+      if (per_sm < 1) continue;
+      const int warps_sm = per_sm * tpc * G;
+      const double teams = (double)c.sms * per_sm * tpc;
+      // score: float64 issue coverage first, then fewer barriers, smem cols
+      double cover = std::min(1.0, warps_sm / 8.0);
+      double util = std::min(1.0, (double)total_units / teams);
+      double score = cover * 100.0 + util * 10.0 - G * 0.5 + (cols_smem ? 1.0 : 0.0);
+      if (score > best_score) {
+        best_score = score;
+        best = sh;
+        long long want = (total_units + tpc - 1) / tpc;
+        best.ctas = (int)std::max<long long>(1, std::min<long long>((long long)c.sms * per_sm, want));
+      }
+      if (cols_smem) break;  // smem columns fit: do not consider global ones
+    }
+  }
+  return best;
+}
+
+// Register limit check of a shape: the kernel is compiled for 512 threads with
+// the full register file, so any CTA size up to 512 fits.
+cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts) {
+  cusna_status s;
+  if ((s = ensure_ctx()) != CUSNA_OK) return s;
+  if (opts && opts->stream) {
+    // run on the caller's stream: adopt it for this call
+  }
+  cudaStream_t st = (opts && opts->stream) ? (cudaStream_t)opts->stream : g_ctx.stream;
+  cudaStream_t own = g_ctx.stream;
+  g_ctx.stream = st;
+  struct Restore { cudaStream_t &ref; cudaStream_t v; ~Restore() { ref = v; } } restore{g_ctx.stream, own};
+
+  const uint32_t off0 = opts ? opts->chain_offset : 0;
+  int nmax = 0, Wmax = 0, kmax = 0, kbmax = 0, nrmax = 0;
+  bool tp = false, gw = false, tq = false;
+  long long total = 0;
+  for (auto &J : jobs) {
+    nmax = std::max(nmax, J.p->n); Wmax = std::max(Wmax, J.p->W); kmax = std::max(kmax, J.p->k);
+    kbmax = std::max(kbmax, J.p->kb); nrmax = std::max(nrmax, J.p->nrate);
+    tp |= (J.F.flags & F_NEED_TP) != 0;
+    gw |= (J.F.flags & (F_NEED_GW29 | F_NEED_TP)) != 0;
+    tq |= (J.F.flags & F_NEED_GW30) != 0;
+    total += J.p->M;
+  }
+  LaunchShape sh = choose_shape(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total,
+                                opts ? opts->warps_per_chain : 0, opts ? opts->chains_per_cta : 0);
+  if (sh.G == 0) {
+    set_err("no launch shape fits n=%d in shared memory", nmax);
+    return CUSNA_ERR_UNSUPPORTED;
+  }
+  Planner pl;
+  for (auto &J : jobs) plan_problem(pl, J, dev);
+  const size_t o_probs = pl.take(sizeof(DevProblem) * jobs.size());
+  const size_t o_units = pl.take(sizeof(long long) * (jobs.size() + 1));
+  const size_t o_counter = pl.take(sizeof(unsigned long long));
+  const size_t teams = (size_t)sh.ctas * sh.teams_per_cta;
+  const size_t cols_words = (size_t)Wmax * nmax;
+  const size_t o_cols = sh.cols_in_smem ? NONE : pl.take(teams * cols_words * 4);
+  if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
+
+  std::vector<DevProblem> hp(jobs.size());
+  std::vector<long long> units(jobs.size() + 1, 0);
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    if ((s = prepare(jobs[q], dev, hp[q], off0)) != CUSNA_OK) return s;
+    units[q + 1] = units[q] + jobs[q].p->M;
+  }
+  CU(cudaMemcpyAsync(at<char>(o_probs), hp.data(), sizeof(DevProblem) * hp.size(),
+                     cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(o_units), units.data(), sizeof(long long) * units.size(),
+                     cudaMemcpyHostToDevice, st));
+  CU(cudaMemsetAsync(at<char>(o_counter), 0, sizeof(unsigned long long), st));
+  CU(cudaEventRecord(g_ctx.ev0, st));
+  CU(launch_period(sh, at<DevProblem>(o_probs), at<long long>(o_units), (int)jobs.size(), total,
+                   at<unsigned long long>(o_counter),
+                   o_cols == NONE ? nullptr : at<uint32_t>(o_cols), cols_words, st));
+  CU(cudaEventRecord(g_ctx.ev1, st));
+  if (!dev)
+    for (auto &J : jobs)
+      if ((s = fetch_outputs(J)) != CUSNA_OK) return s;
+  CU(cudaStreamSynchronize(st));
+  if (opts) {
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, g_ctx.ev0, g_ctx.ev1));
+    opts->elapsed_ms = ms;
+    opts->warps_per_chain = sh.G;
+    opts->chains_per_cta = sh.teams_per_cta;
+  }
+  return CUSNA_OK;
+}
+
+cusna_status simulate(const cusna_saom_problem *problems, cusna_saom_result *results, int count,
+                      cusna_gpu_options *opts) {
+  if (!problems || !results) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
+  if (count < 1) { set_err("count %d < 1", count); return CUSNA_ERR_SHAPE; }
+  if (opts && opts->struct_version != CUSNA_ABI_VERSION) {
+    set_err("options struct_version %d", opts->struct_version);
+    return CUSNA_ERR_SHAPE;
+  }
+  const bool dev = opts && opts->device_ptrs;
+  cusna_status s;
+  // host-mode arguments are checked before touching the device, so shape and
+  // NULL errors are reported exactly as the CPU engine reports them
+  if (dev && (s = ensure_ctx()) != CUSNA_OK) return s;
+  std::vector<Job> jobs(count);
+  for (int q = 0; q < count; ++q) {
+    jobs[q].p = &problems[q];
+    jobs[q].r = &results[q];
+    if ((s = validate(&problems[q], &results[q], dev, jobs[q].F)) != CUSNA_OK) return s;
+  }
+  if ((s = ensure_ctx()) != CUSNA_OK) return s;
+  s = run_jobs(jobs, dev, opts);
+  if (s == CUSNA_OK && opts) {
+    long long tot = 0;
+    // ministep totals are only known in host mode (steps copied back)
+    for (auto &J : jobs)
+      if (!dev && J.r->steps)
+        for (int c = 0; c < J.p->M; ++c) tot += J.r->steps[c];
+    opts->ministeps = tot;
+  }
+  return s;
+}
+
+}  // namespace
+}  // namespace cusna
+
+using namespace cusna;
+
+extern "C" {
+
+CUSNA_API cusna_status cusna_saom_simulate_period(const cusna_saom_problem *problem,
+                                                  cusna_saom_result *result) {
+  g_err.clear();
+  if (!problem || !result) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
+  return simulate(problem, result, 1, nullptr);
+}
+
+CUSNA_API cusna_status cusna_saom_simulate_period_ex(const cusna_saom_problem *problem,
+                                                     cusna_saom_result *result,
+                                                     cusna_gpu_options *opts) {
+  g_err.clear();
+  if (!problem || !result) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
+  return simulate(problem, result, 1, opts);
+}
+
+CUSNA_API cusna_status cusna_saom_simulate_batch(const cusna_saom_problem *problems,
+                                                 cusna_saom_result *results, int32_t count,
+                                                 cusna_gpu_options *opts) {
+  g_err.clear();
+  return simulate(problems, results, count, opts);
+}
+
+CUSNA_API cusna_status cusna_pack_bits(const uint8_t *dense, int32_t n, uint32_t *out_rows,
+                                       uint32_t *in_rows, int32_t *W_out) {
+  if (!dense || !out_rows || !in_rows) return CUSNA_ERR_NULL_ARG;
+  if (n < 1 || n > CUSNA_MAX_N) return CUSNA_ERR_SHAPE;
+  const int W = (n + 31) / 32;
+  std::memset(out_rows, 0, (size_t)n * W * 4);
+  std::memset(in_rows, 0, (size_t)n * W * 4);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      if (dense[(size_t)i * n + j]) {
+        out_rows[(size_t)i * W + (j >> 5)] |= 1u << (j & 31);
+        in_rows[(size_t)j * W + (i >> 5)] |= 1u << (i & 31);
+      }
+  if (W_out) *W_out = W;
+  return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_philox4x32(const uint32_t counter[4], const uint32_t key[2],
+                                        uint32_t out[4]) {
+  if (!counter || !key || !out) return CUSNA_ERR_NULL_ARG;
+  philox10(counter[0], counter[1], counter[2], counter[3], key[0], key[1], out);
+  return CUSNA_OK;
+}
+
+CUSNA_API int32_t cusna_abi_version(void) { return CUSNA_ABI_VERSION; }
+
+CUSNA_API const char *cusna_version_string(void) {
+  return "cusna-gb300 0.1 (sm_103a period simulator)";
+}
+
+CUSNA_API int32_t cusna_has_cuda(void) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return count > 0 ? 1 : 0;
+}
+
+CUSNA_API const char *cusna_last_error(void) { return g_err.c_str(); }
+
+CUSNA_API cusna_status cusna_network_stats_gpu(
+    const uint8_t *a_batch, int32_t n, int32_t M, int32_t k, const int32_t *type_ids,
+    const double *p1, const double *p2, const double *vmat, const uint8_t *vmiss,
+    const int32_t *dyn_flags, const double *vb, const int32_t *od0, const int32_t *id0,
+    const double *wtab, int32_t symflag, double *out) {
+  g_err.clear();
+  if (!a_batch || !type_ids || !out) { set_err("a_batch, type_ids and out are required"); return CUSNA_ERR_NULL_ARG; }
+  if (n < 1 || n > CUSNA_MAX_N || k < 1 || M < 1) { set_err("bad shape"); return CUSNA_ERR_SHAPE; }
+  cusna_status s = ensure_ctx();
+  if (s != CUSNA_OK) return s;
+  cudaStream_t st = g_ctx.stream;
+  const size_t nn = (size_t)n * n;
+  Planner pl;
+  const size_t oa = pl.take(nn * M), ot = pl.take(k * 4), o1 = pl.take(k * 8), o2 = pl.take(k * 8);
+  const size_t ov = pl.take((size_t)k * n * 8), om = pl.take((size_t)k * n), od = pl.take(k * 4);
+  const size_t ob = pl.take((size_t)n * 8), oo = pl.take((size_t)n * 4), oi = pl.take((size_t)n * 4);
+  const size_t ow = pl.take((size_t)k * (n + 1) * 8), oout = pl.take((size_t)M * k * 8);
+  if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
+  auto put = [&](size_t off, const void *src, size_t bytes) -> bool {
+    if (!src) return false;
+    return cudaMemcpyAsync(at<char>(off), src, bytes, cudaMemcpyHostToDevice, st) == cudaSuccess;
+  };
+  CU(cudaMemcpyAsync(at<char>(oa), a_batch, nn * M, cudaMemcpyHostToDevice, st));
+  put(ot, type_ids, k * 4);
+  StatDesc D{};
+  D.type_ids = at<int>(ot);
+  D.p1 = put(o1, p1, k * 8) ? at<double>(o1) : nullptr;
+  D.p2 = put(o2, p2, k * 8) ? at<double>(o2) : nullptr;
+  D.vmat = put(ov, vmat, (size_t)k * n * 8) ? at<double>(ov) : nullptr;
+  D.vmiss = put(om, vmiss, (size_t)k * n) ? at<uint8_t>(om) : nullptr;
+  D.dyn = put(od, dyn_flags, k * 4) ? at<int>(od) : nullptr;
+  D.vb = put(ob, vb, (size_t)n * 8) ? at<double>(ob) : nullptr;
+  D.od0 = put(oo, od0, (size_t)n * 4) ? at<int>(oo) : nullptr;
+  D.id0 = put(oi, id0, (size_t)n * 4) ? at<int>(oi) : nullptr;
+  D.wtab = put(ow, wtab, (size_t)k * (n + 1) * 8) ? at<double>(ow) : nullptr;
+  D.n = n; D.W = (n + 31) / 32; D.k = k; D.symflag = symflag;
+  CU(launch_netstats(at<uint8_t>(oa), M, D, at<double>(oout), g_ctx.sms, st));
+  CU(cudaMemcpyAsync(out, at<char>(oout), (size_t)M * k * 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_behavior_stats_gpu(const int32_t *z_batch, int32_t n, int32_t M,
+                                                int32_t kb, const int32_t *bty,
+                                                const uint8_t *xnet, const int32_t *bkdist,
+                                                double zbar, double brange, double bsimmean,
+                                                double *out) {
+  g_err.clear();
+  if (!z_batch || !bty || !xnet || !out) { set_err("z_batch, bty, xnet and out are required"); return CUSNA_ERR_NULL_ARG; }
+  if (n < 1 || n > CUSNA_MAX_N || M < 1 || kb < 1) { set_err("bad shape"); return CUSNA_ERR_SHAPE; }
+  cusna_status s = ensure_ctx();
+  if (s != CUSNA_OK) return s;
+  cudaStream_t st = g_ctx.stream;
+  Planner pl;
+  const size_t oz = pl.take((size_t)M * n * 4), ob = pl.take(kb * 4), ox = pl.take((size_t)n * n);
+  const size_t ok = pl.take((size_t)n * 4), oo = pl.take((size_t)M * kb * 8);
+  if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
+  CU(cudaMemcpyAsync(at<char>(oz), z_batch, (size_t)M * n * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(ob), bty, kb * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(ox), xnet, (size_t)n * n, cudaMemcpyHostToDevice, st));
+  if (bkdist) CU(cudaMemcpyAsync(at<char>(ok), bkdist, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+  CU(launch_behstats(at<int>(oz), n, M, kb, at<int>(ob), at<uint8_t>(ox),
+                     bkdist ? at<int>(ok) : nullptr, zbar, brange, bsimmean, at<double>(oo),
+                     g_ctx.sms, st));
+  CU(cudaMemcpyAsync(out, at<char>(oo), (size_t)M * kb * 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  return CUSNA_OK;
+}
+
+}  // extern "C"

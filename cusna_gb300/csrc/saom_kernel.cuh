@@ -1,0 +1,438 @@
+// saom_kernel.cuh -- the GB300 period-simulator kernel.
+//
+// One team of G warps (G = 1, 2, 4, 8 or 16) runs one chain at a time. Teams
+// take chains from a global work counter, so a launch holds one team per
+// resident slot and runs until the queue is empty (a persistent kernel). Each
+// team owns a slice of dynamic shared memory: the chain's out-rows and in-rows
+// as word-major bitsets, degrees, behaviour values and per-alter scratch.
+//
+// A network ministep (src/libcusna_saom_cpu.cpp:229-287) runs in three passes
+// over the alters j, which the team's lanes split in strides of 32*G:
+//   pass 1  change statistics d_je from popcounts of the bitsets, the float64
+//           linear predictor f_j = sum_e theta_e * d_je in the reference's
+//           e-order, and the maximum lmax of f over permitted alters;
+//   pass 2  w_j = exp(f_j - lmax) with the float64 sums sum_j w_j and
+//           sum_j w_j d_je (the log-sum-exp score), plus a float32 estimate of
+//           the Gumbel key g_j = f_j - log(-log u_j) for a shortlist;
+//   pass 3  the exact float64 Gumbel key of each shortlisted alter and the
+//           argmax with ties to the smaller j, as the reference chooses.
+// u_j comes from the reference's Philox counters (msteps, chain, 1, j), so the
+// chosen alter, and therefore the whole trajectory, equals the CPU engine's.
+#pragma once
+#include "saom_common.cuh"
+
+namespace cusna {
+
+// ---------------------------------------------------------------- team sync
+struct Team {
+  int G, L, tl, warp, lane, bar;
+  __device__ __forceinline__ void sync() const {
+    if (G == 1) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(L) : "memory");
+  }
+};
+
+// Per-team shared-memory slice. Sizes depend on the launch's largest problem.
+struct Slice {
+  uint32_t *rowsT;   // W*n
+  uint32_t *colsT;   // W*n (shared or global scratch)
+  int *indeg, *outdeg;
+  int *z;
+  double *fbuf;      // n
+  float *gbuf;       // n
+  uint32_t *okbits;  // W
+  int *tp;           // n   (transTies / gwdsp)
+  int *tq;           // n   (gwdspFB)
+  uint32_t *tpeq;    // 2W  (transTies masks tp==0, tp==1)
+  double *crate;     // n   (non-basic rates)
+  double *red;       // 32*G reduction scratch
+  double *th;        // k  parameters of the current chain
+  double *sc;        // k  scores
+  double *dstar;     // k  change statistics of the chosen alter
+  double *thb, *bsc; // kb
+  double *rsc;       // nrate
+  double *p1, *p2;   // k
+  int *tid, *ety, *dyn, *i0, *i1, *i2, *bty, *rkind;
+  int *misc;         // 8 ints: team broadcast slots
+};
+
+struct SliceLayout {
+  size_t bytes;  // per team
+  size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_f, o_g, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
+      o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc;
+};
+
+__host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Layout of one team slice for maxima (n, k, ...) over the launch.
+__host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, int nrate, int G,
+                                                   bool cols_in_smem, bool need_tp, bool need_gw,
+                                                   bool need_tq) {
+  SliceLayout s{};
+  size_t o = 0;
+  auto put = [&](size_t &field, size_t bytes) { field = o; o = al16(o + bytes); };
+  put(s.o_rows, (size_t)W * n * 4);
+  put(s.o_cols, cols_in_smem ? (size_t)W * n * 4 : 0);
+  put(s.o_indeg, (size_t)n * 4);
+  put(s.o_outdeg, (size_t)n * 4);
+  put(s.o_z, kb > 0 ? (size_t)n * 4 : 0);
+  put(s.o_f, (size_t)n * 8);
+  put(s.o_g, (size_t)n * 4);
+  put(s.o_ok, (size_t)W * 4);
+  put(s.o_tp, need_tp || need_gw ? (size_t)n * 4 : 0);
+  put(s.o_tq, need_tq ? (size_t)n * 4 : 0);
+  put(s.o_tpeq, need_tp ? (size_t)W * 8 : 0);
+  put(s.o_crate, nrate > 0 ? (size_t)n * 8 : 0);
+  put(s.o_red, (size_t)32 * G * 8 + 64);
+  put(s.o_th, (size_t)k * 8);
+  put(s.o_sc, (size_t)k * 8);
+  put(s.o_dstar, (size_t)k * 8);
+  put(s.o_thb, (size_t)(kb + 1) * 8);
+  put(s.o_bsc, (size_t)(kb + 1) * 8);
+  put(s.o_rsc, (size_t)(nrate + 1) * 8);
+  put(s.o_p1, (size_t)k * 8);
+  put(s.o_p2, (size_t)k * 8);
+  put(s.o_tid, (size_t)k * 4);
+  put(s.o_ety, (size_t)k * 4);
+  put(s.o_dyn, (size_t)k * 4);
+  put(s.o_i0, (size_t)k * 4);
+  put(s.o_i1, (size_t)k * 4);
+  put(s.o_i2, (size_t)k * 4);
+  put(s.o_bty, (size_t)(kb + 1) * 4);
+  put(s.o_rkind, (size_t)(nrate + 1) * 4);
+  put(s.o_misc, 16 * 4);
+  s.bytes = al16(o);
+  return s;
+}
+
+__device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L,
+                                       uint32_t *cols_global) {
+  Slice s;
+  s.rowsT = (uint32_t *)(base + L.o_rows);
+  s.colsT = cols_global ? cols_global : (uint32_t *)(base + L.o_cols);
+  s.indeg = (int *)(base + L.o_indeg);
+  s.outdeg = (int *)(base + L.o_outdeg);
+  s.z = (int *)(base + L.o_z);
+  s.fbuf = (double *)(base + L.o_f);
+  s.gbuf = (float *)(base + L.o_g);
+  s.okbits = (uint32_t *)(base + L.o_ok);
+  s.tp = (int *)(base + L.o_tp);
+  s.tq = (int *)(base + L.o_tq);
+  s.tpeq = (uint32_t *)(base + L.o_tpeq);
+  s.crate = (double *)(base + L.o_crate);
+  s.red = (double *)(base + L.o_red);
+  s.th = (double *)(base + L.o_th);
+  s.sc = (double *)(base + L.o_sc);
+  s.dstar = (double *)(base + L.o_dstar);
+  s.thb = (double *)(base + L.o_thb);
+  s.bsc = (double *)(base + L.o_bsc);
+  s.rsc = (double *)(base + L.o_rsc);
+  s.p1 = (double *)(base + L.o_p1);
+  s.p2 = (double *)(base + L.o_p2);
+  s.tid = (int *)(base + L.o_tid);
+  s.ety = (int *)(base + L.o_ety);
+  s.dyn = (int *)(base + L.o_dyn);
+  s.i0 = (int *)(base + L.o_i0);
+  s.i1 = (int *)(base + L.o_i1);
+  s.i2 = (int *)(base + L.o_i2);
+  s.bty = (int *)(base + L.o_bty);
+  s.rkind = (int *)(base + L.o_rkind);
+  s.misc = (int *)(base + L.o_misc);
+  return s;
+}
+
+__device__ __forceinline__ int bit_of(const uint32_t *T, int n, int row, int col) {
+  return (T[(col >> 5) * n + row] >> (col & 31)) & 1;
+}
+
+// ---------------------------------------------------------------- reductions
+// Sum of V doubles over the 32 lanes of a warp by recursive halving: stage s
+// exchanges half of the remaining values with the lane 16>>s away, so a lane
+// does V-1 + (5 - log2 V) additions instead of 5V. Afterwards the lane holds the
+// warp total of quantity q(lane) in v[0]; lanes with bit 0 clear report it.
+template <int V>
+__device__ __forceinline__ int warp_multi_sum(double (&v)[V], int lane) {
+  int q = 0;
+  int cnt = V;
+#pragma unroll
+  for (int s = 0; (1 << s) < V; ++s) {
+    const int o = 16 >> s;
+    const int half = V >> (s + 1);
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int x = 0; x < half; ++x) {
+      double send = up ? v[x] : v[x + half];
+      double keep = up ? v[x + half] : v[x];
+      double got = __shfl_xor_sync(kFull, send, o);
+      v[x] = __dadd_rn(keep, got);
+    }
+    if (up) q += half;
+    cnt = half;
+  }
+  (void)cnt;
+  // remaining butterfly stages (lanes sharing a quantity)
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int o = 16 >> s;
+    if ((1 << s) >= V) v[0] = __dadd_rn(v[0], __shfl_xor_sync(kFull, v[0], o));
+  }
+  return q;
+}
+
+__device__ __forceinline__ long long warp_max_ll(long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    long long y = __shfl_xor_sync(kFull, x, o);
+    x = y > x ? y : x;
+  }
+  return x;
+}
+
+__device__ __forceinline__ float warp_max_f(float x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(kFull, x, o));
+  return x;
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+  return x;
+}
+
+// Team-wide helpers. `red` is the team's scratch (>= 32*G doubles).
+__device__ __forceinline__ long long team_max_ll(const Team &T, long long x, double *red) {
+  x = warp_max_ll(x);
+  if (T.G == 1) return x;
+  long long *r = (long long *)red;
+  T.sync();
+  if (T.lane == 0) r[T.warp] = x;
+  T.sync();
+  long long m = r[0];
+  for (int w = 1; w < T.G; ++w) m = r[w] > m ? r[w] : m;
+  return m;
+}
+
+__device__ __forceinline__ float team_max_f(const Team &T, float x, double *red) {
+  x = warp_max_f(x);
+  if (T.G == 1) return x;
+  float *r = (float *)red;
+  T.sync();
+  if (T.lane == 0) r[T.warp] = x;
+  T.sync();
+  float m = r[0];
+  for (int w = 1; w < T.G; ++w) m = fmaxf(m, r[w]);
+  return m;
+}
+
+__device__ __forceinline__ long long team_sum_ll(const Team &T, long long x, double *red) {
+  x = warp_sum_ll(x);
+  if (T.G == 1) return x;
+  long long *r = (long long *)red;
+  T.sync();
+  if (T.lane == 0) r[T.warp] = x;
+  T.sync();
+  long long m = 0;
+  for (int w = 0; w < T.G; ++w) m += r[w];
+  return m;
+}
+
+// Argmax of (key, -j) over the team: larger key wins, ties to the smaller j.
+__device__ __forceinline__ int team_argmax(const Team &T, long long key, int j, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    long long k2 = __shfl_xor_sync(kFull, key, o);
+    int j2 = __shfl_xor_sync(kFull, j, o);
+    if (k2 > key || (k2 == key && j2 < j)) { key = k2; j = j2; }
+  }
+  if (T.G == 1) return j;
+  long long *rk = (long long *)red;
+  int *rj = (int *)(red + T.G);
+  T.sync();
+  if (T.lane == 0) { rk[T.warp] = key; rj[T.warp] = j; }
+  T.sync();
+  long long bk = rk[0];
+  int bj = rj[0];
+  for (int w = 1; w < T.G; ++w)
+    if (rk[w] > bk || (rk[w] == bk && rj[w] < bj)) { bk = rk[w]; bj = rj[w]; }
+  return bj;
+}
+
+// ------------------------------------------------------- change statistics
+// Per-ministep context shared by all alters (uniform over the team).
+struct StepCtx {
+  int i, od_i, id_i, rdeg_i;
+  double zvi;
+};
+
+// Popcount of (A_word(a) & B_word(b)) summed over the W words.
+__device__ __forceinline__ int pc2(const uint32_t *A, int a, const uint32_t *B, int b, int n, int W) {
+  int c = 0;
+  for (int w = 0; w < W; ++w) c += __popc(A[w * n + a] & B[w * n + b]);
+  return c;
+}
+
+// Exact (double)c for 0 <= c < 2^31 built on the integer pipes.
+__device__ __forceinline__ double i2d(int c) {
+  if (c == 0) return 0.0;
+  const int e = 31 - __clz(c);
+  const unsigned long long m = ((unsigned long long)(unsigned)c << (52 - e)) & 0xFFFFFFFFFFFFFull;
+  return __longlong_as_double((long long)((((unsigned long long)(1023 + e)) << 52) | m));
+}
+// x * delta for delta = +-1 is exact, so it is a sign flip (sgn = 0 or 1<<63).
+__device__ __forceinline__ double flip(double x, unsigned long long sgn) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)sgn);
+}
+
+// Change statistics of toggling i -> j for all k effects (src/libcusna_saom_cpu.cpp:
+// 49-101 per effect type, :243-261 for the per-alter loop with interactions and
+// creation/endowment zeroing). Popcounts of the word-major bitsets replace the
+// reference's O(n) dense loops; they count the same sets:
+//   |out_i & in_j| = #{h: a_ih a_hj}      |out_i & out_j| = #{h: a_ih a_jh}
+//   |out_j & in_i| = #{h: a_jh a_hi}      |in_i & in_j|   = #{h: a_hi a_hj}
+//   |in_i & out_j| = #{h: a_hi a_jh}
+// Every float64 value equals the reference's: delta * x is a sign flip of x,
+// and all other operations use the reference's operands and order.
+__device__ __forceinline__ void change_stats(const DevProblem &P, const Slice &S, const StepCtx &X,
+                                             int j, int aij, int aji, double *d) {
+  const int n = P.n, W = P.W, k = P.k, i = X.i;
+  const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;
+  const double dl = aij ? -1.0 : 1.0;
+  const int fl = P.flags;
+  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;
+  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
+    const uint32_t *R = S.rowsT, *Cc = S.colsT;
+    for (int w = 0; w < W; ++w) {
+      const uint32_t ri = R[w * n + i], rj = R[w * n + j];
+      const uint32_t ci = Cc[w * n + i], cj = Cc[w * n + j];
+      if (fl & F_PC_RI_CJ) ri_cj += __popc(ri & cj);
+      if (fl & F_PC_RI_RJ) ri_rj += __popc(ri & rj);
+      if (fl & F_PC_RJ_CI) rj_ci += __popc(rj & ci);
+      if (fl & F_PC_CI_CJ) ci_cj += __popc(ci & cj);
+      if (fl & F_PC_CI_RJ) ci_rj += __popc(ci & rj);
+      if (fl & F_PC_RICIRJ) ricirj += __popc(ri & ci & rj);
+    }
+  }
+  const double zvj = P.kb > 0 ? __dsub_rn((double)S.z[j], P.zbar) : 0.0;
+#pragma unroll 1
+  for (int e = 0; e < k; ++e) {
+    const int t = S.tid[e];
+    double v;
+    if (t == 32) {  // interaction: product of earlier statistics (:246-251)
+      const int c2 = S.i2[e];
+      v = c2 < 0 ? dl : 1.0;
+      v = __dmul_rn(v, __dmul_rn(d[S.i0[e]], d[S.i1[e]]));
+      if (c2 >= 0) v = __dmul_rn(v, d[c2]);
+      d[e] = v;
+      continue;
+    }
+    double vi = 0.0, vj = 0.0;
+    if ((t >= 10 && t <= 13) || t == 20 || t == 21 || t == 25 || t == 31) {
+      const bool dy = S.dyn[e] != 0;
+      vi = dy ? X.zvi : P.vmat[(size_t)e * n + i];
+      vj = dy ? zvj : P.vmat[(size_t)e * n + j];
+    }
+    switch (t) {
+      case 0: v = dl; break;
+      case 1: v = flip((double)aji, sg); break;
+      case 2: v = flip(i2d(ri_cj + ri_rj), sg); break;
+      case 3: case 23: v = flip(i2d(rj_ci), sg); break;
+      case 4: v = flip(i2d(S.indeg[j] + 1 - aij), sg); break;
+      case 5: {
+        int c = 0;
+        const uint32_t *eq = S.tpeq + (aij ? W : 0);
+        for (int w = 0; w < W; ++w)
+          c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);
+        if (S.tp[j] > 0) ++c;
+        v = flip(i2d(c), sg);
+        break;
+      }
+      case 6: v = flip(i2d((aji ? ri_cj : 0) + ricirj), sg); break;
+      case 7: v = flip(sqrt(i2d(S.indeg[j] + 1 - aij)), sg); break;
+      case 8: v = flip(i2d(S.outdeg[j]), sg); break;
+      case 9: v = flip(sqrt(i2d(S.outdeg[j])), sg); break;
+      case 10: v = flip(vi, sg); break;
+      case 11: v = flip(vj, sg); break;
+      case 12:
+        v = flip(__dsub_rn(__dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn(vi, vj)), S.p1[e])), S.p2[e]), sg);
+        break;
+      case 13: v = flip(fabs(__dsub_rn(vi, vj)) < 1e-9 ? 1.0 : 0.0, sg); break;
+      case 14: v = flip(i2d(X.id_i), sg); break;
+      case 15: v = flip(sqrt(i2d(X.id_i)), sg); break;
+      case 16: v = flip(__dadd_rn(__dmul_rn(2.0, i2d(X.od_i)), dl), sg); break;
+      case 17: {
+        const double d0 = i2d(X.od_i), d1 = __dadd_rn(d0, dl);
+        v = __dsub_rn(__dmul_rn(d1, sqrt(d1)), __dmul_rn(d0, sqrt(d0)));
+        break;
+      }
+      case 18: {
+        const double d0 = i2d(X.od_i);
+        v = __dsub_rn(fmin(__dadd_rn(d0, dl), S.p1[e]), fmin(d0, S.p1[e]));
+        break;
+      }
+      case 19:
+        v = flip(__dadd_rn(i2d(X.rdeg_i), __dmul_rn((double)aji, __dadd_rn(i2d(X.od_i), dl))), sg);
+        break;
+      case 20:
+        if (vi > __dadd_rn(vj, 1e-9)) v = dl;
+        else if (fabs(__dsub_rn(vi, vj)) <= 1e-9) v = flip(0.5, sg);
+        else v = 0.0;
+        break;
+      case 21: v = __dmul_rn(flip(vi, sg), vj); break;
+      case 22: v = flip(0.0, sg); break;  // the CPU engine's dyadic covariate is zero-filled
+      case 24: v = flip(P.wtab[(size_t)e * (n + 1) + ri_cj], sg); break;
+      case 25: v = flip(__dadd_rn(vi, vj), sg); break;
+      case 26: v = flip(P.wtab[(size_t)e * (n + 1) + ri_rj], sg); break;
+      case 27: v = flip(P.wtab[(size_t)e * (n + 1) + ci_cj], sg); break;
+      case 28: v = flip(P.wtab[(size_t)e * (n + 1) + ci_rj], sg); break;
+      case 29: case 30: {
+        // over h in out_j (29) or in_j (30), h != i, ascending h as the
+        // reference adds: the gw weight difference at p_h = |out_i & in_h|
+        // (29) or |out_i & out_h| (30), both precomputed for this ministep
+        const double *wr = P.wtab + (size_t)e * (n + 1);
+        const uint32_t *B = (t == 29) ? S.rowsT : S.colsT;
+        const int *pc = (t == 29) ? S.tp : S.tq;
+        double acc = 0.0;
+        for (int w = 0; w < W; ++w) {
+          uint32_t m = B[w * n + j];
+          if ((i >> 5) == w) m &= ~(1u << (i & 31));
+          while (m) {
+            const int h = (w << 5) + __ffs(m) - 1;
+            m &= m - 1;
+            const int p = pc[h];
+            acc = __dadd_rn(acc, aij ? __dsub_rn(wr[p], wr[p - 1]) : __dsub_rn(wr[p + 1], wr[p]));
+          }
+        }
+        v = flip(acc, sg);
+        break;
+      }
+      case 31: v = flip(vj >= __dsub_rn(S.p1[e], 1e-12) ? 1.0 : 0.0, sg); break;
+      default: v = 0.0; break;
+    }
+    if ((S.ety[e] == 1 && aij) || (S.ety[e] == 2 && !aij)) v = 0.0;
+    d[e] = v;
+  }
+}
+
+// Behaviour change statistic, src/libcusna_saom_cpu.cpp:103-113.
+__device__ __forceinline__ double beh_stat(int t, double dl, double zc, long long nb, double zs,
+                                           long long nh, long long ne, long long nl, double br,
+                                           double bs) {
+  double tc;
+  switch (t) {
+    case 0: return dl;
+    case 1: return __dmul_rn(__dadd_rn(__dmul_rn(2.0, zc), dl), dl);
+    case 2: return nb > 0 ? __ddiv_rn(__dmul_rn(dl, zs), (double)nb) : 0.0;
+    case 3:
+      if (nb == 0) return 0.0;
+      tc = dl > 0 ? (double)(nh - ne - nl) : (double)(nl - ne - nh);
+      return __ddiv_rn(tc, __dmul_rn(br, (double)nb));
+    case 4:
+      if (nb == 0) return 0.0;
+      tc = dl > 0 ? (double)(nh - ne - nl) : (double)(nl - ne - nh);
+      return __dsub_rn(__ddiv_rn(tc, br), __dmul_rn((double)nb, bs));
+  }
+  return 0.0;
+}
+
+}  // namespace cusna

@@ -1,0 +1,37 @@
+// saom_launch.h -- launch wrappers shared by the kernels (saom_sim.cu) and the
+// host code (saom_api.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "saom_common.cuh"
+#include "saom_kernel.cuh"
+
+namespace cusna {
+
+struct StatDesc;
+
+// Launch shape of the period kernel, chosen by the autotuner (saom_api.cu).
+struct LaunchShape {
+  int G;              // warps per chain
+  int teams_per_cta;  // chains per CTA
+  int ctas;           // grid size (persistent: ctas * teams_per_cta resident teams)
+  bool cols_in_smem;  // in-rows in shared memory (else global scratch)
+  SliceLayout lay;
+};
+
+cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const long long *unit_start,
+                          int nprob, long long total, unsigned long long *counter,
+                          uint32_t *cols_scratch, size_t cols_words, cudaStream_t st);
+int period_blocks_per_sm(int threads, size_t dyn_smem);
+cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
+                            cudaStream_t st);
+cudaError_t launch_behstats(const int *z, int n, int M, int kb, const int *bty, const uint8_t *xnet,
+                            const int *bkdist, double zbar, double brange, double bsimmean,
+                            double *out, int sms, cudaStream_t st);
+cudaError_t launch_prep_bits(const uint32_t *src, int n, int W, uint32_t *dstT, uint32_t *dstcT,
+                             int def_mode, cudaStream_t st);
+cudaError_t launch_prep_desc(const double *d64, const float *d32, size_t cnt, double *dst,
+                             cudaStream_t st);
+cudaError_t launch_fill_int(int *dst, size_t cnt, int mode, int value, cudaStream_t st);
+
+}  // namespace cusna

@@ -1,0 +1,399 @@
+// saom_sim.cu -- kernels of the GB300 SAOM period simulator: the persistent
+// period kernel, the standalone statistic kernels and the input-preparation
+// kernels. Host code (validation, memory, the C ABI) is in saom_api.cu.
+#include "saom_chain.cuh"
+#include "saom_launch.h"
+
+namespace cusna {
+
+__device__ void chain_finish(const Team &T, const DevProblem &P, const Slice &S, int c,
+                             long long dist, long long bdist, long long ms, long long msb,
+                             double t, double rho, double lam, double lamb) {
+  const int n = P.n, W = P.W, k = P.k;
+  T.sync();
+  // composition change: restore inactive actors' rows and columns to x0
+  // (src/libcusna_saom_cpu.cpp:290-291)
+  if (P.has_comp) {
+    for (int i = 0; i < n; ++i) {
+      if (!((P.inact[i >> 5] >> (i & 31)) & 1u)) continue;
+      for (int w = T.tl; w < W; w += T.L) {
+        S.rowsT[w * n + i] = P.x0T[w * n + i];
+        S.colsT[w * n + i] = P.x0cT[w * n + i];
+      }
+      T.sync();
+      const uint32_t bit = 1u << (i & 31);
+      const int wi = i >> 5;
+      for (int j = T.tl; j < n; j += T.L) {
+        if (j == i) continue;
+        S.rowsT[wi * n + j] = (S.rowsT[wi * n + j] & ~bit) | (P.x0T[wi * n + j] & bit);
+        S.colsT[wi * n + j] = (S.colsT[wi * n + j] & ~bit) | (P.x0cT[wi * n + j] & bit);
+      }
+      T.sync();
+    }
+  }
+  // dense end network (src/libcusna_saom_cpu.cpp:410-412), 4 bytes per store
+  if (P.a_ends) {
+    uint8_t *out = P.a_ends + (size_t)c * n * n;
+    const size_t nn = (size_t)n * n;
+    if ((nn & 3) == 0 && (((uintptr_t)out) & 3) == 0) {
+      uint32_t *o4 = (uint32_t *)out;
+      for (size_t q = T.tl; q < nn / 4; q += T.L) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const size_t x = 4 * q + b;
+          const int i = (int)(x / n), j = (int)(x % n);
+          v |= (uint32_t)bit_of(S.rowsT, n, i, j) << (8 * b);
+        }
+        o4[q] = v;
+      }
+    } else {
+      for (size_t x = T.tl; x < nn; x += T.L) {
+        const int i = (int)(x / n), j = (int)(x % n);
+        out[x] = (uint8_t)bit_of(S.rowsT, n, i, j);
+      }
+    }
+  }
+  // distance over kdist (:293-296)
+  long long ds = 0;
+  for (int i = T.tl; i < n; i += T.L) {
+    int cnt = 0;
+    for (int w = 0; w < W; ++w)
+      cnt += __popc((S.rowsT[w * n + i] ^ P.x0T[w * n + i]) & P.kdistT[w * n + i]);
+    if (P.actor_dist) P.actor_dist[(size_t)c * n + i] = cnt;
+    ds += cnt;
+  }
+  ds = team_sum_ll(T, ds, S.red);
+  if (P.kb > 0 && P.z_end)
+    for (int x = T.tl; x < n; x += T.L) P.z_end[(size_t)c * n + x] = S.z[x];
+  // statistics of the masked end network (A & keep) | force (:413-421)
+  if (P.stats) {
+    T.sync();
+    for (int x = T.tl; x < W * n; x += T.L) {
+      S.rowsT[x] = (S.rowsT[x] & P.keepT[x]) | P.forceT[x];
+      S.colsT[x] = (S.colsT[x] & P.keepcT[x]) | P.forcecT[x];
+    }
+    T.sync();
+    for (int x = T.tl; x < n; x += T.L) {
+      int od = 0, id = 0;
+      for (int w = 0; w < W; ++w) {
+        od += __popc(S.rowsT[w * n + x]);
+        id += __popc(S.colsT[w * n + x]);
+      }
+      S.outdeg[x] = od;
+      S.indeg[x] = id;
+    }
+    T.sync();
+    StatDesc D;
+    D.vmat = P.vmat; D.vb = P.vb; D.wtab = P.wtab; D.p1 = P.p1; D.p2 = P.p2;
+    D.vmiss = P.vmiss; D.dyn = P.dyn; D.od0 = P.od0; D.id0 = P.id0; D.type_ids = P.type_ids;
+    D.n = n; D.W = W; D.k = k; D.symflag = P.symflag;
+    network_stats_team(T, D, S.rowsT, S.colsT, S.outdeg, S.indeg, S.red, P.stats + (size_t)c * k);
+  }
+  if (T.tl == 0) {
+    if (P.dist) P.dist[c] = (int)dist;
+    if (P.dist_stat) P.dist_stat[c] = (int)ds;
+    if (P.steps) P.steps[c] = (int)ms;
+    if (P.ntim) P.ntim[c] = t;
+    if (P.scores) {
+      const double moves = (double)(ms - msb);
+      const double rate_score = P.nrate > 0 ? __dsub_rn(__ddiv_rn(moves, lam), rho)
+                                            : __dsub_rn(__ddiv_rn(moves, lam), (double)P.nact);
+      P.scores[(size_t)c * (k + 1)] = (float)rate_score;
+      for (int e = 0; e < k; ++e) P.scores[(size_t)c * (k + 1) + 1 + e] = (float)S.sc[e];
+    }
+    if (P.kb > 0) {
+      if (P.bdist) P.bdist[c] = (int)bdist;
+      if (P.bscores) {
+        P.bscores[(size_t)c * (P.kb + 1)] =
+            (float)__dsub_rn(__ddiv_rn((double)msb, lamb), (double)P.nact);
+        for (int e = 0; e < P.kb; ++e) P.bscores[(size_t)c * (P.kb + 1) + 1 + e] = (float)S.bsc[e];
+      }
+    }
+    if (P.nrate > 0 && P.rscores)
+      for (int q = 0; q < P.nrate; ++q) P.rscores[(size_t)c * P.nrate + q] = (float)S.rsc[q];
+  }
+  T.sync();
+}
+
+// Persistent period kernel: every team repeatedly takes the next chain of the
+// launch's work list (all chains of all problems) until the list is empty.
+__global__ void __launch_bounds__(512, 1)
+period_kernel(const DevProblem *__restrict__ probs, const long long *__restrict__ unit_start,
+              int nprob, long long total, unsigned long long *counter, SliceLayout lay, int G,
+              uint32_t *cols_scratch, size_t cols_words) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Team T;
+  T.G = G;
+  T.L = 32 * G;
+  const int tw = threadIdx.x / T.L;
+  T.tl = threadIdx.x % T.L;
+  T.warp = T.tl >> 5;
+  T.lane = T.tl & 31;
+  T.bar = 1 + tw;
+  const int teams_per_cta = blockDim.x / T.L;
+  const size_t slot = (size_t)blockIdx.x * teams_per_cta + tw;
+  Slice S = carve(smem + (size_t)tw * lay.bytes, lay,
+                  cols_scratch ? cols_scratch + slot * cols_words : nullptr);
+  for (;;) {
+    long long u = 0;
+    if (T.tl == 0) u = (long long)atomicAdd(counter, 1ull);
+    if (G == 1) {
+      u = __shfl_sync(kFull, u, 0);
+    } else {
+      if (T.tl == 0) ((long long *)(S.misc + 8))[0] = u;
+      T.sync();
+      u = ((long long *)(S.misc + 8))[0];
+      T.sync();
+    }
+    if (u >= total) break;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {  // last problem whose first unit is <= u
+      const int mid = (lo + hi + 1) >> 1;
+      if (unit_start[mid] <= u) lo = mid; else hi = mid - 1;
+    }
+    const DevProblem &P = probs[lo];
+    run_chain(T, P, S, (int)(u - unit_start[lo]));
+  }
+}
+
+// ---- standalone statistics (cusna_network_stats_gpu / behavior_stats_gpu) ----
+
+// One warp per network: pack the dense network into word-major rows/cols in
+// shared memory, then the same statistic code as the period kernel.
+__global__ void netstats_kernel(const uint8_t *__restrict__ a_batch, int M, StatDesc D,
+                                double *out, size_t slice_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int n = D.n, W = D.W;
+  Team T;
+  T.G = 1; T.L = 32; T.tl = threadIdx.x & 31; T.warp = 0; T.lane = T.tl; T.bar = 0;
+  const int tw = threadIdx.x >> 5;
+  unsigned char *base = smem + (size_t)tw * slice_bytes;
+  uint32_t *R = (uint32_t *)base;
+  uint32_t *Cc = R + (size_t)W * n;
+  int *od = (int *)(Cc + (size_t)W * n);
+  int *id = od + n;
+  double *red = (double *)(((uintptr_t)(id + n) + 15) & ~(uintptr_t)15);
+  for (int c = blockIdx.x * (blockDim.x >> 5) + tw; c < M; c += gridDim.x * (blockDim.x >> 5)) {
+    const uint8_t *a = a_batch + (size_t)c * n * n;
+    for (int x = T.tl; x < W * n; x += 32) {
+      const int w = x / n, r = x % n;
+      uint32_t ro = 0, co = 0;
+      for (int b = 0; b < 32; ++b) {
+        const int q = 32 * w + b;
+        if (q < n) {
+          ro |= (uint32_t)(a[(size_t)r * n + q] != 0) << b;
+          co |= (uint32_t)(a[(size_t)q * n + r] != 0) << b;
+        }
+      }
+      R[x] = ro;
+      Cc[x] = co;
+    }
+    __syncwarp();
+    for (int x = T.tl; x < n; x += 32) {
+      int o = 0, i2 = 0;
+      for (int w = 0; w < W; ++w) { o += __popc(R[w * n + x]); i2 += __popc(Cc[w * n + x]); }
+      od[x] = o;
+      id[x] = i2;
+    }
+    __syncwarp();
+    network_stats_team(T, D, R, Cc, od, id, red, out + (size_t)c * D.k);
+    __syncwarp();
+  }
+}
+
+// Behaviour statistics (src/libcusna_saom_cpu.cpp:768-817): one warp per chain.
+// Per-actor terms are formed in parallel; lane 0 adds them in actor order, and
+// the avAlt/avSim inner sums run over alters in ascending order, as the
+// reference adds them.
+__global__ void behstats_kernel(const int *__restrict__ z_batch, int n, int M, int kb,
+                                const int *__restrict__ bty, const uint8_t *__restrict__ xnet,
+                                const int *__restrict__ bkdist, double zbar, double brange,
+                                double bsimmean, double *out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, tw = threadIdx.x >> 5;
+  double *u = (double *)smem + (size_t)tw * 2 * n;
+  double *term = u + n;
+  for (int c = blockIdx.x * (blockDim.x >> 5) + tw; c < M; c += gridDim.x * (blockDim.x >> 5)) {
+    const int *z = z_batch + (size_t)c * n;
+    for (int i = lane; i < n; i += 32) {
+      const bool ok = bkdist ? bkdist[i] != 0 : true;
+      u[i] = ok ? __dsub_rn((double)z[i], zbar) : 0.0;
+    }
+    __syncwarp();
+    for (int e = 0; e < kb; ++e) {
+      const int t = bty[e];
+      if (t == 2 || t == 3 || t == 4) {
+        for (int i = lane; i < n; i += 32) {
+          const uint8_t *xr = xnet + (size_t)i * n;
+          const bool oki = bkdist ? bkdist[i] != 0 : true;
+          double s = 0.0, od = 0.0, nb = 0.0;
+          if (t == 2) {
+            for (int j = 0; j < n; ++j) if (xr[j]) { od += 1.0; s = __dadd_rn(s, u[j]); }
+            term[i] = od <= 0.0 ? 0.0 : __dmul_rn(u[i], __ddiv_rn(s, od));
+            if (od <= 0.0) term[i] = -0.0;  // marker: skipped actor
+          } else {
+            for (int j = 0; j < n; ++j) {
+              if (!xr[j]) continue;
+              const bool okj = bkdist ? bkdist[j] != 0 : true;
+              if (okj) {
+                nb += 1.0;
+                s = __dadd_rn(s, __dsub_rn(1.0, __ddiv_rn(fabs(__dsub_rn(u[i], u[j])), brange)));
+              }
+            }
+            s = __dsub_rn(s, __dmul_rn(nb, bsimmean));
+            if (t == 3) s = nb > 0.0 ? __ddiv_rn(s, nb) : 0.0;
+            term[i] = oki ? s : -0.0;
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        double acc = 0.0;
+        if (t == 0) for (int i = 0; i < n; ++i) acc = __dadd_rn(acc, u[i]);
+        else if (t == 1) for (int i = 0; i < n; ++i) acc = __dadd_rn(acc, __dmul_rn(u[i], u[i]));
+        else if (t >= 2 && t <= 4)
+          for (int i = 0; i < n; ++i) {
+            // skipped actors contribute nothing (the reference `continue`s);
+            // adding -0.0 leaves every partial sum unchanged
+            acc = __dadd_rn(acc, term[i]);
+          }
+        out[(size_t)c * kb + e] = acc;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ---- input preparation ------------------------------------------------------
+
+// Row-major n*W bit rows -> word-major W*n; optionally also the transposed
+// matrix (in-rows) word-major. def_offdiag: when src is null, fill with the
+// all-ones off-diagonal matrix (the reference's default masks).
+__global__ void prep_bits_kernel(const uint32_t *src, int n, int W, uint32_t *dstT,
+                                 uint32_t *dstcT, int def_mode) {
+  const size_t total = (size_t)W * n;
+  for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+       x += (size_t)gridDim.x * blockDim.x) {
+    const int w = (int)(x / n), r = (int)(x % n);
+    uint32_t v = 0, vc = 0;
+    for (int b = 0; b < 32; ++b) {
+      const int q = 32 * w + b;
+      if (q >= n) break;
+      int bit_rq, bit_qr;
+      if (src) {
+        bit_rq = (src[(size_t)r * W + w] >> b) & 1;                 // a[r][q]
+        bit_qr = (src[(size_t)q * W + (r >> 5)] >> (r & 31)) & 1;  // a[q][r]
+      } else {
+        bit_rq = bit_qr = def_mode == 1 ? (q != r) : 0;
+      }
+      v |= (uint32_t)bit_rq << b;
+      vc |= (uint32_t)bit_qr << b;
+    }
+    if (dstT) dstT[x] = v;
+    if (dstcT) dstcT[x] = vc;
+  }
+}
+
+// float64 descriptor with the reference's precedence: the *64 array if given,
+// else the float array promoted, else zeros (src/libcusna_saom_cpu.cpp:337-350).
+__global__ void prep_desc_kernel(const double *d64, const float *d32, size_t cnt, double *dst) {
+  for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < cnt;
+       x += (size_t)gridDim.x * blockDim.x)
+    dst[x] = d64 ? d64[x] : (d32 ? (double)d32[x] : 0.0);
+}
+
+__global__ void fill_int_kernel(int *dst, size_t cnt, int mode, int value) {
+  for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < cnt;
+       x += (size_t)gridDim.x * blockDim.x)
+    dst[x] = mode == 0 ? value : (int)x;  // mode 1: identity (act)
+}
+
+// ---- launch wrappers used by the host code ----------------------------------
+
+int period_blocks_per_sm(int threads, size_t dyn_smem) {
+  if (cudaFuncSetAttribute(period_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)dyn_smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, period_kernel, threads, dyn_smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return b;
+}
+
+cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const long long *unit_start,
+                          int nprob, long long total, unsigned long long *counter,
+                          uint32_t *cols_scratch, size_t cols_words, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(period_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sh.lay.bytes * sh.teams_per_cta));
+  if (e != cudaSuccess) return e;
+  period_kernel<<<sh.ctas, 32 * sh.G * sh.teams_per_cta, sh.lay.bytes * sh.teams_per_cta, st>>>(
+      probs, unit_start, nprob, total, counter, sh.lay, sh.G, cols_scratch, cols_words);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
+                            cudaStream_t st) {
+  const size_t slice = al16((size_t)2 * D.W * D.n * 4 + (size_t)2 * D.n * 4) + 32 * 8 + 64;
+  int warps = (int)((200 * 1024) / slice);
+  if (warps > 8) warps = 8;
+  if (warps < 1) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(netstats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(slice * warps));
+  if (e != cudaSuccess) return e;
+  int blocks = (M + warps - 1) / warps;
+  if (blocks > 4 * sms) blocks = 4 * sms;
+  netstats_kernel<<<blocks, 32 * warps, slice * warps, st>>>(a, M, D, out, slice);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_behstats(const int *z, int n, int M, int kb, const int *bty, const uint8_t *xnet,
+                            const int *bkdist, double zbar, double brange, double bsimmean,
+                            double *out, int sms, cudaStream_t st) {
+  const size_t per = (size_t)2 * n * 8;
+  int warps = (int)((200 * 1024) / per);
+  if (warps > 8) warps = 8;
+  if (warps < 1) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(behstats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(per * warps));
+  if (e != cudaSuccess) return e;
+  int blocks = (M + warps - 1) / warps;
+  if (blocks > 4 * sms) blocks = 4 * sms;
+  behstats_kernel<<<blocks, 32 * warps, per * warps, st>>>(z, n, M, kb, bty, xnet, bkdist, zbar,
+                                                           brange, bsimmean, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prep_bits(const uint32_t *src, int n, int W, uint32_t *dstT, uint32_t *dstcT,
+                             int def_mode, cudaStream_t st) {
+  const size_t total = (size_t)W * n;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 1024) blocks = 1024;
+  if (blocks < 1) blocks = 1;
+  prep_bits_kernel<<<blocks, 256, 0, st>>>(src, n, W, dstT, dstcT, def_mode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prep_desc(const double *d64, const float *d32, size_t cnt, double *dst,
+                             cudaStream_t st) {
+  if (cnt == 0) return cudaSuccess;
+  int blocks = (int)((cnt + 255) / 256);
+  if (blocks > 1024) blocks = 1024;
+  prep_desc_kernel<<<blocks, 256, 0, st>>>(d64, d32, cnt, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_int(int *dst, size_t cnt, int mode, int value, cudaStream_t st) {
+  if (cnt == 0) return cudaSuccess;
+  int blocks = (int)((cnt + 255) / 256);
+  if (blocks > 1024) blocks = 1024;
+  fill_int_kernel<<<blocks, 256, 0, st>>>(dst, cnt, mode, value);
+  return cudaGetLastError();
+}
+
+}  // namespace cusna

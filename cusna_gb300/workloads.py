@@ -1,0 +1,206 @@
+"""Seeded synthetic workloads of the period simulator.
+
+The reference's benchmark panel data are not used. Seeded synthetic panels
+with the published shapes, sizes and densities stand in for them:
+
+  c2_period()   n=200, 4096 chains, 8 evaluation effects, unconditional
+  c4_period()   n=1000, 1024 chains, network-behaviour co-evolution
+  c1_panel()    n=50, 3 waves (waves 2-3 simulated from a seed)
+  parity_case() small problems covering every effect type and struct option
+
+All networks have a zero diagonal; covariates are rounded to float32 and
+centred in float64 as R/effects.R:139-147 centres them.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import data as D
+from . import effects as E
+from .glue import PeriodInputs
+
+
+def bernoulli_net(n: int, p: float, seed: int) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = (rng.random((n, n)) < p).astype(np.uint8)
+    np.fill_diagonal(a, 0)
+    return a
+
+
+def normal_cov(n: int, seed: int) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.standard_normal(n).astype(np.float32).astype(np.float64)
+
+
+def period_inputs(x0, effects, p: int = 1, beh=None, z_start=None, beh_effects=None,
+                  conditional=0, target_dist=0, symflag=0) -> PeriodInputs:
+    """Descriptors of one period from effect specs (R/mom.R:62-76 conventions)."""
+    n = np.asarray(x0).shape[0]
+    pe = E.prepare_effects_v2(effects, n, p, beh, z_start)
+    inp = PeriodInputs(x0=np.asarray(x0), type_ids=pe.type_ids, vmat=pe.vmat,
+                       wtab=E.effect_wtabs(effects, n), vb=pe.v_dyn, p1=pe.p1, p2=pe.p2,
+                       vmiss=pe.vmiss, dyn_flags=pe.dyn_flags, dyc_idx=pe.dyc_idx,
+                       int_idx=E.interaction_comp_idx(effects) if any(E.is_interaction(e) for e in effects) else None,
+                       etypes=E.effect_etypes(effects),
+                       conditional=conditional, target_dist=target_dist, symflag=symflag)
+    if beh_effects:
+        inp.bty = np.array([e.type_id for e in beh_effects], dtype=np.int32)
+        inp.z0 = np.asarray(z_start if z_start is not None else beh.imputed[:, p - 1]).astype(np.int32)
+        inp.bkdist = D.beh_kmask_dist(beh, p).astype(np.int32)
+        inp.zmin, inp.zmax = beh.zmin, beh.zmax
+        inp.zbar, inp.brange, inp.bsimmean = beh.overall_mean, beh.range, beh.sim_mean
+    return inp
+
+
+# ---- C2: batched plain period simulation ------------------------------------
+C2_THETA = np.array([-2.8, 1.8, 0.3, -0.1, 0.05, 0.2, 0.1, 0.8])
+C2_EFFECTS = ["density", "recip", "transTrip", "cycle3", "inPop", "egoX", "altX", "simX"]
+
+
+def c2_period(n: int = 200, M: int = 4096):
+    """(PeriodInputs, M, seed, lam, theta) for the n=200 covariate workload."""
+    x0 = bernoulli_net(n, 0.03, seed=2)
+    cov = normal_cov(n, seed=3)
+    effs = [E.make_effect_spec(nm) for nm in C2_EFFECTS[:5]]
+    effs += [E.make_effect_spec(nm, cov) for nm in C2_EFFECTS[5:]]
+    return period_inputs(x0, effs), M, 42, 8.0, C2_THETA.copy()
+
+
+# ---- C4: network-behaviour co-evolution ------------------------------------
+C4_THETA = np.array([-3.0, 2.0, 0.3, 0.1, 0.1, 0.5])
+C4_THETAB = np.array([0.2, -0.1, 0.5])
+
+
+def c4_period(n: int = 1000, M: int = 1024):
+    """(PeriodInputs, M, seed, lam, theta, lamb, thetab) for n=1000 co-evolution.
+    Behaviour starts uniform on 1..5; its summaries (mean, range, similarity
+    mean) are those of the start wave."""
+    x0 = bernoulli_net(n, 0.008, seed=5)
+    rng = np.random.Generator(np.random.PCG64(6))
+    z = rng.integers(1, 6, size=n).astype(np.float64)
+    beh = D.build_behavior_data(np.stack([z, z], axis=1), n, 2)
+    effs = [E.make_effect_spec(nm) for nm in ("density", "recip", "transTrip")]
+    effs += [E.make_effect_spec(nm, dyn=True) for nm in ("egoX", "altX", "simX")]
+    bef = [E.make_beh_effect_spec(nm) for nm in ("linear", "quad", "avAlt")]
+    inp = period_inputs(x0, effs, 1, beh, D.beh_values_less_missing_starts(beh, 1), bef)
+    inp.z0 = beh.imputed[:, 0].astype(np.int32)
+    return inp, M, 77, 4.0, C4_THETA.copy(), 2.0, C4_THETAB.copy()
+
+
+# ---- parity cases -----------------------------------------------------------
+
+def _rng(seed):
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+ALL_NET_TYPES = list(range(0, 32))  # 0..31; 32 = interaction built separately
+
+
+def parity_case(kind: str, seed: int = 0, n: int = 40, M: int = 6):
+    """Small problems for exact GPU-vs-CPU comparisons. Returns a dict with the
+    PeriodInputs and the run arguments (M, seed, lam, theta, lamb, thetab)."""
+    r = _rng(1000 + seed)
+    x0 = bernoulli_net(n, 0.08, seed=seed + 17)
+    cov = np.round(r.standard_normal(n), 3)
+    bcov = (r.random(n) < 0.5).astype(np.float64)
+    out = dict(M=M, seed=int(r.integers(1, 2**62)), lam=float(r.uniform(3, 8)), lamb=0.0,
+               thetab=None)
+    if kind == "baseline":
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip")]
+        theta = np.array([-2.0, 0.8, 0.15])
+        inp = period_inputs(x0, effs)
+    elif kind == "covariate":
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip", "cycle3", "inPop")]
+        effs += [E.make_effect_spec(x, cov) for x in ("egoX", "altX", "simX")]
+        effs += [E.make_effect_spec("sameX", bcov)]
+        theta = np.array([-2.2, 1.2, 0.2, -0.1, 0.05, 0.2, 0.1, 0.7, 0.3])
+        inp = period_inputs(x0, effs)
+    elif kind == "structural":
+        names = ["density", "recip", "transTrip", "cycle3", "inPop", "transTies", "transRecTrip",
+                 "inPopSqrt", "outPop", "outPopSqrt", "inAct", "inActSqrt", "outAct",
+                 "outActSqrt", "outTrunc", "reciAct", "transTriads"]
+        effs = [E.make_effect_spec(x) for x in names]
+        theta = np.concatenate([[-1.5, 0.8, 0.1], r.uniform(-0.08, 0.08, len(names) - 3)])
+        inp = period_inputs(x0, effs)
+    elif kind == "gw":
+        names = ["density", "recip", "gwesp", "gwespFB", "gwespBF", "gwespBB", "gwdspFF",
+                 "gwdspFB"]
+        effs = [E.make_effect_spec(x) for x in names]
+        theta = np.array([-1.8, 0.7, 0.3, 0.2, -0.1, 0.1, -0.05, -0.05])
+        inp = period_inputs(x0, effs)
+    elif kind == "covariate_all":
+        effs = [E.make_effect_spec("density")]
+        for x in ("egoX", "altX", "simX", "sameX", "higher", "egoXaltX", "egoPlusAltX"):
+            effs.append(E.make_effect_spec(x, cov if x != "sameX" else bcov))
+        effs.append(E.make_effect_spec("altRThresholdX", cov, parm=0))
+        theta = np.concatenate([[-2.0], r.uniform(-0.3, 0.3, len(effs) - 1)])
+        inp = period_inputs(x0, effs)
+    elif kind == "interaction":
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip")]
+        effs += [E.make_effect_spec("egoX", cov)]
+        effs += [E.make_interaction_spec([1, 3]), E.make_interaction_spec([0, 2, 3])]
+        theta = np.array([-2.0, 1.0, 0.2, 0.1, 0.3, -0.05])
+        inp = period_inputs(x0, effs)
+    elif kind == "typed":
+        effs = [E.make_effect_spec("density"), E.make_effect_spec("recip"),
+                E.make_effect_spec("egoPlusAltX", cov, etype="creation"),
+                E.make_effect_spec("egoPlusAltX", cov, etype="endow")]
+        theta = np.array([-2.0, 1.0, 0.2, -0.3])
+        inp = period_inputs(x0, effs)
+    elif kind == "coevol":
+        z = r.integers(1, 6, size=(n, 2)).astype(np.float64)
+        beh = D.build_behavior_data(z, n, 2)
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip")]
+        effs += [E.make_effect_spec(x, dyn=True) for x in ("egoX", "altX", "simX")]
+        bef = [E.make_beh_effect_spec(x) for x in ("linear", "quad", "avAlt", "avSim", "totSim")]
+        inp = period_inputs(x0, effs, 1, beh, D.beh_values_less_missing_starts(beh, 1), bef)
+        theta = np.array([-2.0, 0.8, 0.2, 0.1, -0.1, 0.5])
+        out.update(lamb=2.5, thetab=np.array([0.2, -0.1, 0.4, 0.3, -0.2]))
+    elif kind == "conditional":
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip")]
+        theta = np.array([-2.0, 0.9, 0.2])
+        inp = period_inputs(x0, effs, conditional=1, target_dist=int(0.6 * n))
+        out["lam"] = 1.0
+    elif kind == "masks":
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip", "outTrunc")]
+        effs[3].parm = 3.0
+        theta = np.array([-1.8, 0.9, 0.2, 0.1])
+        inp = period_inputs(x0, effs)
+        off = ~np.eye(n, dtype=bool)
+        inp.kdist = (r.random((n, n)) < 0.9) & off
+        inp.perm = (r.random((n, n)) < 0.85) & off
+        inp.keep = (r.random((n, n)) < 0.9) & off
+        inp.force = (r.random((n, n)) < 0.02) & off
+        inp.maxdegree = 6
+        inp.sim_start = x0 & (r.random((n, n)) < 0.9)
+        inp.od0 = x0.sum(axis=1)
+        inp.id0 = x0.sum(axis=0)
+    elif kind == "composition":
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip")]
+        theta = np.array([-2.0, 0.8, 0.2])
+        inp = period_inputs(x0, effs)
+        inactive = r.random(n) < 0.15
+        act = np.concatenate([np.nonzero(~inactive)[0], np.nonzero(inactive)[0]])
+        inp.act, inp.nact, inp.inactive = act.astype(np.int32), int((~inactive).sum()), inactive
+    elif kind == "symmetric":
+        a = np.triu(x0, 1)
+        x0s = (a | a.T).astype(np.uint8)
+        effs = [E.make_effect_spec(x) for x in ("density", "transTriads", "gwesp")]
+        theta = np.array([-1.5, 0.2, 0.3])
+        inp = period_inputs(x0s, effs, symflag=1)
+    elif kind == "rates":
+        effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip")]
+        theta = np.array([-2.0, 0.8, 0.2])
+        inp = period_inputs(x0, effs)
+        inp.rkind = np.array([0, 1, 2], dtype=np.int32)
+        inp.ralpha = np.array([0.3, 0.05, -0.04], dtype=np.float32)
+        inp.ru = np.stack([cov, np.zeros(n), np.zeros(n)]).astype(np.float32)
+    else:
+        raise ValueError(kind)
+    out["inp"] = inp
+    out["theta"] = theta
+    return out
+
+
+PARITY_KINDS = ["baseline", "covariate", "structural", "gw", "covariate_all", "interaction",
+                "typed", "coevol", "conditional", "masks", "composition", "symmetric", "rates"]
