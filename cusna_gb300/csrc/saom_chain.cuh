@@ -278,7 +278,9 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
           }
         }
         S.fbuf[j] = f;
-        if (ok) {
+        // a NaN predictor never raises the maximum (the reference compares
+        // f > lmax) and is never chosen (its Gumbel key compares false)
+        if (ok && !isnan(f)) {
           const long long kf = dkey(f);
           kmax = kf > kmax ? kf : kmax;
         }

@@ -162,7 +162,9 @@ def effect_sim_params(spec: EffectSpec) -> tuple[float, float]:
             d = 1.0 - np.abs(x[:, None] - x[None, :]) / rng
             tot += float(d.sum()) - len(x)
             cnt += len(x) * (len(x) - 1)
-    return 1.0 / rng, (tot / cnt if cnt > 0 else 0.0)
+    with np.errstate(divide="ignore"):   # R: 1/0 = Inf
+        inv = np.float64(1.0) / np.float64(rng)
+    return float(inv), (tot / cnt if cnt > 0 else 0.0)
 
 
 def rate_cov_values(spec: dict, p: int = 1) -> np.ndarray:
@@ -200,7 +202,8 @@ def prepare_effects_v2(effects, n: int, p: int = 1, beh=None, z_start=None) -> D
         if t == EFF_SIMX:
             if e.dyn:
                 if beh is not None:
-                    p1[idx] = 1.0 / beh.range
+                    with np.errstate(divide="ignore"):   # R: 1/0 = Inf
+                        p1[idx] = np.float64(1.0) / np.float64(beh.range)
                     p2[idx] = beh.sim_mean
             else:
                 p1[idx], p2[idx] = effect_sim_params(e)
