@@ -1,0 +1,358 @@
+"""Benchmark of the GB300 SAOM period simulator.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl gb300|reference]
+                    [--workload c2|c4] [--chains M]
+
+Metric: ministeps/s (network plus behaviour ministeps summed over all chains,
+divided by time), on the batched plain period-simulation workload: n=200
+actors, 4096 chains, 8 effects (density, recip, transTrip, cycle3, inPop,
+covariate ego/alter/similarity), rate 8, unconditional. One step is one
+simulator call over all chains of the period.
+
+  value  device-resident inputs (libcusna device-pointer mode), the summed
+         CUDA-event time of the K steps; L2 is flushed (256 MiB write) between
+         steps, outside the timed events
+  e2e    the reference-facing call cusna_saom_simulate_period with pinned host
+         buffers: host->device copies, the kernels and the device->host result
+         copy inside the timed region, host wall clock
+Under torchrun each rank simulates its own chains (chain offset rank*M, one
+Philox key), so the work per GPU is fixed (weak scaling); value is the sum of
+the ranks' ministeps over the slowest rank's time.
+
+--impl reference times the reference's CPU engine on the host cores on a
+bounded sample of the same workload (oracle/_ref where it was compiled from
+the reference sources, else the oracle's C restatement).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from cusna_gb300 import workloads as WL  # noqa: E402
+from cusna_gb300.glue import marshal_period, result_dict  # noqa: E402
+
+WORKLOADS = {
+    "c2": "n=200 actors, wave-1 density 0.03, 8 effects (density, recip, transTrip, cycle3, "
+          "inPop, egoX, altX, simX of a N(0,1) covariate), rate 8, unconditional period",
+    "c4": "n=1000 actors, wave-1 density 0.008, network effects density, recip, transTrip, "
+          "behaviour ego/alter/similarity; behaviour 1..5 with linear, quad, avAlt; rates 4/2",
+}
+
+
+def workload(name, M):
+    if name == "c2":
+        inp, M, seed, lam, theta = WL.c2_period(M=M)
+        return inp, M, seed, lam, theta, 0.0, None
+    inp, M, seed, lam, theta, lamb, thetab = WL.c4_period(M=M)
+    return inp, M, seed, lam, theta, lamb, thetab
+
+
+def fp64_flops_per_network_ministep(n, k):
+    """Algorithmic float64 work of one network ministep: per alter, the linear
+    predictor (k multiplies + k adds), the log-sum-exp shift, exponential and
+    sum (1 + 10 + 1, an exponential counted as 10 flops) and the k weighted
+    score sums (k FMAs = 2k flops)."""
+    return n * (4 * k + 12)
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self, device_index=0):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return None
+        rows = [[x.strip() for x in r] for r in rows if len(r) >= 9 and r[0].strip() == str(device_index)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        mx = float(rows[0][2])
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    """--impl reference: the reference CPU engine on the host cores."""
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    import oracle
+    kind = "reference" if oracle.reference_available() else "port"
+    eng = oracle.Oracle(kind)
+    threads = eng.max_threads() if kind == "port" else (os.cpu_count() or 1)
+    inp, M, seed, lam, theta, lamb, thetab = workload(args.workload, args.chains)
+    sample = args.cpu_chains or (256 if args.workload == "c2" else 8)
+    times, steps = [], []
+    for it in range(args.warmup + args.steps):
+        m = marshal_period(inp, sample, seed + it, lam, theta, lamb=lamb, thetab=thetab)
+        t0 = time.perf_counter()
+        out = eng.simulate(m, threads=threads)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            steps.append(int(out["steps"].sum()))
+    val = sum(steps) / sum(times)
+    line = {
+        "impl": "reference", "metric": "ministeps/s", "value": val, "unit": "ministeps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload]}",
+                   "chains_per_step": sample, "chains_full_workload": M},
+        "cpu_baseline": {"value": val, "unit": "ministeps/s", "cores": threads, "kind": kind,
+                         "sample": f"{sample} of the workload's {M} chains per step"},
+        "e2e": {"value": val, "unit": "ministeps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def pinned_copy(m, torch):
+    """Move every host array of a marshalled period into pinned memory."""
+    pinned = {}
+    for name, arr in m.keep.items():
+        a = np.ascontiguousarray(arr)
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = a.view(np.uint8).reshape(-1)
+        pinned[name] = (t, a.dtype, a.shape)
+        field = name[4:] if name.startswith("out_") else name
+        target = m.result if name.startswith("out_") else m.problem
+        setattr(target, field, t.data_ptr())
+    return pinned
+
+
+def device_copy(m, torch, dev):
+    dmap = {}
+    for name, arr in m.keep.items():
+        a = np.ascontiguousarray(arr)
+        t = torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).to(dev)
+        dmap[name] = t
+        field = name[4:] if name.startswith("out_") else name
+        target = m.result if name.startswith("out_") else m.problem
+        setattr(target, field, t.data_ptr())
+    return dmap
+
+
+def cpu_baseline(args, inp, M, seed, lam, theta, lamb, thetab):
+    import oracle
+    kind = "reference" if oracle.reference_available() else "port"
+    eng = oracle.Oracle(kind)
+    threads = eng.max_threads() if kind == "port" else (os.cpu_count() or 1)
+    sample = args.cpu_chains or (512 if args.workload == "c2" else 8)
+    m = marshal_period(inp, sample, seed, lam, theta, lamb=lamb, thetab=thetab)
+    t0 = time.perf_counter()
+    out = eng.simulate(m, threads=threads)
+    dt = time.perf_counter() - t0
+    st = int(out["steps"].sum())
+    return {"value": st / dt, "unit": "ministeps/s", "cores": threads, "kind": kind,
+            "sample": f"{sample} of the {M} chains ({st} ministeps, {dt:.1f} s)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--chains", type=int, default=0)
+    ap.add_argument("--cpu-chains", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.chains == 0:
+        args.chains = 4096 if args.workload == "c2" else 1024
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from cusna_gb300 import build as B
+    from cusna_gb300 import sim as G
+    from cusna_gb300.abi import load_library
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B.build()
+    lib = load_library()
+
+    inp, M, seed, lam, theta, lamb, thetab = workload(args.workload, args.chains)
+    n, k = inp.n, inp.k
+    # device-resident inputs and outputs
+    m_dev = marshal_period(inp, M, seed, lam, theta, lamb=lamb, thetab=thetab)
+    dmap = device_copy(m_dev, torch, dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(opts):
+        G.simulate_ex(m_dev, opts)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step(G.options(device_ptrs=True, chain_offset=rank * M, stream=stream.cuda_stream))
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    kernel_ms, launches = [], []
+    clk_path = os.path.join(tempfile.gettempdir(), f"cusna_clocks_{os.getpid()}.csv")
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(clk_path) as clocks:
+        t_wall0 = time.perf_counter()
+        for s in range(args.steps):
+            flush.zero_()
+            o = G.options(device_ptrs=True, chain_offset=rank * M, stream=stream.cuda_stream)
+            ev[s][0].record(stream)
+            step(o)
+            ev[s][1].record(stream)
+            kernel_ms.append(o.elapsed_ms)
+            launches.append(o.launches)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    steps_out = dmap["out_steps"].cpu().numpy().view(np.int32)
+    ministeps = int(steps_out.sum())           # identical every step (fixed seed)
+    msb_frac = 0.0
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        t = torch.tensor([total_ms, float(ministeps)], device=dev, dtype=torch.float64)
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        total_ms, all_ministeps = float(tmax[0]), float(t[1])
+    else:
+        all_ministeps = float(ministeps)
+    value = all_ministeps * args.steps / (total_ms / 1e3)
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- float64 roofline of the period kernel ---------------------------
+    fp64_peak = C.c_double(0.0)
+    lib.cusna_measure_fp64_tflops(C.byref(fp64_peak))
+    net_steps = ministeps
+    if inp.kb > 0:
+        # behaviour ministeps do no per-alter work; count network ministeps only
+        m_h = marshal_period(inp, min(M, 64), seed, lam, theta, lamb=lamb, thetab=thetab)
+        r_h = G.simulate(m_h)
+        tot = r_h["steps"].sum()
+        # behaviour ministeps from the behaviour rate score: msb = (score + nact) * lamb
+        beh = np.round((r_h["bscores"][:, 0].astype(np.float64) + inp.n) * lamb)
+        net_steps = int(ministeps * (1.0 - float(beh.sum()) / float(tot)))
+    flops = fp64_flops_per_network_ministep(n, k) * net_steps
+    kern_avg_ms = float(np.mean(kernel_ms))
+    achieved = flops / (kern_avg_ms / 1e3) / 1e12
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak.value,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak.value if fp64_peak.value else None,
+                "traffic": None,
+                "peak_source": "measured in this run: float64 FMA loop (cusna_measure_fp64_tflops)",
+                "algorithmic_flops_per_launch": flops,
+                "kernel_ms": kern_avg_ms}
+
+    # ---- end to end through the reference-facing C ABI ---------------------
+    e2e = None
+    if not args.no_e2e:
+        m_h = marshal_period(inp, M, seed, lam, theta, lamb=lamb, thetab=thetab)
+        pinned = pinned_copy(m_h, torch)
+        h2d = sum(t.numel() for nm, (t, _, _) in pinned.items() if not nm.startswith("out_"))
+        d2h = sum(t.numel() for nm, (t, _, _) in pinned.items() if nm.startswith("out_"))
+        P, R = C.byref(m_h.problem), C.byref(m_h.result)
+        for _ in range(max(1, args.warmup)):
+            assert lib.cusna_saom_simulate_period(P, R) == 0
+        walls = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            assert lib.cusna_saom_simulate_period(P, R) == 0
+            walls.append(time.perf_counter() - t0)
+        e2e = {"value": ministeps / float(np.mean(walls)), "unit": "ministeps/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": 1e3 * float(np.mean(walls))}
+
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        cpu = cpu_baseline(args, inp, M, seed, lam, theta, lamb, thetab)
+
+    clk = clocks.summary(local)
+    line = {
+        "metric": "ministeps/s", "value": value, "unit": "ministeps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload]}",
+                   "chains_per_gpu": M, "n": n, "effects": k,
+                   "ministeps_per_step": all_ministeps,
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                   "parallelism": f"replicas x{ws}, chains sharded by chain offset"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(sum(launches)), "clocks": clk,
+        "wall_s_timed_region": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -68,7 +68,7 @@ class GpuOptions(C.Structure):
     _fields_ = [
         ("struct_version", C.c_int32), ("device_ptrs", C.c_int32),
         ("chain_offset", C.c_uint32), ("warps_per_chain", C.c_int32),
-        ("chains_per_cta", C.c_int32), ("reserved0", C.c_int32),
+        ("chains_per_cta", C.c_int32), ("launches", C.c_int32),
         ("stream", _p), ("elapsed_ms", C.c_double), ("ministeps", C.c_int64),
     ]
 
@@ -116,6 +116,8 @@ def load_library(path: str | None = None):
     lib.cusna_behavior_stats_gpu.argtypes = [_p, i32, i32, i32, _p, _p, _p,
                                              C.c_double, C.c_double, C.c_double, _p]
     lib.cusna_behavior_stats_gpu.restype = i32
+    lib.cusna_measure_fp64_tflops.argtypes = [P(C.c_double)]
+    lib.cusna_measure_fp64_tflops.restype = i32
     if path is None:
         _lib = lib
     return lib
@@ -126,7 +128,7 @@ EXPORTED_SYMBOLS = [
     "cusna_saom_simulate_period", "cusna_pack_bits", "cusna_philox4x32",
     "cusna_abi_version", "cusna_version_string", "cusna_has_cuda", "cusna_last_error",
     "cusna_saom_simulate_period_ex", "cusna_saom_simulate_batch",
-    "cusna_network_stats_gpu", "cusna_behavior_stats_gpu",
+    "cusna_network_stats_gpu", "cusna_behavior_stats_gpu", "cusna_measure_fp64_tflops",
 ]
 
 

@@ -555,6 +555,7 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
   struct Restore { cudaStream_t &ref; cudaStream_t v; ~Restore() { ref = v; } } restore{g_ctx.stream, own};
 
   const uint32_t off0 = opts ? opts->chain_offset : 0;
+  const long long launches0 = kernel_launches();
   int nmax = 0, Wmax = 0, kmax = 0, kbmax = 0, nrmax = 0;
   bool tp = false, gw = false, tq = false;
   long long total = 0;
@@ -608,6 +609,7 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
     opts->elapsed_ms = ms;
     opts->warps_per_chain = sh.G;
     opts->chains_per_cta = sh.teams_per_cta;
+    opts->launches = (int32_t)(kernel_launches() - launches0);
   }
   return CUSNA_OK;
 }

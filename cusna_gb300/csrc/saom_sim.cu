@@ -311,6 +311,14 @@ __global__ void fill_int_kernel(int *dst, size_t cnt, int mode, int value) {
 
 // ---- launch wrappers used by the host code ----------------------------------
 
+// Kernels launched by this thread (reported through cusna_gpu_options).
+thread_local long long g_launches = 0;
+long long kernel_launches() { return g_launches; }
+static cudaError_t counted(cudaError_t e) {
+  if (e == cudaSuccess) ++g_launches;
+  return e;
+}
+
 int period_blocks_per_sm(int threads, size_t dyn_smem) {
   if (cudaFuncSetAttribute(period_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)dyn_smem) != cudaSuccess) {
@@ -334,7 +342,7 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
   if (e != cudaSuccess) return e;
   period_kernel<<<sh.ctas, 32 * sh.G * sh.teams_per_cta, sh.lay.bytes * sh.teams_per_cta, st>>>(
       probs, unit_start, nprob, total, counter, sh.lay, sh.G, cols_scratch, cols_words);
-  return cudaGetLastError();
+  return counted(cudaGetLastError());
 }
 
 cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
@@ -349,7 +357,7 @@ cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *
   int blocks = (M + warps - 1) / warps;
   if (blocks > 4 * sms) blocks = 4 * sms;
   netstats_kernel<<<blocks, 32 * warps, slice * warps, st>>>(a, M, D, out, slice);
-  return cudaGetLastError();
+  return counted(cudaGetLastError());
 }
 
 cudaError_t launch_behstats(const int *z, int n, int M, int kb, const int *bty, const uint8_t *xnet,
@@ -366,7 +374,7 @@ cudaError_t launch_behstats(const int *z, int n, int M, int kb, const int *bty, 
   if (blocks > 4 * sms) blocks = 4 * sms;
   behstats_kernel<<<blocks, 32 * warps, per * warps, st>>>(z, n, M, kb, bty, xnet, bkdist, zbar,
                                                            brange, bsimmean, out);
-  return cudaGetLastError();
+  return counted(cudaGetLastError());
 }
 
 cudaError_t launch_prep_bits(const uint32_t *src, int n, int W, uint32_t *dstT, uint32_t *dstcT,
@@ -376,7 +384,7 @@ cudaError_t launch_prep_bits(const uint32_t *src, int n, int W, uint32_t *dstT, 
   if (blocks > 1024) blocks = 1024;
   if (blocks < 1) blocks = 1;
   prep_bits_kernel<<<blocks, 256, 0, st>>>(src, n, W, dstT, dstcT, def_mode);
-  return cudaGetLastError();
+  return counted(cudaGetLastError());
 }
 
 cudaError_t launch_prep_desc(const double *d64, const float *d32, size_t cnt, double *dst,
@@ -385,7 +393,7 @@ cudaError_t launch_prep_desc(const double *d64, const float *d32, size_t cnt, do
   int blocks = (int)((cnt + 255) / 256);
   if (blocks > 1024) blocks = 1024;
   prep_desc_kernel<<<blocks, 256, 0, st>>>(d64, d32, cnt, dst);
-  return cudaGetLastError();
+  return counted(cudaGetLastError());
 }
 
 cudaError_t launch_fill_int(int *dst, size_t cnt, int mode, int value, cudaStream_t st) {
@@ -393,7 +401,7 @@ cudaError_t launch_fill_int(int *dst, size_t cnt, int mode, int value, cudaStrea
   int blocks = (int)((cnt + 255) / 256);
   if (blocks > 1024) blocks = 1024;
   fill_int_kernel<<<blocks, 256, 0, st>>>(dst, cnt, mode, value);
-  return cudaGetLastError();
+  return counted(cudaGetLastError());
 }
 
 }  // namespace cusna

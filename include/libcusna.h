@@ -208,7 +208,7 @@ typedef struct cusna_gpu_options {
                                   GPUs with identical results                  */
     int32_t  warps_per_chain;  /* 0 = autotuned                               */
     int32_t  chains_per_cta;   /* 0 = autotuned                               */
-    int32_t  reserved0;
+    int32_t  launches;         /* out: kernels this call launched             */
     void    *stream;           /* cudaStream_t to run on (NULL = the library's
                                   own per-thread stream)                       */
     double   elapsed_ms;       /* out: device time of the simulation kernels  */
@@ -248,6 +248,11 @@ CUSNA_API cusna_status cusna_behavior_stats_gpu(
     const int32_t *z_batch, int32_t n, int32_t M, int32_t kb,
     const int32_t *bty, const uint8_t *xnet, const int32_t *bkdist,
     double zbar, double brange, double bsimmean, double *out);
+
+/* Measured float64 FMA throughput of the current device in TFLOP/s (an FMA
+ * counts 2 flops): the peak against which the simulator's float64 work is
+ * reported. Runs a short synthetic kernel. */
+CUSNA_API cusna_status cusna_measure_fp64_tflops(double *tflops);
 
 #ifdef __cplusplus
 }  /* extern "C" */
