@@ -46,19 +46,26 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> str:
-    os.makedirs(OUT_DIR, exist_ok=True)
-    os.makedirs(BUILD_DIR, exist_ok=True)
+def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False,
+          out: str | None = None, extra_flags: list[str] | None = None) -> str:
+    """Compile and link; `out`/`extra_flags` build a variant elsewhere (e.g. a
+    different register budget) without touching the in-tree library."""
+    lib_path = out or LIB
+    build_dir = BUILD_DIR if out is None else os.path.join(os.path.dirname(out), "_build_" +
+                                                           os.path.basename(out).replace(".so", ""))
+    os.makedirs(os.path.dirname(lib_path), exist_ok=True)
+    os.makedirs(build_dir, exist_ok=True)
+    extra = list(extra_flags or [])
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "libcusna.h"))
     srcs = sources()
     objs = []
     jobs = []
     for s in srcs:
-        o = os.path.join(BUILD_DIR, os.path.basename(s)[:-3] + ".o")
+        o = os.path.join(build_dir, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
         if force or ptxas_info or _stale(o, [s] + headers):
-            cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o]
+            cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o]
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)
@@ -70,13 +77,13 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
                 sys.stderr.write(r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    if force or jobs or _stale(lib_path, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib_path] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
-    return LIB
+    return lib_path
 
 
 if __name__ == "__main__":

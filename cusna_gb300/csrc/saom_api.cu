@@ -489,17 +489,21 @@ cusna_status fetch_outputs(Job &J) {
 }
 
 // ---- launch-shape autotuner ---------------------------------------------------
-// The simulator is float64-bound on GB300, so the shape only has to keep every
-// SM sub-partition issuing float64 work: at least two warps per sub-partition
-// (8 per SM) with the chain state in shared memory. Among the shapes that fit,
-// prefer the fewest warps per chain (no team barriers) and many chains per SM.
+// The simulator is bound by the float64 pipe, whose instructions have long
+// latencies, so the shape that wins keeps the most warps resident per SM while
+// every resident team has a chain to run. For each team size G (warps per
+// chain), chain state in shared memory or in-rows in global scratch, and teams
+// per CTA, the CUDA occupancy calculator gives the resident CTAs per SM (shared
+// memory, registers and warps all count). The score is the number of warps that
+// will be busy: min(resident teams, chains) * G per SM, capped at 48; ties go to
+// smaller teams (fewer barriers) and to in-rows in shared memory.
 LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bool gw,
                          bool tq, long long total_units, int force_G, int force_tpc) {
   const Ctx &c = g_ctx;
   LaunchShape best{};
   best.G = 0;
-  const int Gs[5] = {1, 2, 4, 8, 16};
   double best_score = -1.0;
+  const int Gs[5] = {1, 2, 4, 8, 16};
   for (int gi = 0; gi < 5; ++gi) {
     const int G = Gs[gi];
     if (force_G && G != force_G) continue;
@@ -509,33 +513,27 @@ LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, boo
       sh.cols_in_smem = cols_smem;
       sh.lay = make_layout(nmax, Wmax, kmax, kbmax, nrmax, G, cols_smem, tp, gw, tq);
       if (sh.lay.bytes > (size_t)c.smem_optin) continue;
-      int tpc = 1;
-      if (G == 1) {
-        tpc = (int)std::min<size_t>(8, (size_t)c.smem_optin / sh.lay.bytes);
-        tpc = std::max(1, tpc);
+      for (int tpc = 1; tpc <= 16; tpc *= 2) {
+        if (force_tpc && tpc != force_tpc) continue;
+        const int threads = 32 * G * tpc;
+        if (threads > 512 || (G > 1 && tpc > 15)) continue;
+        const size_t dyn = sh.lay.bytes * tpc;
+        if (dyn > (size_t)c.smem_optin) continue;
+        const int per_sm = period_blocks_per_sm(threads, dyn);
+        if (per_sm < 1) continue;
+        const double teams_sm = (double)per_sm * tpc;
+        const double chains_sm = (double)total_units / c.sms;
+        const double busy_warps = std::min(teams_sm, std::max(chains_sm, 1.0)) * G;
+        const double score = std::min(busy_warps, 48.0) * 100.0 - G - (cols_smem ? 0.0 : 50.0) - tpc * 0.01;
+        if (score > best_score) {
+          best_score = score;
+          best = sh;
+          best.teams_per_cta = tpc;
+          const long long want = (total_units + tpc - 1) / tpc;
+          best.ctas = (int)std::max<long long>(1, std::min<long long>((long long)c.sms * per_sm, want));
+        }
       }
-      if (force_tpc) {
-        tpc = force_tpc;
-        if (sh.lay.bytes * tpc > (size_t)c.smem_optin) continue;
-      }
-      if (G > 1 && tpc > 15) continue;
-      sh.teams_per_cta = tpc;
-      const size_t dyn = sh.lay.bytes * tpc;
-      int per_sm = period_blocks_per_sm(32 * G * tpc, dyn);
-      if (per_sm < 1) continue;
-      const int warps_sm = per_sm * tpc * G;
-      const double teams = (double)c.sms * per_sm * tpc;
-      // score: float64 issue coverage first, then fewer barriers, smem cols
-      double cover = std::min(1.0, warps_sm / 8.0);
-      double util = std::min(1.0, (double)total_units / teams);
-      double score = cover * 100.0 + util * 10.0 - G * 0.5 + (cols_smem ? 1.0 : 0.0);
-      if (score > best_score) {
-        best_score = score;
-        best = sh;
-        long long want = (total_units + tpc - 1) / tpc;
-        best.ctas = (int)std::max<long long>(1, std::min<long long>((long long)c.sms * per_sm, want));
-      }
-      if (cols_smem) break;  // smem columns fit: do not consider global ones
+      if (cols_smem && best.G == G) break;  // in-rows fit in shared memory for this G
     }
   }
   return best;

@@ -204,6 +204,72 @@ __device__ int rate_draw(const Team &T, const DevProblem &P, const Slice &S, con
   return focal;
 }
 
+// Top-2 of the float32 Gumbel estimates: best value b1 at alter j1 (ties to
+// the smaller j) and the largest value b2 of every other alter.
+struct Top2 {
+  float b1, b2;
+  int j1;
+};
+__device__ __forceinline__ void top2_merge(Top2 &a, const Top2 &c) {
+  if (c.b1 > a.b1 || (c.b1 == a.b1 && c.j1 < a.j1)) {
+    a.b2 = fmaxf(c.b2, a.b1);
+    a.b1 = c.b1;
+    a.j1 = c.j1;
+  } else {
+    a.b2 = fmaxf(a.b2, c.b1);
+  }
+}
+__device__ __forceinline__ Top2 team_top2(const Team &T, Top2 x, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Top2 y;
+    y.b1 = __shfl_xor_sync(kFull, x.b1, o);
+    y.b2 = __shfl_xor_sync(kFull, x.b2, o);
+    y.j1 = __shfl_xor_sync(kFull, x.j1, o);
+    top2_merge(x, y);
+  }
+  if (T.G == 1) return x;
+  float *rb = (float *)red;
+  int *rj = (int *)(red + T.G);
+  T.sync();
+  if (T.lane == 0) { rb[2 * T.warp] = x.b1; rb[2 * T.warp + 1] = x.b2; rj[T.warp] = x.j1; }
+  T.sync();
+  Top2 a{rb[0], rb[1], rj[0]};
+  for (int w = 1; w < T.G; ++w) top2_merge(a, Top2{rb[2 * w], rb[2 * w + 1], rj[w]});
+  return a;
+}
+
+// float32 image of y (finite, <= 0) truncated toward zero: relative error
+// below 2^-23, formed on the integer pipes. Values below -1e4 (never in the
+// Gumbel shortlist, whose members have y >= -26.1) become -inf.
+__device__ __forceinline__ float shortlist_f32(double y) {
+  if (!(y > -1e4)) return -INFINITY;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
+  const int fe = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+  if (fe <= 0) return 0.0f;
+  const unsigned m = (unsigned)((b >> 29) & 0x7FFFFFu);
+  return __uint_as_float((unsigned)((b >> 63) << 31) | ((unsigned)fe << 23) | m);
+}
+
+__device__ __forceinline__ bool is_nan64(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return ((b >> 52) & 0x7FF) == 0x7FF && (b & 0xFFFFFFFFFFFFFull) != 0;
+}
+
+// Team sums of sume and wsum[0..k-1]: warp recursive halving over V >= k+1
+// values, then one slot per (quantity, warp) in red[q*G + warp].
+template <int V>
+__device__ __forceinline__ void lse_reduce(const Team &T, const Slice &S, double sume,
+                                           const double *wsum, int k) {
+  double v[V];
+  v[0] = sume;
+#pragma unroll
+  for (int q = 1; q < V; ++q) v[q] = (q - 1 < k) ? wsum[q - 1] : 0.0;
+  const int q = warp_multi_sum<V>(v, T.lane);
+  const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
+  if (writer && q <= k) S.red[q * T.G + T.warp] = v[0];
+}
+
 // One chain: the ministep loop and the chain's outputs.
 __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, int c) {
   const int n = P.n, W = P.W, k = P.k, L = T.L;
@@ -212,34 +278,51 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
 
   const double lam = (double)P.lam[c];
   const double lamb = P.lamb ? (double)P.lamb[c] : 0.0;
+  // the reference's constant-rate expressions (src/libcusna_saom_cpu.cpp:195,197)
+  const double den = __dmul_rn((double)P.nact, __dadd_rn(lam, lamb));
+  const double pnet = __ddiv_rn(lam, __dadd_rn(lam, lamb));
   long long dist = 0, bdist = 0, ms = 0, msb = 0;
   double t = 0.0, rho = 0.0;
-  double d[24];
-  double wsum[24];
+  double d[24], wsum[24], dbest[24];
 
   for (;;) {
-    uint32_t rr[4];
-    philox10((uint32_t)ms, chain, 0u, 0u, P.k0, P.k1, rr);
     int i;
     bool is_net;
+    uint32_t r3;
     if (P.nrate > 0) {
+      uint32_t rr[4];
+      philox10((uint32_t)ms, chain, 0u, 0u, P.k0, P.k1, rr);
       i = rate_draw(T, P, S, rr, lam, t, rho);
       if (i < 0) break;
       is_net = true;
+      r3 = rr[3];
     } else {
-      // constant rate (src/libcusna_saom_cpu.cpp:195-199); every lane computes
-      // the same scalars
-      const double den = __dmul_rn((double)P.nact, __dadd_rn(lam, lamb));
-      t = __dadd_rn(t, __ddiv_rn(-log(unif01(rr[0])), den));
+      // constant rate (:195-199). The draws of 32 ministeps are formed at
+      // once, one per lane of warp 0 (they depend only on the counters), and
+      // the time is accumulated in order, so every value equals the reference's.
+      const int slot = (int)(ms & 31);
+      if (slot == 0) {
+        if (T.warp == 0) {
+          uint32_t rr[4];
+          philox10((uint32_t)(ms + T.lane), chain, 0u, 0u, P.k0, P.k1, rr);
+          S.rtau[T.lane] = __ddiv_rn(-log(unif01(rr[0])), den);
+          S.rnet[T.lane] = (P.kb == 0 || unif01(rr[1]) < pnet) ? 1 : 0;
+          long long idx = (long long)__dmul_rn(unif01(rr[2]), (double)P.nact);
+          if (idx >= P.nact) idx = P.nact - 1;
+          S.rfocal[T.lane] = P.act[idx];
+          S.rr3[T.lane] = rr[3];
+        }
+        T.sync();
+      }
+      t = __dadd_rn(t, S.rtau[slot]);
       if (!P.cond && t > 1.0) break;
-      is_net = P.kb == 0 || unif01(rr[1]) < __ddiv_rn(lam, __dadd_rn(lam, lamb));
-      long long idx = (long long)__dmul_rn(unif01(rr[2]), (double)P.nact);
-      if (idx >= P.nact) idx = P.nact - 1;
-      i = P.act[idx];
+      is_net = S.rnet[slot] != 0;
+      i = S.rfocal[slot];
+      r3 = S.rr3[slot];
     }
 
     if (!is_net) {
-      if (T.tl == 0) beh_step(P, S, i, rr[3], &bdist);
+      if (T.tl == 0) beh_step(P, S, i, r3, &bdist);
       T.sync();
       ++msb;
       ++ms;
@@ -280,7 +363,7 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
         S.fbuf[j] = f;
         // a NaN predictor never raises the maximum (the reference compares
         // f > lmax) and is never chosen (its Gumbel key compares false)
-        if (ok && !isnan(f)) {
+        if (ok && !is_nan64(f)) {
           const long long kf = dkey(f);
           kmax = kf > kmax ? kf : kmax;
         }
@@ -291,10 +374,14 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
     const double lmax = dunkey(team_max_ll(T, kmax, S.red));
     T.sync();
 
-    // ---- pass 2: log-sum-exp sums and the float32 Gumbel estimates ---------
+    // ---- pass 2: log-sum-exp sums and float32 Gumbel estimates --------------
+    // The estimate of g_j - lmax, shortlist_f32(f_j - lmax) - loglog_est(u_j),
+    // is within 2^-23*26.1 + 2.2e-6 + 2^-24*23 < 7e-6 of the float64 value for
+    // every alter that can be the argmax (those have f_j - lmax >= -26.1, as
+    // their key is at least the key of the lmax alter, >= -3.2).
     double sume = 0.0;
     for (int e = 0; e < k; ++e) wsum[e] = 0.0;
-    float gbest = -INFINITY;
+    Top2 best{-INFINITY, -INFINITY, 0x7FFFFFFF};
     for (int j = T.tl; j < n; j += L) {
       if (!((S.okbits[j >> 5] >> (j & 31)) & 1u)) {
         S.gbuf[j] = -INFINITY;
@@ -311,71 +398,79 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
       }
       uint32_t ph[4];
       philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-      const float gt = (float)y - loglog_est(ph[0]);
+      const float gt = shortlist_f32(y) - loglog_est(ph[0]);
       S.gbuf[j] = gt;
-      gbest = fmaxf(gbest, gt);
-    }
-    // team sums of sume and wsum[0..k-1] into red[q*G + warp]
-    {
-      double v[32];
-#pragma unroll
-      for (int q = 0; q < 32; ++q) v[q] = 0.0;
-      v[0] = sume;
-#pragma unroll
-      for (int q = 1; q < 32; ++q)
-        if (q - 1 < k) v[q] = wsum[q - 1];
-      const int q = warp_multi_sum<32>(v, T.lane);
-      const float gmax0 = team_max_f(T, gbest, S.red);
-      T.sync();
-      if (q <= k) S.red[q * T.G + T.warp] = v[0];
-      if (T.tl == 0) ((float *)(S.misc + 6))[0] = gmax0;
-      T.sync();
-    }
-    const float gmax = ((float *)(S.misc + 6))[0];
-
-    // ---- pass 3: exact Gumbel keys of the shortlist ------------------------
-    long long bk = dkey(-1e300);
-    int bj = 0x7FFFFFFF;
-    const float thr = gmax - kGumbelWindow;
-    for (int j = T.tl; j < n; j += L) {
-      if (S.gbuf[j] >= thr) {
-        uint32_t ph[4];
-        philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-        const double g = __dsub_rn(S.fbuf[j], log(-log(unif01(ph[0]))));
-        const long long kg = dkey(g);
-        if (kg > bk || (kg == bk && j < bj)) { bk = kg; bj = j; }
+      if (gt > best.b1) {  // j ascending within a lane: ties keep the earlier j
+        best.b2 = best.b1;
+        best.b1 = gt;
+        best.j1 = j;
+        if (j != i)
+          for (int e = 0; e < k; ++e) dbest[e] = d[e];
+      } else {
+        best.b2 = fmaxf(best.b2, gt);
       }
     }
-    const int jstar = team_argmax(T, bk, bj, S.red + 26 * T.G);
+    const int jsaved = best.j1;
+    if (k + 1 <= 8) lse_reduce<8>(T, S, sume, wsum, k);
+    else if (k + 1 <= 16) lse_reduce<16>(T, S, sume, wsum, k);
+    else lse_reduce<32>(T, S, sume, wsum, k);
+    const Top2 top = team_top2(T, best, S.red + 26 * T.G);
 
-    // ---- score update and toggle (team lane 0) -----------------------------
-    if (T.tl == 0) {
-      double tot[25];
-      for (int q = 0; q <= k; ++q) {
-        double s = 0.0;
-        for (int w = 0; w < T.G; ++w) s = __dadd_rn(s, S.red[q * T.G + w]);
-        tot[q] = s;
+    // ---- the chosen alter ---------------------------------------------------
+    // The float estimates decide unless the top two are within the window;
+    // then the shortlist's exact float64 keys decide, ties to the smaller j.
+    int jstar;
+    if (top.b1 - top.b2 > kGumbelWindow) {
+      jstar = top.j1;
+    } else {
+      long long bk = dkey(-1e300);
+      int bj = 0x7FFFFFFF;
+      const float thr = top.b1 - kGumbelWindow;
+      for (int j = T.tl; j < n; j += L) {
+        if (S.gbuf[j] >= thr) {
+          uint32_t ph[4];
+          philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
+          const double g = __dsub_rn(S.fbuf[j], log(-log(unif01(ph[0]))));
+          if (is_nan64(g)) continue;
+          const long long kg = dkey(g);
+          if (kg > bk || (kg == bk && j < bj)) { bk = kg; bj = j; }
+        }
       }
-      if (jstar != i) {
+      jstar = team_argmax(T, bk, bj, S.red + 29 * T.G);
+    }
+
+    // ---- score update (lane e updates effect e) and toggle ----------------
+    if (T.tl == jstar % L) {
+      if (jstar == i) {
+        for (int e = 0; e < k; ++e) S.dstar[e] = 0.0;
+      } else if (jsaved == jstar) {
+        for (int e = 0; e < k; ++e) S.dstar[e] = dbest[e];
+      } else {
         const int aij = bit_of(S.rowsT, n, i, jstar);
         const int aji = bit_of(S.colsT, n, i, jstar);
         change_stats(P, S, X, jstar, aij, aji, d);
-      } else {
-        for (int e = 0; e < k; ++e) d[e] = 0.0;
+        for (int e = 0; e < k; ++e) S.dstar[e] = d[e];
       }
-      for (int e = 0; e < k; ++e)
-        S.sc[e] = __dadd_rn(S.sc[e], __dsub_rn(d[e], __ddiv_rn(tot[e + 1], tot[0])));
+    }
+    const int aij_star = bit_of(S.rowsT, n, i, jstar);
+    T.sync();
+    if (T.tl < k) {
+      const int e = T.tl;
+      double s0 = 0.0, se = 0.0;
+      for (int w = 0; w < T.G; ++w) {
+        s0 = __dadd_rn(s0, S.red[w]);
+        se = __dadd_rn(se, S.red[(e + 1) * T.G + w]);
+      }
+      S.sc[e] = __dadd_rn(S.sc[e], __dsub_rn(S.dstar[e], __ddiv_rn(se, s0)));
     }
     ++ms;
     if (jstar != i) {
       const int j = jstar;
-      const int aij = bit_of(S.rowsT, n, i, j);
       const long long chg = P.symflag ? 2 : 1;
       if (bit_of(P.kdistT, n, i, j))
-        dist += (aij == bit_of(P.x0T, n, i, j)) ? chg : -chg;
-      T.sync();  // every lane has read the pre-toggle state
+        dist += (aij_star == bit_of(P.x0T, n, i, j)) ? chg : -chg;
       if (T.tl == 0) {
-        const int dl = 1 - 2 * aij;
+        const int dl = 1 - 2 * aij_star;
         S.rowsT[(j >> 5) * n + i] ^= 1u << (j & 31);
         S.colsT[(i >> 5) * n + j] ^= 1u << (i & 31);
         S.indeg[j] += dl;

@@ -53,13 +53,16 @@ struct Slice {
   double *rsc;       // nrate
   double *p1, *p2;   // k
   int *tid, *ety, *dyn, *i0, *i1, *i2, *bty, *rkind;
-  int *misc;         // 8 ints: team broadcast slots
+  int *misc;         // 16 ints: team broadcast slots
+  double *rtau;      // 32 constant-rate draws: time increments,
+  int *rnet, *rfocal; //   network/behaviour flag, focal actor,
+  uint32_t *rr3;     //   behaviour uniform
 };
 
 struct SliceLayout {
   size_t bytes;  // per team
   size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_f, o_g, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
-      o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc;
+      o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc, o_rtau, o_rnet, o_rfocal, o_rr3;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -101,6 +104,10 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_bty, (size_t)(kb + 1) * 4);
   put(s.o_rkind, (size_t)(nrate + 1) * 4);
   put(s.o_misc, 16 * 4);
+  put(s.o_rtau, 32 * 8);
+  put(s.o_rnet, 32 * 4);
+  put(s.o_rfocal, 32 * 4);
+  put(s.o_rr3, 32 * 4);
   s.bytes = al16(o);
   return s;
 }
@@ -138,6 +145,10 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   s.bty = (int *)(base + L.o_bty);
   s.rkind = (int *)(base + L.o_rkind);
   s.misc = (int *)(base + L.o_misc);
+  s.rtau = (double *)(base + L.o_rtau);
+  s.rnet = (int *)(base + L.o_rnet);
+  s.rfocal = (int *)(base + L.o_rfocal);
+  s.rr3 = (uint32_t *)(base + L.o_rr3);
   return s;
 }
 

@@ -118,7 +118,13 @@ __device__ void chain_finish(const Team &T, const DevProblem &P, const Slice &S,
 
 // Persistent period kernel: every team repeatedly takes the next chain of the
 // launch's work list (all chains of all problems) until the list is empty.
-__global__ void __launch_bounds__(512, 1)
+// MAXT is the largest CTA the instantiation serves: 256 threads with a register
+// budget for three CTAs per SM (teams of up to 8 warps), or 512 (16-warp teams).
+#ifndef CUSNA_MINB_256
+#define CUSNA_MINB_256 3  // resident 256-thread CTAs per SM the register budget allows
+#endif
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, MAXT == 512 ? 1 : CUSNA_MINB_256)
 period_kernel(const DevProblem *__restrict__ probs, const long long *__restrict__ unit_start,
               int nprob, long long total, unsigned long long *counter, SliceLayout lay, int G,
               uint32_t *cols_scratch, size_t cols_words) {
@@ -319,14 +325,15 @@ static cudaError_t counted(cudaError_t e) {
   return e;
 }
 
-int period_blocks_per_sm(int threads, size_t dyn_smem) {
-  if (cudaFuncSetAttribute(period_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <int MAXT>
+static int blocks_per_sm_t(int threads, size_t dyn_smem) {
+  if (cudaFuncSetAttribute(period_kernel<MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)dyn_smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   int b = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, period_kernel, threads, dyn_smem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, period_kernel<MAXT>, threads, dyn_smem) !=
       cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -334,14 +341,21 @@ int period_blocks_per_sm(int threads, size_t dyn_smem) {
   return b;
 }
 
+int period_blocks_per_sm(int threads, size_t dyn_smem) {
+  return threads <= 256 ? blocks_per_sm_t<256>(threads, dyn_smem)
+                        : blocks_per_sm_t<512>(threads, dyn_smem);
+}
+
 cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const long long *unit_start,
                           int nprob, long long total, unsigned long long *counter,
                           uint32_t *cols_scratch, size_t cols_words, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(period_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(sh.lay.bytes * sh.teams_per_cta));
+  const int threads = 32 * sh.G * sh.teams_per_cta;
+  const size_t dyn = sh.lay.bytes * sh.teams_per_cta;
+  auto kern = threads <= 256 ? period_kernel<256> : period_kernel<512>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
   if (e != cudaSuccess) return e;
-  period_kernel<<<sh.ctas, 32 * sh.G * sh.teams_per_cta, sh.lay.bytes * sh.teams_per_cta, st>>>(
-      probs, unit_start, nprob, total, counter, sh.lay, sh.G, cols_scratch, cols_words);
+  kern<<<sh.ctas, threads, dyn, st>>>(probs, unit_start, nprob, total, counter, sh.lay, sh.G,
+                                      cols_scratch, cols_words);
   return counted(cudaGetLastError());
 }
 
