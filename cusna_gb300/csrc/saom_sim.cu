@@ -121,7 +121,7 @@ __device__ void chain_finish(const Team &T, const DevProblem &P, const Slice &S,
 // MAXT is the largest CTA the instantiation serves: 256 threads with a register
 // budget for three CTAs per SM (teams of up to 8 warps), or 512 (16-warp teams).
 #ifndef CUSNA_MINB_256
-#define CUSNA_MINB_256 3  // resident 256-thread CTAs per SM the register budget allows
+#define CUSNA_MINB_256 2  // resident 256-thread CTAs per SM the register budget allows
 #endif
 template <int MAXT>
 __global__ void __launch_bounds__(MAXT, MAXT == 512 ? 1 : CUSNA_MINB_256)
