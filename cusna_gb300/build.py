@@ -24,6 +24,7 @@ LIB = os.path.join(OUT_DIR, "libcusna_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-ffp-contract=off",
               "-Xcompiler", "-fvisibility=hidden", "-DLIBCUSNA_BUILD",
               "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 

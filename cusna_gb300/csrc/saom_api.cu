@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -107,11 +108,162 @@ T *at(size_t off) {
 }
 
 
-// Per-problem host-side facts read during validation.
+// Per-problem host-side facts read during validation, and the effect plan.
 struct Facts {
   std::vector<int> tid, i0, i1, i2, rk;
   int flags = 0;
+  std::vector<int> kind, cfn, offd, offt;  // effect plan, k each
+  std::vector<double> pool;                // its tables
+  int zlo = 0, zR = 1;
 };
+
+template <class T>
+cusna_status fetch_vec(const T *src, size_t cnt, bool dev, std::vector<T> &dst) {
+  dst.clear();
+  if (!src || cnt == 0) return CUSNA_OK;
+  dst.resize(cnt);
+  if (dev) CU(cudaMemcpy(dst.data(), src, cnt * sizeof(T), cudaMemcpyDeviceToHost));
+  else std::memcpy(dst.data(), src, cnt * sizeof(T));
+  return CUSNA_OK;
+}
+
+// float64 descriptor with the CPU engine's precedence (*64, else float, else 0)
+cusna_status fetch_desc(const double *d64, const float *d32, size_t cnt, bool dev,
+                        std::vector<double> &out) {
+  out.assign(cnt, 0.0);
+  cusna_status s;
+  if (d64) return fetch_vec(d64, cnt, dev, out);
+  if (d32) {
+    std::vector<float> f;
+    if ((s = fetch_vec(d32, cnt, dev, f)) != CUSNA_OK) return s;
+    for (size_t q = 0; q < cnt; ++q) out[q] = (double)f[q];
+  }
+  return CUSNA_OK;
+}
+
+// Dyadic covariate magnitude of types 12, 20, 21, 25 for covariate values
+// (vi, vj): the expressions of src/libcusna_saom_cpu.cpp:72,80-81,84 without the
+// delta factor (this file is compiled without floating-point contraction).
+double dyad_value(int t, double vi, double vj, double q1, double q2) {
+  switch (t) {
+    case 12: return 1.0 - std::fabs(vi - vj) * q1 - q2;
+    case 20: return vi > vj + 1e-9 ? 1.0 : (std::fabs(vi - vj) <= 1e-9 ? 0.5 : 0.0);
+    case 21: return vi * vj;
+    default: return vi + vj;  // 25
+  }
+}
+
+// The effect plan (see K_* in saom_common.cuh): per effect how the kernel
+// forms d and theta*d, and the tables it reads. Term tables (theta * magnitude)
+// are built when every chain has the same theta, the usual case; otherwise the
+// kernel multiplies.
+cusna_status build_plan(const cusna_saom_problem *p, bool dev, Facts &F) {
+  const int n = p->n, k = p->k, M = p->M;
+  cusna_status s;
+  std::vector<float> th;
+  if ((s = fetch_vec(p->theta, (size_t)M * k, dev, th)) != CUSNA_OK) return s;
+  bool uniform = true;
+  for (int c = 1; c < M && uniform; ++c)
+    if (std::memcmp(&th[(size_t)c * k], &th[0], k * sizeof(float)) != 0) uniform = false;
+  std::vector<double> vm, wt, p1, p2;
+  std::vector<int> dyn, z0;
+  if ((s = fetch_desc(p->vmat64, p->vmat, (size_t)k * n, dev, vm)) != CUSNA_OK) return s;
+  if ((s = fetch_desc(p->wtab64, p->wtab, (size_t)k * (n + 1), dev, wt)) != CUSNA_OK) return s;
+  if ((s = fetch_desc(p->p1_64, p->p1, (size_t)k, dev, p1)) != CUSNA_OK) return s;
+  if ((s = fetch_desc(p->p2_64, p->p2, (size_t)k, dev, p2)) != CUSNA_OK) return s;
+  if ((s = fetch_vec(p->dyn_flags, (size_t)k, dev, dyn)) != CUSNA_OK) return s;
+  if ((s = fetch_vec(p->z0, (size_t)n, dev, z0)) != CUSNA_OK) return s;
+  if (dyn.empty()) dyn.assign(k, 0);
+  if (z0.empty()) z0.assign(n, 0);
+  bool has_dyn = false;
+  for (int e = 0; e < k; ++e) has_dyn |= dyn[e] != 0;
+  const bool has_z = p->kb > 0 || has_dyn;
+  // reachable behaviour values: the start values and, with behaviour
+  // dynamics, [zmin, zmax] (a ministep moves z by one within those bounds)
+  long long lo = *std::min_element(z0.begin(), z0.end()), hi = *std::max_element(z0.begin(), z0.end());
+  if (p->kb > 0) { lo = std::min<long long>(lo, p->zmin); hi = std::max<long long>(hi, p->zmax); }
+  const long long zR = hi - lo + 1;
+  const double zbar = (double)p->zbar;
+  const bool zalt_ok = has_z && zR <= 65536;
+  const bool zdyad_ok = has_z && zR <= 256;
+  F.zlo = (int)lo;
+  F.zR = (int)std::max<long long>(1, std::min<long long>(zR, 65536));
+  F.kind.assign(k, K_GEN); F.cfn.assign(k, 0); F.offd.assign(k, 0); F.offt.assign(k, 0);
+  F.pool.clear();
+  auto add = [&](size_t cnt) { const size_t o = F.pool.size(); F.pool.resize(o + cnt, 0.0); return (int)o; };
+  auto cnt_table = [&](int e, int cfn, size_t size) {
+    F.kind[e] = K_CNT; F.cfn[e] = cfn;
+    if (uniform) {
+      F.offt[e] = add(size);
+      for (size_t c = 0; c < size; ++c) F.pool[F.offt[e] + c] = (double)th[e] * (double)c;
+    }
+  };
+  auto look_table = [&](int e, int cfn, size_t size, auto value) {
+    F.kind[e] = K_LOOK; F.cfn[e] = cfn;
+    F.offd[e] = add(size);
+    for (size_t x = 0; x < size; ++x) F.pool[F.offd[e] + x] = value(x);
+    if (uniform) {
+      F.offt[e] = add(size);
+      for (size_t x = 0; x < size; ++x) F.pool[F.offt[e] + x] = (double)th[e] * F.pool[F.offd[e] + x];
+    }
+  };
+  const size_t N = (size_t)n;
+  int fl = 0;
+  for (int e = 0; e < k; ++e) {
+    const int t = F.tid[e];
+    const double *v = &vm[(size_t)e * n];
+    switch (t) {
+      case 0: cnt_table(e, 0, 2); break;
+      case 1: cnt_table(e, 1, 2); break;
+      case 2: cnt_table(e, 2, 2 * N + 1); break;
+      case 3: case 23: cnt_table(e, 3, N + 1); break;
+      case 4: cnt_table(e, 4, N + 2); break;
+      case 5: cnt_table(e, 5, 2 * N + 2); break;
+      case 6: cnt_table(e, 6, 2 * N + 1); break;
+      case 8: cnt_table(e, 7, N + 1); break;
+      case 7: look_table(e, 4, N + 2, [](size_t c) { return std::sqrt((double)c); }); break;
+      case 9: look_table(e, 7, N + 1, [](size_t c) { return std::sqrt((double)c); }); break;
+      case 10: case 14: case 15: case 16: case 17: case 18: case 19:
+        F.kind[e] = K_STEP; fl |= F_HAS_STEP; break;
+      case 11: case 31: {
+        const double q1 = p1[e];
+        auto f = [&](double x) { return t == 11 ? x : (x >= q1 - 1e-12 ? 1.0 : 0.0); };
+        if (dyn[e]) {
+          if (zalt_ok) look_table(e, 13, (size_t)zR, [&](size_t x) { return f((double)(lo + (long long)x) - zbar); });
+        } else {
+          look_table(e, 12, N, [&](size_t j) { return f(v[j]); });
+        }
+        break;
+      }
+      case 12: case 20: case 21: case 25: {
+        const double q1 = p1[e], q2 = p2[e];
+        if (dyn[e]) {
+          if (zdyad_ok)
+            look_table(e, 15, (size_t)(zR * zR), [&](size_t x) {
+              const double vi = (double)(lo + (long long)(x / zR)) - zbar;
+              const double vj = (double)(lo + (long long)(x % zR)) - zbar;
+              return dyad_value(t, vi, vj, q1, q2);
+            });
+        } else if (n <= 1024) {
+          look_table(e, 14, N * N, [&](size_t x) { return dyad_value(t, v[x / N], v[x % N], q1, q2); });
+        }
+        break;
+      }
+      case 22: F.kind[e] = K_ZERO; break;
+      case 24: look_table(e, 8, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
+      case 26: look_table(e, 9, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
+      case 27: look_table(e, 10, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
+      case 28: look_table(e, 11, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
+      case 13: case 29: case 30: case 32: break;  // K_GEN
+      default: F.kind[e] = K_ZERO; break;       // unknown ids: the reference's 0
+    }
+  }
+  if (F.pool.empty()) F.pool.push_back(0.0);
+  if (uniform) fl |= F_THETA_TAB;
+  if (has_z) fl |= F_HAS_Z;
+  F.flags |= fl;
+  return CUSNA_OK;
+}
 
 cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, bool dev,
                       Facts &F) {
@@ -185,6 +337,7 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
     }
   }
   F.flags = fl;
+  if ((s = build_plan(p, dev, F)) != CUSNA_OK) return s;
   // gwdsp change statistics index the weight table at p+1 with p <= n-2 on a
   // network without self-ties; a self-tie in the start network could push p to
   // n and read past the table, so such problems are rejected
@@ -216,6 +369,7 @@ struct ProbBufs {
   size_t x0T, x0cT, simT, simcT, kdistT, permT, keepT, forceT, keepcT, forcecT;
   size_t vmat, wtab, p1, p2, vb, ralpha, ru;
   size_t etypes, dyn, i0, i1, i2, act, z0, bkdist, inact, vmiss;
+  size_t ekind, ecfn, eoffd, eofft, pool;
   // raw copies (host mode)
   size_t r_x0, r_sim, r_kd, r_pm, r_keep, r_force, r_theta, r_lam, r_lamb, r_thetab, r_tid,
       r_ety, r_dyn, r_i0, r_i1, r_i2, r_vmat64, r_vmat32, r_wtab64, r_wtab32, r_p164, r_p132,
@@ -255,6 +409,8 @@ void plan_problem(Planner &pl, Job &J, bool dev) {
   B.i1 = pl.take(k * 4); B.i2 = pl.take(k * 4); B.act = pl.take(n * 4);
   B.z0 = pl.take(n * 4); B.bkdist = pl.take(n * 4); B.inact = pl.take(W * 4);
   B.vmiss = NONE;
+  B.ekind = pl.take(k * 4); B.ecfn = pl.take(k * 4); B.eoffd = pl.take(k * 4);
+  B.eofft = pl.take(k * 4); B.pool = pl.take(J.F.pool.size() * 8);
   if (!dev) {
     B.r_x0 = pl.take(n * W * 4);
     B.r_sim = maybe(pl, p->sim_out, n * W * 4);
@@ -417,7 +573,7 @@ cusna_status prepare(Job &J, bool dev, DevProblem &D, uint32_t chain_offset) {
   D.k0 = (uint32_t)(p->seed & 0xFFFFFFFFu);
   D.k1 = (uint32_t)(p->seed >> 32);
   D.flags = J.F.flags | ((r->want_end_nets && r->a_ends) ? F_WANT_ENDS : 0);
-  D.zmin = p->zmin; D.zmax = p->zmax;
+  D.zmin = p->zmin; D.zmax = p->zmax; D.zlo = J.F.zlo; D.zR = J.F.zR;
   D.zbar = (double)p->zbar; D.brange = (double)p->brange; D.bsimmean = (double)p->bsimmean;
   D.type_ids = tid; D.etypes = at<int>(B.etypes); D.dyn = at<int>(B.dyn);
   D.int0 = at<int>(B.i0); D.int1 = at<int>(B.i1); D.int2 = at<int>(B.i2);
@@ -433,6 +589,13 @@ cusna_status prepare(Job &J, bool dev, DevProblem &D, uint32_t chain_offset) {
   D.keepT = at<uint32_t>(B.keepT); D.forceT = at<uint32_t>(B.forceT);
   D.keepcT = at<uint32_t>(B.keepcT); D.forcecT = at<uint32_t>(B.forcecT);
   D.lam = lam; D.theta = theta; D.lamb = lamb; D.thetab = thetab;
+  CU(cudaMemcpyAsync(at<int>(B.ekind), J.F.kind.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<int>(B.ecfn), J.F.cfn.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<int>(B.eoffd), J.F.offd.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<int>(B.eofft), J.F.offt.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<double>(B.pool), J.F.pool.data(), J.F.pool.size() * 8, cudaMemcpyHostToDevice, st));
+  D.ekind = at<int>(B.ekind); D.ecfn = at<int>(B.ecfn); D.eoffd = at<int>(B.eoffd);
+  D.eofft = at<int>(B.eofft); D.tab = at<double>(B.pool);
   auto out = [&](void *user, size_t off) -> void * {
     if (!user) return nullptr;
     return dev ? user : (off == NONE ? nullptr : at<char>(off));

@@ -26,7 +26,12 @@ __device__ __forceinline__ void chain_init(const Team &T, const DevProblem &P, c
     S.i2[e] = P.int2[e];
     S.p1[e] = P.p1[e];
     S.p2[e] = P.p2[e];
+    S.ekind[e] = P.ekind[e];
+    S.ecfn[e] = P.ecfn[e];
+    S.eoffd[e] = P.eoffd[e];
+    S.eofft[e] = P.eofft[e];
   }
+  for (int x = T.tl; x < 64; x += L) S.exptab[x] = kExp2Frac64[x];
   for (int e = T.tl; e < P.kb; e += L) {
     S.thb[e] = P.thetab ? (double)P.thetab[(size_t)c * P.kb + e] : 0.0;
     S.bsc[e] = 0.0;
@@ -36,7 +41,7 @@ __device__ __forceinline__ void chain_init(const Team &T, const DevProblem &P, c
     S.rsc[q] = 0.0;
     S.rkind[q] = P.rkind[q];
   }
-  if (P.kb > 0)
+  if (P.flags & F_HAS_Z)
     for (int x = T.tl; x < n; x += L) S.z[x] = P.z0[x];
   if (P.nrate > 0)
     for (int x = T.tl; x < n; x += L) S.crate[x] = 1.0;
@@ -339,7 +344,11 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
     X.rdeg_i = 0;
     if (P.flags & F_NEED_RDEG)
       for (int w = 0; w < W; ++w) X.rdeg_i += __popc(S.rowsT[w * n + i] & S.colsT[w * n + i]);
-    X.zvi = P.kb > 0 ? __dsub_rn((double)S.z[i], P.zbar) : 0.0;
+    X.zvi = (P.flags & F_HAS_Z) ? __dsub_rn((double)S.z[i], P.zbar) : 0.0;
+    if (P.flags & F_HAS_STEP) {
+      step_values(T, P, S, X);
+      T.sync();
+    }
 
     // ---- pass 1: change statistics, f_j, lmax ------------------------------
     long long kmax = dkey(-1e30);
@@ -356,8 +365,7 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
                !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg);
           if (ok) {
             const int aji = bit_of(S.colsT, n, i, j);
-            change_stats(P, S, X, j, aij, aji, d);
-            for (int e = 0; e < k; ++e) f = __dadd_rn(f, __dmul_rn(S.th[e], d[e]));
+            f = change_stats<true>(P, S, X, j, aij, aji, d);
           }
         }
         S.fbuf[j] = f;
@@ -388,12 +396,12 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
         continue;
       }
       const double y = __dsub_rn(S.fbuf[j], lmax);
-      const double wj = exp(y);
+      const double wj = exp_weight(y, S.exptab);
       sume = __dadd_rn(sume, wj);
       if (j != i) {
         const int aij = bit_of(S.rowsT, n, i, j);
         const int aji = bit_of(S.colsT, n, i, j);
-        change_stats(P, S, X, j, aij, aji, d);
+        change_stats<false>(P, S, X, j, aij, aji, d);
         for (int e = 0; e < k; ++e) wsum[e] = fma(wj, d[e], wsum[e]);
       }
       uint32_t ph[4];
@@ -448,7 +456,7 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
       } else {
         const int aij = bit_of(S.rowsT, n, i, jstar);
         const int aji = bit_of(S.colsT, n, i, jstar);
-        change_stats(P, S, X, jstar, aij, aji, d);
+        change_stats<false>(P, S, X, jstar, aij, aji, d);
         for (int e = 0; e < k; ++e) S.dstar[e] = d[e];
       }
     }

@@ -57,12 +57,16 @@ struct Slice {
   double *rtau;      // 32 constant-rate draws: time increments,
   int *rnet, *rfocal; //   network/behaviour flag, focal actor,
   uint32_t *rr3;     //   behaviour uniform
+  int *ekind, *ecfn, *eoffd, *eofft;  // k  effect plan
+  double *stepd, *stept;  // 4k  per-ministep K_STEP magnitudes and terms
+  double *exptab;    // 64  2^(j/64) for exp_weight
 };
 
 struct SliceLayout {
   size_t bytes;  // per team
   size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_f, o_g, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
-      o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc, o_rtau, o_rnet, o_rfocal, o_rr3;
+      o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc, o_rtau, o_rnet, o_rfocal, o_rr3, o_ekind, o_ecfn, o_eoffd, o_eofft,
+      o_stepd, o_stept, o_exptab;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -78,7 +82,7 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_cols, cols_in_smem ? (size_t)W * n * 4 : 0);
   put(s.o_indeg, (size_t)n * 4);
   put(s.o_outdeg, (size_t)n * 4);
-  put(s.o_z, kb > 0 ? (size_t)n * 4 : 0);
+  put(s.o_z, (size_t)n * 4);
   put(s.o_f, (size_t)n * 8);
   put(s.o_g, (size_t)n * 4);
   put(s.o_ok, (size_t)W * 4);
@@ -108,6 +112,13 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_rnet, 32 * 4);
   put(s.o_rfocal, 32 * 4);
   put(s.o_rr3, 32 * 4);
+  put(s.o_ekind, (size_t)k * 4);
+  put(s.o_ecfn, (size_t)k * 4);
+  put(s.o_eoffd, (size_t)k * 4);
+  put(s.o_eofft, (size_t)k * 4);
+  put(s.o_stepd, (size_t)k * 4 * 8);
+  put(s.o_stept, (size_t)k * 4 * 8);
+  put(s.o_exptab, 64 * 8);
   s.bytes = al16(o);
   return s;
 }
@@ -149,6 +160,13 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   s.rnet = (int *)(base + L.o_rnet);
   s.rfocal = (int *)(base + L.o_rfocal);
   s.rr3 = (uint32_t *)(base + L.o_rr3);
+  s.ekind = (int *)(base + L.o_ekind);
+  s.ecfn = (int *)(base + L.o_ecfn);
+  s.eoffd = (int *)(base + L.o_eoffd);
+  s.eofft = (int *)(base + L.o_eofft);
+  s.stepd = (double *)(base + L.o_stepd);
+  s.stept = (double *)(base + L.o_stept);
+  s.exptab = (double *)(base + L.o_exptab);
   return s;
 }
 
@@ -295,79 +313,77 @@ __device__ __forceinline__ double flip(double x, unsigned long long sgn) {
   return __longlong_as_double(__double_as_longlong(x) ^ (long long)sgn);
 }
 
-// Change statistics of toggling i -> j for all k effects (src/libcusna_saom_cpu.cpp:
-// 49-101 per effect type, :243-261 for the per-alter loop with interactions and
-// creation/endowment zeroing). Popcounts of the word-major bitsets replace the
-// reference's O(n) dense loops; they count the same sets:
-//   |out_i & in_j| = #{h: a_ih a_hj}      |out_i & out_j| = #{h: a_ih a_jh}
-//   |out_j & in_i| = #{h: a_jh a_hi}      |in_i & in_j|   = #{h: a_hi a_hj}
-//   |in_i & out_j| = #{h: a_hi a_jh}
-// Every float64 value equals the reference's: delta * x is a sign flip of x,
-// and all other operations use the reference's operands and order.
-__device__ __forceinline__ void change_stats(const DevProblem &P, const Slice &S, const StepCtx &X,
-                                             int j, int aij, int aji, double *d) {
-  const int n = P.n, W = P.W, k = P.k, i = X.i;
+// Generic change statistic of one effect (src/libcusna_saom_cpu.cpp:49-101 and
+// :246-251): the reference formula evaluated per alter. Used for the kinds no
+// table covers (gwdsp, interactions, dyadic covariates of very large n).
+__device__ __noinline__ double gen_stat(const DevProblem &P, const Slice &S, const StepCtx &X,
+                                        int e, int j, int aij, int aji, int ri_cj, int ri_rj,
+                                        int rj_ci, int ci_cj, int ci_rj, const double *d) {
+  const int n = P.n, W = P.W, i = X.i, t = S.tid[e];
   const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;
   const double dl = aij ? -1.0 : 1.0;
-  const int fl = P.flags;
-  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;
-  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
-    const uint32_t *R = S.rowsT, *Cc = S.colsT;
-    for (int w = 0; w < W; ++w) {
-      const uint32_t ri = R[w * n + i], rj = R[w * n + j];
-      const uint32_t ci = Cc[w * n + i], cj = Cc[w * n + j];
-      if (fl & F_PC_RI_CJ) ri_cj += __popc(ri & cj);
-      if (fl & F_PC_RI_RJ) ri_rj += __popc(ri & rj);
-      if (fl & F_PC_RJ_CI) rj_ci += __popc(rj & ci);
-      if (fl & F_PC_CI_CJ) ci_cj += __popc(ci & cj);
-      if (fl & F_PC_CI_RJ) ci_rj += __popc(ci & rj);
-      if (fl & F_PC_RICIRJ) ricirj += __popc(ri & ci & rj);
-    }
+  if (t == 32) {
+    const int c2 = S.i2[e];
+    double v = c2 < 0 ? dl : 1.0;
+    v = __dmul_rn(v, __dmul_rn(d[S.i0[e]], d[S.i1[e]]));
+    if (c2 >= 0) v = __dmul_rn(v, d[c2]);
+    return v;
   }
-  const double zvj = P.kb > 0 ? __dsub_rn((double)S.z[j], P.zbar) : 0.0;
-#pragma unroll 1
-  for (int e = 0; e < k; ++e) {
-    const int t = S.tid[e];
-    double v;
-    if (t == 32) {  // interaction: product of earlier statistics (:246-251)
-      const int c2 = S.i2[e];
-      v = c2 < 0 ? dl : 1.0;
-      v = __dmul_rn(v, __dmul_rn(d[S.i0[e]], d[S.i1[e]]));
-      if (c2 >= 0) v = __dmul_rn(v, d[c2]);
-      d[e] = v;
-      continue;
-    }
-    double vi = 0.0, vj = 0.0;
-    if ((t >= 10 && t <= 13) || t == 20 || t == 21 || t == 25 || t == 31) {
-      const bool dy = S.dyn[e] != 0;
-      vi = dy ? X.zvi : P.vmat[(size_t)e * n + i];
-      vj = dy ? zvj : P.vmat[(size_t)e * n + j];
-    }
-    switch (t) {
-      case 0: v = dl; break;
-      case 1: v = flip((double)aji, sg); break;
-      case 2: v = flip(i2d(ri_cj + ri_rj), sg); break;
-      case 3: case 23: v = flip(i2d(rj_ci), sg); break;
-      case 4: v = flip(i2d(S.indeg[j] + 1 - aij), sg); break;
-      case 5: {
-        int c = 0;
-        const uint32_t *eq = S.tpeq + (aij ? W : 0);
-        for (int w = 0; w < W; ++w)
-          c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);
-        if (S.tp[j] > 0) ++c;
-        v = flip(i2d(c), sg);
-        break;
+  double vi = 0.0, vj = 0.0;
+  if ((t >= 10 && t <= 13) || t == 20 || t == 21 || t == 25 || t == 31) {
+    const bool dy = S.dyn[e] != 0;
+    vi = dy ? X.zvi : P.vmat[(size_t)e * n + i];
+    vj = dy ? __dsub_rn((double)S.z[j], P.zbar) : P.vmat[(size_t)e * n + j];
+  }
+  switch (t) {
+    case 11: return flip(vj, sg);
+    case 12: return flip(__dsub_rn(__dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn(vi, vj)), S.p1[e])), S.p2[e]), sg);
+    case 13: return flip(fabs(__dsub_rn(vi, vj)) < 1e-9 ? 1.0 : 0.0, sg);
+    case 20:
+      if (vi > __dadd_rn(vj, 1e-9)) return dl;
+      if (fabs(__dsub_rn(vi, vj)) <= 1e-9) return flip(0.5, sg);
+      return 0.0;
+    case 21: return __dmul_rn(flip(vi, sg), vj);
+    case 25: return flip(__dadd_rn(vi, vj), sg);
+    case 31: return flip(vj >= __dsub_rn(S.p1[e], 1e-12) ? 1.0 : 0.0, sg);
+    case 29: case 30: {
+      // over h in out_j (29) or in_j (30), h != i, ascending h as the reference
+      // adds: the gw weight difference at p_h = |out_i & in_h| (29) or
+      // |out_i & out_h| (30), both precomputed for this ministep
+      const double *wr = P.wtab + (size_t)e * (n + 1);
+      const uint32_t *B = (t == 29) ? S.rowsT : S.colsT;
+      const int *pc = (t == 29) ? S.tp : S.tq;
+      double acc = 0.0;
+      for (int w = 0; w < W; ++w) {
+        uint32_t m = B[w * n + j];
+        if ((i >> 5) == w) m &= ~(1u << (i & 31));
+        while (m) {
+          const int h = (w << 5) + __ffs(m) - 1;
+          m &= m - 1;
+          const int p = pc[h];
+          acc = __dadd_rn(acc, aij ? __dsub_rn(wr[p], wr[p - 1]) : __dsub_rn(wr[p + 1], wr[p]));
+        }
       }
-      case 6: v = flip(i2d((aji ? ri_cj : 0) + ricirj), sg); break;
-      case 7: v = flip(sqrt(i2d(S.indeg[j] + 1 - aij)), sg); break;
-      case 8: v = flip(i2d(S.outdeg[j]), sg); break;
-      case 9: v = flip(sqrt(i2d(S.outdeg[j])), sg); break;
-      case 10: v = flip(vi, sg); break;
-      case 11: v = flip(vj, sg); break;
-      case 12:
-        v = flip(__dsub_rn(__dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn(vi, vj)), S.p1[e])), S.p2[e]), sg);
-        break;
-      case 13: v = flip(fabs(__dsub_rn(vi, vj)) < 1e-9 ? 1.0 : 0.0, sg); break;
+      return flip(acc, sg);
+    }
+    default: return 0.0;
+  }
+}
+
+// Per-ministep magnitudes of the K_STEP effects (types 10, 14-19): for each
+// (a_ij, a_ji) the reference's d and theta * d, into stepd/stept[e*4 + q],
+// q = 2*a_ij + a_ji. Lanes take (e, q) pairs.
+__device__ __forceinline__ void step_values(const Team &T, const DevProblem &P, const Slice &S,
+                                            const StepCtx &X) {
+  for (int x = T.tl; x < 4 * P.k; x += T.L) {
+    const int e = x >> 2, q = x & 3;
+    if (S.ekind[e] != K_STEP) continue;
+    const int aij = q >> 1, aji = q & 1;
+    const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;
+    const double dl = aij ? -1.0 : 1.0;
+    double v;
+    switch (S.tid[e]) {
+      case 10: v = flip(S.dyn[e] ? X.zvi : P.vmat[(size_t)e * P.n + X.i], sg); break;
       case 14: v = flip(i2d(X.id_i), sg); break;
       case 15: v = flip(sqrt(i2d(X.id_i)), sg); break;
       case 16: v = flip(__dadd_rn(__dmul_rn(2.0, i2d(X.od_i)), dl), sg); break;
@@ -384,45 +400,110 @@ __device__ __forceinline__ void change_stats(const DevProblem &P, const Slice &S
       case 19:
         v = flip(__dadd_rn(i2d(X.rdeg_i), __dmul_rn((double)aji, __dadd_rn(i2d(X.od_i), dl))), sg);
         break;
-      case 20:
-        if (vi > __dadd_rn(vj, 1e-9)) v = dl;
-        else if (fabs(__dsub_rn(vi, vj)) <= 1e-9) v = flip(0.5, sg);
-        else v = 0.0;
-        break;
-      case 21: v = __dmul_rn(flip(vi, sg), vj); break;
-      case 22: v = flip(0.0, sg); break;  // the CPU engine's dyadic covariate is zero-filled
-      case 24: v = flip(P.wtab[(size_t)e * (n + 1) + ri_cj], sg); break;
-      case 25: v = flip(__dadd_rn(vi, vj), sg); break;
-      case 26: v = flip(P.wtab[(size_t)e * (n + 1) + ri_rj], sg); break;
-      case 27: v = flip(P.wtab[(size_t)e * (n + 1) + ci_cj], sg); break;
-      case 28: v = flip(P.wtab[(size_t)e * (n + 1) + ci_rj], sg); break;
-      case 29: case 30: {
-        // over h in out_j (29) or in_j (30), h != i, ascending h as the
-        // reference adds: the gw weight difference at p_h = |out_i & in_h|
-        // (29) or |out_i & out_h| (30), both precomputed for this ministep
-        const double *wr = P.wtab + (size_t)e * (n + 1);
-        const uint32_t *B = (t == 29) ? S.rowsT : S.colsT;
-        const int *pc = (t == 29) ? S.tp : S.tq;
-        double acc = 0.0;
-        for (int w = 0; w < W; ++w) {
-          uint32_t m = B[w * n + j];
-          if ((i >> 5) == w) m &= ~(1u << (i & 31));
-          while (m) {
-            const int h = (w << 5) + __ffs(m) - 1;
-            m &= m - 1;
-            const int p = pc[h];
-            acc = __dadd_rn(acc, aij ? __dsub_rn(wr[p], wr[p - 1]) : __dsub_rn(wr[p + 1], wr[p]));
-          }
-        }
-        v = flip(acc, sg);
-        break;
-      }
-      case 31: v = flip(vj >= __dsub_rn(S.p1[e], 1e-12) ? 1.0 : 0.0, sg); break;
       default: v = 0.0; break;
     }
-    if ((S.ety[e] == 1 && aij) || (S.ety[e] == 2 && !aij)) v = 0.0;
-    d[e] = v;
+    S.stepd[x] = v;
+    S.stept[x] = __dmul_rn(S.th[e], v);
   }
+}
+
+// Change statistics of toggling i -> j for all k effects into d[0..k-1]
+// (src/libcusna_saom_cpu.cpp:49-101 per effect type, :243-261 for the loop with
+// interactions and creation/endowment zeroing), and with TERMS the linear
+// predictor f = sum_e theta_e d_e in the reference's e-order. Popcounts of the
+// word-major bitsets replace the reference's O(n) dense loops; they count the
+// same sets:
+//   |out_i & in_j| = #{h: a_ih a_hj}      |out_i & out_j| = #{h: a_ih a_jh}
+//   |out_j & in_i| = #{h: a_jh a_hi}      |in_i & in_j|   = #{h: a_hi a_hj}
+//   |in_i & out_j| = #{h: a_hi a_jh}
+// Every d and every term equals the reference's float64 value: delta * x is a
+// sign flip, table entries are the reference's expressions evaluated once, and
+// f adds the terms in e-order (terms of zeroed effects are +-0 and change
+// nothing, so they are skipped).
+template <bool TERMS>
+__device__ __forceinline__ double change_stats(const DevProblem &P, const Slice &S,
+                                               const StepCtx &X, int j, int aij, int aji,
+                                               double *d) {
+  const int n = P.n, W = P.W, k = P.k, i = X.i;
+  const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;
+  const int fl = P.flags;
+  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;
+  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
+    const uint32_t *R = S.rowsT, *Cc = S.colsT;
+    for (int w = 0; w < W; ++w) {
+      const uint32_t ri = R[w * n + i], rj = R[w * n + j];
+      const uint32_t ci = Cc[w * n + i], cj = Cc[w * n + j];
+      if (fl & F_PC_RI_CJ) ri_cj += __popc(ri & cj);
+      if (fl & F_PC_RI_RJ) ri_rj += __popc(ri & rj);
+      if (fl & F_PC_RJ_CI) rj_ci += __popc(rj & ci);
+      if (fl & F_PC_CI_CJ) ci_cj += __popc(ci & cj);
+      if (fl & F_PC_CI_RJ) ci_rj += __popc(ci & rj);
+      if (fl & F_PC_RICIRJ) ricirj += __popc(ri & ci & rj);
+    }
+  }
+  const bool ttab = (fl & F_THETA_TAB) != 0;
+  double f = 0.0;
+#pragma unroll 1
+  for (int e = 0; e < k; ++e) {
+    const int kind = S.ekind[e], cfn = S.ecfn[e];
+    double v, term = 0.0;
+    bool has_term = TERMS;
+    if (kind == K_CNT) {
+      int c;
+      switch (cfn) {
+        case 0: c = 1; break;
+        case 1: c = aji; break;
+        case 2: c = ri_cj + ri_rj; break;
+        case 3: c = rj_ci; break;
+        case 4: c = S.indeg[j] + 1 - aij; break;
+        case 5: {
+          c = 0;
+          const uint32_t *eq = S.tpeq + (aij ? W : 0);
+          for (int w = 0; w < W; ++w)
+            c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);
+          if (S.tp[j] > 0) ++c;
+          break;
+        }
+        case 6: c = (aji ? ri_cj : 0) + ricirj; break;
+        default: c = S.outdeg[j]; break;  // 7
+      }
+      v = flip(i2d(c), sg);
+      if (TERMS) term = ttab ? flip(P.tab[S.eofft[e] + c], sg) : __dmul_rn(S.th[e], v);
+    } else if (kind == K_LOOK) {
+      int idx;
+      switch (cfn) {
+        case 4: idx = S.indeg[j] + 1 - aij; break;
+        case 7: idx = S.outdeg[j]; break;
+        case 8: idx = ri_cj; break;
+        case 9: idx = ri_rj; break;
+        case 10: idx = ci_cj; break;
+        case 11: idx = ci_rj; break;
+        case 12: idx = j; break;
+        case 13: idx = S.z[j] - P.zlo; break;
+        case 14: idx = i * n + j; break;
+        default: idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo); break;  // 15
+      }
+      v = flip(P.tab[S.eoffd[e] + idx], sg);
+      if (TERMS) term = ttab ? flip(P.tab[S.eofft[e] + idx], sg) : __dmul_rn(S.th[e], v);
+    } else if (kind == K_STEP) {
+      const int q = 2 * aij + aji;
+      v = S.stepd[4 * e + q];
+      term = S.stept[4 * e + q];
+    } else if (kind == K_ZERO) {
+      v = 0.0;
+      has_term = false;
+    } else {
+      v = gen_stat(P, S, X, e, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, d);
+      if (TERMS) term = __dmul_rn(S.th[e], v);
+    }
+    if ((S.ety[e] == 1 && aij) || (S.ety[e] == 2 && !aij)) {
+      v = 0.0;
+      has_term = false;
+    }
+    d[e] = v;
+    if (has_term) f = __dadd_rn(f, term);
+  }
+  return f;
 }
 
 // Behaviour change statistic, src/libcusna_saom_cpu.cpp:103-113.
