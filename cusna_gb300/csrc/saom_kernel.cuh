@@ -316,7 +316,7 @@ __device__ __forceinline__ double flip(double x, unsigned long long sgn) {
 // Generic change statistic of one effect (src/libcusna_saom_cpu.cpp:49-101 and
 // :246-251): the reference formula evaluated per alter. Used for the kinds no
 // table covers (gwdsp, interactions, dyadic covariates of very large n).
-__device__ __noinline__ double gen_stat(const DevProblem &P, const Slice &S, const StepCtx &X,
+static __device__ __noinline__ double gen_stat(const DevProblem &P, const Slice &S, const StepCtx &X,
                                         int e, int j, int aij, int aji, int ri_cj, int ri_rj,
                                         int rj_ci, int ci_cj, int ci_rj, const double *d) {
   const int n = P.n, W = P.W, i = X.i, t = S.tid[e];
