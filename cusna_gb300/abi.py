@@ -116,6 +116,8 @@ def load_library(path: str | None = None):
     lib.cusna_behavior_stats_gpu.argtypes = [_p, i32, i32, i32, _p, _p, _p,
                                              C.c_double, C.c_double, C.c_double, _p]
     lib.cusna_behavior_stats_gpu.restype = i32
+    lib.cusna_saom_simulate_period_static.argtypes = [P(SaomProblem), P(SaomResult), _p]
+    lib.cusna_saom_simulate_period_static.restype = i32
     lib.cusna_measure_fp64_tflops.argtypes = [P(C.c_double)]
     lib.cusna_measure_fp64_tflops.restype = i32
     if path is None:
@@ -129,6 +131,7 @@ EXPORTED_SYMBOLS = [
     "cusna_abi_version", "cusna_version_string", "cusna_has_cuda", "cusna_last_error",
     "cusna_saom_simulate_period_ex", "cusna_saom_simulate_batch",
     "cusna_network_stats_gpu", "cusna_behavior_stats_gpu", "cusna_measure_fp64_tflops",
+    "cusna_saom_simulate_period_static",
 ]
 
 

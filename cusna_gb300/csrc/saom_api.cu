@@ -808,6 +808,10 @@ cusna_status simulate(const cusna_saom_problem *problems, cusna_saom_result *res
 }
 
 }  // namespace
+
+// Error text for cusna_last_error() from the other translation units.
+void set_last_error(const char *msg) { g_err = msg; }
+
 }  // namespace cusna
 
 using namespace cusna;

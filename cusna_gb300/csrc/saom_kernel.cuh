@@ -336,6 +336,12 @@ static __device__ __noinline__ double gen_stat(const DevProblem &P, const Slice 
     vj = dy ? __dsub_rn((double)S.z[j], P.zbar) : P.vmat[(size_t)e * n + j];
   }
   switch (t) {
+    case 7: return flip(sqrt(i2d(S.indeg[j] + 1 - aij)), sg);
+    case 9: return flip(sqrt(i2d(S.outdeg[j])), sg);
+    case 24: return flip(P.wtab[(size_t)e * (n + 1) + ri_cj], sg);
+    case 26: return flip(P.wtab[(size_t)e * (n + 1) + ri_rj], sg);
+    case 27: return flip(P.wtab[(size_t)e * (n + 1) + ci_cj], sg);
+    case 28: return flip(P.wtab[(size_t)e * (n + 1) + ci_rj], sg);
     case 11: return flip(vj, sg);
     case 12: return flip(__dsub_rn(__dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn(vi, vj)), S.p1[e])), S.p2[e]), sg);
     case 13: return flip(fabs(__dsub_rn(vi, vj)) < 1e-9 ? 1.0 : 0.0, sg);

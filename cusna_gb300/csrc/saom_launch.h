@@ -24,6 +24,7 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
                           uint32_t *cols_scratch, size_t cols_words, cudaStream_t st);
 int period_blocks_per_sm(int threads, size_t dyn_smem);
 long long kernel_launches();  // kernels launched so far by the calling thread
+void set_last_error(const char *msg);  // text of cusna_last_error() for this thread
 cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
                             cudaStream_t st);
 cudaError_t launch_behstats(const int *z, int n, int M, int kb, const int *bty, const uint8_t *xnet,

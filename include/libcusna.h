@@ -249,6 +249,24 @@ CUSNA_API cusna_status cusna_behavior_stats_gpu(
     const int32_t *bty, const uint8_t *xnet, const int32_t *bkdist,
     double zbar, double brange, double bsimmean, double *out);
 
+/* cusna_saom_simulate_period for callers that cannot allocate device memory.
+ * No counterpart in the reference. Callers that cannot call cudaMalloc
+ * include code running while a stream is captured into a CUDA graph, hosts
+ * whose device memory belongs to another allocator, and latency-bound loops
+ * that must not enter the allocator. The call allocates nothing. Every problem
+ * and result pointer must be a device pointer (as with device_ptrs in
+ * cusna_gpu_options), and the work runs on `stream` (a cudaStream_t; NULL for
+ * the default stream). The call returns once the results are written.
+ * Its scratch is one fixed 16 MiB array in device memory. Every GPU that loads
+ * the library holds that array until the process exits. A problem that needs
+ * more scratch is refused with CUSNA_ERR_UNSUPPORTED and the size in
+ * cusna_last_error(). The first call on each device looks up the array's
+ * device address, so make that first call before any stream capture begins.
+ * All calls share the array: calls whose GPU work overlaps, from two streams
+ * or two threads, race on it and must be serialised by the caller. */
+CUSNA_API cusna_status cusna_saom_simulate_period_static(
+    const cusna_saom_problem *problem, cusna_saom_result *result, void *stream);
+
 /* Measured float64 FMA throughput of the current device in TFLOP/s (an FMA
  * counts 2 flops): the peak against which the simulator's float64 work is
  * reported. Runs a short synthetic kernel. */
