@@ -204,3 +204,27 @@ def parity_case(kind: str, seed: int = 0, n: int = 40, M: int = 6):
 
 PARITY_KINDS = ["baseline", "covariate", "structural", "gw", "covariate_all", "interaction",
                 "typed", "coevol", "conditional", "masks", "composition", "symmetric", "rates"]
+
+
+# ---- C1: synthetic 3-wave panel, waves 2-3 simulated ------------------------
+C1_THETA = np.array([-2.5, 2.0, 0.4])
+
+
+def simulate_next_wave(engine, x, effects_names, lam, theta, seed):
+    """One unconditional period from network x with the given effects; the end
+    network of chain 0 is the next wave."""
+    from .glue import marshal_period
+    effs = [E.make_effect_spec(nm) for nm in effects_names]
+    inp = period_inputs(x, effs)
+    m = marshal_period(inp, 1, seed, lam, theta, want_ends=True)
+    return engine.simulate_batch([m])[0]["a_ends"][0].astype(np.int64)
+
+
+def c1_panel(engine, n: int = 50):
+    """Wave 1 Bernoulli(0.05) (seed 1); waves 2 and 3 simulated with rate 6,
+    density -2.5, recip 2.0, transTrip 0.4 (Philox seeds 11 and 12)."""
+    names = ("density", "recip", "transTrip")
+    w1 = bernoulli_net(n, 0.05, seed=1).astype(np.int64)
+    w2 = simulate_next_wave(engine, w1, names, 6.0, C1_THETA, 11)
+    w3 = simulate_next_wave(engine, w2, names, 6.0, C1_THETA, 12)
+    return [w1, w2, w3]

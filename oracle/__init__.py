@@ -82,6 +82,10 @@ class Oracle:
             raise RuntimeError(f"{self.kind} simulate_period status {st}")
         return result_dict(m)
 
+    def simulate_batch(self, ms, threads: int = 0) -> list:
+        """The engine interface of cusna_gb300.mom: one call per period."""
+        return [self.simulate(m, threads=threads) for m in ms]
+
     def network_stats(self, a, n, k, type_ids, p1, p2, vmat, vmiss, dyn_flags, vb, od0, id0,
                       wtab, symflag) -> np.ndarray:
         def c(x, dt):
