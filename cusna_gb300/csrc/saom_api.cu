@@ -670,11 +670,14 @@ LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, boo
   for (int gi = 0; gi < 5; ++gi) {
     const int G = Gs[gi];
     if (force_G && G != force_G) continue;
-    for (int cols_smem = 1; cols_smem >= 0; --cols_smem) {
+    // in-rows, then out-rows move to global scratch when shared memory is short
+    for (int place = 0; place < 3; ++place) {
+      const bool rows_smem = place < 2, cols_smem = place == 0;
       LaunchShape sh{};
       sh.G = G;
       sh.cols_in_smem = cols_smem;
-      sh.lay = make_layout(nmax, Wmax, kmax, kbmax, nrmax, G, cols_smem, tp, gw, tq);
+      sh.rows_in_smem = rows_smem;
+      sh.lay = make_layout(nmax, Wmax, kmax, kbmax, nrmax, G, rows_smem, cols_smem, tp, gw, tq);
       if (sh.lay.bytes > (size_t)c.smem_optin) continue;
       for (int tpc = 1; tpc <= 16; tpc *= 2) {
         if (force_tpc && tpc != force_tpc) continue;
@@ -687,7 +690,8 @@ LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, boo
         const double teams_sm = (double)per_sm * tpc;
         const double chains_sm = (double)total_units / c.sms;
         const double busy_warps = std::min(teams_sm, std::max(chains_sm, 1.0)) * G;
-        const double score = std::min(busy_warps, 48.0) * 100.0 - G - (cols_smem ? 0.0 : 50.0) - tpc * 0.01;
+        const double score = std::min(busy_warps, 48.0) * 100.0 - G - (cols_smem ? 0.0 : 50.0) -
+                             (rows_smem ? 0.0 : 50.0) - tpc * 0.01;
         if (score > best_score) {
           best_score = score;
           best = sh;
@@ -696,7 +700,7 @@ LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, boo
           best.ctas = (int)std::max<long long>(1, std::min<long long>((long long)c.sms * per_sm, want));
         }
       }
-      if (cols_smem && best.G == G) break;  // in-rows fit in shared memory for this G
+      if (best.G == G && best.cols_in_smem == cols_smem && best.rows_in_smem == rows_smem) break;
     }
   }
   return best;
@@ -742,6 +746,7 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
   const size_t teams = (size_t)sh.ctas * sh.teams_per_cta;
   const size_t cols_words = (size_t)Wmax * nmax;
   const size_t o_cols = sh.cols_in_smem ? NONE : pl.take(teams * cols_words * 4);
+  const size_t o_rows = sh.rows_in_smem ? NONE : pl.take(teams * cols_words * 4);
   if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
 
   std::vector<DevProblem> hp(jobs.size());
@@ -758,7 +763,8 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
   CU(cudaEventRecord(g_ctx.ev0, st));
   CU(launch_period(sh, at<DevProblem>(o_probs), at<long long>(o_units), (int)jobs.size(), total,
                    at<unsigned long long>(o_counter),
-                   o_cols == NONE ? nullptr : at<uint32_t>(o_cols), cols_words, st));
+                   o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
+                   o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
   CU(cudaEventRecord(g_ctx.ev1, st));
   if (!dev)
     for (auto &J : jobs)

@@ -36,7 +36,7 @@ struct Team {
 struct Slice {
   uint32_t *rowsT;   // W*n
   uint32_t *colsT;   // W*n (shared or global scratch)
-  int *indeg, *outdeg;
+  short *indeg, *outdeg;  // n each (degrees < 2^15 as n <= 8192)
   int *z;
   double *fbuf;      // n
   float *gbuf;       // n
@@ -73,15 +73,15 @@ __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15
 
 // Layout of one team slice for maxima (n, k, ...) over the launch.
 __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, int nrate, int G,
-                                                   bool cols_in_smem, bool need_tp, bool need_gw,
-                                                   bool need_tq) {
+                                                   bool rows_in_smem, bool cols_in_smem,
+                                                   bool need_tp, bool need_gw, bool need_tq) {
   SliceLayout s{};
   size_t o = 0;
   auto put = [&](size_t &field, size_t bytes) { field = o; o = al16(o + bytes); };
-  put(s.o_rows, (size_t)W * n * 4);
+  put(s.o_rows, rows_in_smem ? (size_t)W * n * 4 : 0);
   put(s.o_cols, cols_in_smem ? (size_t)W * n * 4 : 0);
-  put(s.o_indeg, (size_t)n * 4);
-  put(s.o_outdeg, (size_t)n * 4);
+  put(s.o_indeg, (size_t)n * 2);
+  put(s.o_outdeg, (size_t)n * 2);
   put(s.o_z, (size_t)n * 4);
   put(s.o_f, (size_t)n * 8);
   put(s.o_g, (size_t)n * 4);
@@ -124,12 +124,12 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
 }
 
 __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L,
-                                       uint32_t *cols_global) {
+                                       uint32_t *cols_global, uint32_t *rows_global) {
   Slice s;
-  s.rowsT = (uint32_t *)(base + L.o_rows);
+  s.rowsT = rows_global ? rows_global : (uint32_t *)(base + L.o_rows);
   s.colsT = cols_global ? cols_global : (uint32_t *)(base + L.o_cols);
-  s.indeg = (int *)(base + L.o_indeg);
-  s.outdeg = (int *)(base + L.o_outdeg);
+  s.indeg = (short *)(base + L.o_indeg);
+  s.outdeg = (short *)(base + L.o_outdeg);
   s.z = (int *)(base + L.o_z);
   s.fbuf = (double *)(base + L.o_f);
   s.gbuf = (float *)(base + L.o_g);

@@ -16,12 +16,14 @@ struct LaunchShape {
   int teams_per_cta;  // chains per CTA
   int ctas;           // grid size (persistent: ctas * teams_per_cta resident teams)
   bool cols_in_smem;  // in-rows in shared memory (else global scratch)
+  bool rows_in_smem;  // out-rows in shared memory (else global scratch)
   SliceLayout lay;
 };
 
 cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const long long *unit_start,
                           int nprob, long long total, unsigned long long *counter,
-                          uint32_t *cols_scratch, size_t cols_words, cudaStream_t st);
+                          uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
+                          cudaStream_t st);
 int period_blocks_per_sm(int threads, size_t dyn_smem);
 long long kernel_launches();  // kernels launched so far by the calling thread
 void set_last_error(const char *msg);  // text of cusna_last_error() for this thread

@@ -127,7 +127,7 @@ template <int MAXT>
 __global__ void __launch_bounds__(MAXT, MAXT == 512 ? 1 : CUSNA_MINB_256)
 period_kernel(const DevProblem *__restrict__ probs, const long long *__restrict__ unit_start,
               int nprob, long long total, unsigned long long *counter, SliceLayout lay, int G,
-              uint32_t *cols_scratch, size_t cols_words) {
+              uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words) {
   extern __shared__ __align__(16) unsigned char smem[];
   Team T;
   T.G = G;
@@ -140,7 +140,8 @@ period_kernel(const DevProblem *__restrict__ probs, const long long *__restrict_
   const int teams_per_cta = blockDim.x / T.L;
   const size_t slot = (size_t)blockIdx.x * teams_per_cta + tw;
   Slice S = carve(smem + (size_t)tw * lay.bytes, lay,
-                  cols_scratch ? cols_scratch + slot * cols_words : nullptr);
+                  cols_scratch ? cols_scratch + slot * cols_words : nullptr,
+                  rows_scratch ? rows_scratch + slot * cols_words : nullptr);
   for (;;) {
     long long u = 0;
     if (T.tl == 0) u = (long long)atomicAdd(counter, 1ull);
@@ -348,14 +349,15 @@ int period_blocks_per_sm(int threads, size_t dyn_smem) {
 
 cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const long long *unit_start,
                           int nprob, long long total, unsigned long long *counter,
-                          uint32_t *cols_scratch, size_t cols_words, cudaStream_t st) {
+                          uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
+                          cudaStream_t st) {
   const int threads = 32 * sh.G * sh.teams_per_cta;
   const size_t dyn = sh.lay.bytes * sh.teams_per_cta;
   auto kern = threads <= 256 ? period_kernel<256> : period_kernel<512>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
   if (e != cudaSuccess) return e;
   kern<<<sh.ctas, threads, dyn, st>>>(probs, unit_start, nprob, total, counter, sh.lay, sh.G,
-                                      cols_scratch, cols_words);
+                                      cols_scratch, rows_scratch, cols_words);
   return counted(cudaGetLastError());
 }
 

@@ -201,7 +201,8 @@ extern "C" CUSNA_API cusna_status cusna_saom_simulate_period_static(
       LaunchShape sh{};
       sh.G = G;
       sh.cols_in_smem = cs;
-      sh.lay = make_layout(n, W, k, kb, nr, G, cs, need_tp, need_gw, need_tq);
+      sh.rows_in_smem = true;
+      sh.lay = make_layout(n, W, k, kb, nr, G, true, cs, need_tp, need_gw, need_tq);
       if (sh.lay.bytes > (size_t)smem_optin) continue;
       for (int tpc = 1; tpc <= 16; tpc *= 2) {
         const int threads = 32 * G * tpc;
@@ -336,7 +337,7 @@ extern "C" CUSNA_API cusna_status cusna_saom_simulate_period_static(
   SCU(cudaMemsetAsync(base + oCnt, 0, sizeof(unsigned long long), s));  // work counter starts at 0
   SCU(launch_period(best, (const DevProblem *)(base + oProb), (const long long *)(base + oUnits), 1,
                     (long long)M, (unsigned long long *)(base + oCnt),
-                    best.cols_in_smem ? nullptr : U32(oCols), (size_t)W * n, s));
+                    best.cols_in_smem ? nullptr : U32(oCols), nullptr, (size_t)W * n, s));
   SCU(cudaStreamSynchronize(s));
   return CUSNA_OK;
 }

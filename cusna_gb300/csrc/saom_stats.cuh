@@ -32,9 +32,10 @@ struct StatDesc {
 
 // Statistics of the network in (R, C) (word-major rows / in-rows) with degrees
 // outdeg/indeg already filled. out[k] is written by team lane 0.
+template <class DegT>
 __device__ inline void network_stats_team(const Team &T, const StatDesc &D, const uint32_t *R,
-                                   const uint32_t *Cc, const int *outdeg, const int *indeg,
-                                   double *red, double *out) {
+                                          const uint32_t *Cc, const DegT *outdeg,
+                                          const DegT *indeg, double *red, double *out) {
   const int n = D.n, W = D.W, k = D.k;
   for (int e = 0; e < k; ++e) {
     const int t = D.type_ids[e];

@@ -185,3 +185,11 @@ def test_gpu_error_statuses(gpu_lib):
     assert lib.cusna_saom_simulate_period(C.byref(m.problem), C.byref(m.result)) == ERR_NULL_ARG
     with pytest.raises(CudaError):
         G.simulate(m)
+
+
+def test_gpu_large_n_rows_in_global_scratch(gpu_lib, port):
+    """n = 1500 (out-rows and in-rows 282 KB each, beyond shared memory): the
+    chain state moves to global scratch and the trajectory is unchanged."""
+    c = WL.parity_case("conditional", seed=3, n=1500, M=2)
+    c["inp"].target_dist = 400
+    assert_parity(run_case(GpuEngine(), c), run_case(port, c), "n1500")
