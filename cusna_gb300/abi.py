@@ -120,6 +120,22 @@ def load_library(path: str | None = None):
     lib.cusna_saom_simulate_period_static.restype = i32
     lib.cusna_measure_fp64_tflops.argtypes = [P(C.c_double)]
     lib.cusna_measure_fp64_tflops.restype = i32
+    sz, f32 = C.c_size_t, C.c_float
+    lib.cusna_mlp_param_count.argtypes = [i32, i32, i32]
+    lib.cusna_mlp_param_count.restype = sz
+    lib.cusna_mlp_workspace_bytes.argtypes = [i32, i32, i32, i32]
+    lib.cusna_mlp_workspace_bytes.restype = sz
+    lib.cusna_mlp_init.argtypes = [_p, i32, i32, i32, C.c_uint64, _p]
+    lib.cusna_mlp_init.restype = i32
+    lib.cusna_mlp_forward.argtypes = [_p, _p, i32, _p, _p, sz, i32, i32, i32, _p]
+    lib.cusna_mlp_forward.restype = i32
+    lib.cusna_mlp_grad.argtypes = [_p, _p, _p, _p, i32, _p, _p, _p, sz, i32, i32, i32, _p]
+    lib.cusna_mlp_grad.restype = i32
+    lib.cusna_mlp_train_step.argtypes = [_p, _p, _p, _p, _p, _p, _p, i32, i32, f32, f32, f32,
+                                         f32, _p, _p, sz, i32, i32, i32, _p]
+    lib.cusna_mlp_train_step.restype = i32
+    lib.cusna_mlp_jacobian.argtypes = [_p, _p, i32, i32, _p, _p, _p, sz, i32, i32, i32, _p]
+    lib.cusna_mlp_jacobian.restype = i32
     if path is None:
         _lib = lib
     return lib
@@ -132,6 +148,8 @@ EXPORTED_SYMBOLS = [
     "cusna_saom_simulate_period_ex", "cusna_saom_simulate_batch",
     "cusna_network_stats_gpu", "cusna_behavior_stats_gpu", "cusna_measure_fp64_tflops",
     "cusna_saom_simulate_period_static",
+    "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",
+    "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_jacobian",
 ]
 
 

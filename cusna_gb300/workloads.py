@@ -228,3 +228,35 @@ def c1_panel(engine, n: int = 50):
     w2 = simulate_next_wave(engine, w1, names, 6.0, C1_THETA, 11)
     w3 = simulate_next_wave(engine, w2, names, 6.0, C1_THETA, 12)
     return [w1, w2, w3]
+
+
+# ---- C5: surrogate-assisted MoM panel ---------------------------------------
+C5_LAMBDA = 7.0
+C5_THETA = np.array([-2.6, 2.0, 0.35, -0.15, 0.04, 0.1, 0.9])
+C5_EFFECTS = ["density", "recip", "transTrip", "cycle3", "inPop", "altX", "simX"]
+
+
+def c5_effects(cov):
+    """The seven evaluation effects of the n=300 surrogate panel."""
+    return [E.make_effect_spec(nm, cov if nm.endswith("X") else None) for nm in C5_EFFECTS]
+
+
+def c5_panel(engine, n: int = 300):
+    """Wave 1 Bernoulli(0.03) (seed 7), covariate N(0,1) (seed 8); waves 2 and 3
+    simulated with rate 7 and C5_THETA (Philox seeds 21 and 22). Returns
+    (waves, covariate)."""
+    from .glue import marshal_period
+    cov = normal_cov(n, seed=8)
+    effs = c5_effects(cov)
+    waves = [bernoulli_net(n, 0.03, seed=7).astype(np.int64)]
+    for seed in (21, 22):
+        m = marshal_period(period_inputs(waves[-1], effs), 1, seed, C5_LAMBDA, C5_THETA,
+                           want_ends=True)
+        waves.append(engine.simulate_batch([m])[0]["a_ends"][0].astype(np.int64))
+    return waves, cov
+
+
+def c5_theta_true() -> np.ndarray:
+    """The data-generating parameter vector in the unconditional estimator's
+    layout (rate per period, then the evaluation effects)."""
+    return np.concatenate([[C5_LAMBDA, C5_LAMBDA], C5_THETA])

@@ -272,6 +272,53 @@ CUSNA_API cusna_status cusna_saom_simulate_period_static(
  * reported. Runs a short synthetic kernel. */
 CUSNA_API cusna_status cusna_measure_fp64_tflops(double *tflops);
 
+/* ---- moment surrogate (no counterpart in the reference) --------------------
+ * A multilayer perceptron n_in -> hidden -> hidden -> n_out with GELU
+ * activations, used by the estimator to stand in for simulated moments in
+ * Robbins-Monro phases 1-2. Products run on the tensor cores with bfloat16
+ * operands and float32 accumulation; parameters, gradients and Adam moments are
+ * float32 in one buffer of cusna_mlp_param_count() floats laid out
+ * [W1 (hidden x n_in) | b1 | W2 (hidden x hidden) | b2 | W3 (n_out x hidden) | b3].
+ * n_in and hidden are multiples of 16 (hidden <= 4096), 1 <= n_out <= 16.
+ * Every pointer is a device pointer; work is a device workspace of at least
+ * cusna_mlp_workspace_bytes(.., batch) bytes (work_bytes, checked); the work
+ * runs asynchronously on `stream` (a cudaStream_t, NULL for the default). */
+CUSNA_API size_t cusna_mlp_param_count(int32_t n_in, int32_t hidden, int32_t n_out);
+CUSNA_API size_t cusna_mlp_workspace_bytes(int32_t n_in, int32_t hidden, int32_t n_out,
+                                           int32_t batch);
+/* He-normal hidden-layer weights from a Philox stream keyed by seed; the
+ * output layer and the biases start at zero (the untrained network predicts
+ * zero). */
+CUSNA_API cusna_status cusna_mlp_init(float *params, int32_t n_in, int32_t hidden,
+                                      int32_t n_out, uint64_t seed, void *stream);
+/* y[batch x n_out] = network(x[batch x n_in]). */
+CUSNA_API cusna_status cusna_mlp_forward(const float *params, const float *x, int32_t batch,
+                                         float *y, void *work, size_t work_bytes, int32_t n_in,
+                                         int32_t hidden, int32_t n_out, void *stream);
+/* Mean squared error of the network on rows rows[0..batch) of x and t (rows
+ * NULL: the first batch rows) and its gradient with respect to every parameter
+ * into grad; *loss (device, may be NULL) receives the loss. batch is a multiple
+ * of 16. */
+CUSNA_API cusna_status cusna_mlp_grad(const float *params, const float *x, const float *t,
+                                      const int32_t *rows, int32_t batch, float *grad,
+                                      float *loss, void *work, size_t work_bytes, int32_t n_in,
+                                      int32_t hidden, int32_t n_out, void *stream);
+/* cusna_mlp_grad followed by one Adam step (step = 1, 2, ...; bias-corrected)
+ * on params with moment buffers adam_m and adam_v. */
+CUSNA_API cusna_status cusna_mlp_train_step(float *params, float *grad, float *adam_m,
+                                            float *adam_v, const float *x, const float *t,
+                                            const int32_t *rows, int32_t batch, int32_t step,
+                                            float lr, float beta1, float beta2, float eps,
+                                            float *loss, void *work, size_t work_bytes,
+                                            int32_t n_in, int32_t hidden, int32_t n_out,
+                                            void *stream);
+/* Outputs y[batch x n_out] and their Jacobian J[batch x n_out x n_wrt] with
+ * respect to the first n_wrt inputs (forward-mode, float32). */
+CUSNA_API cusna_status cusna_mlp_jacobian(const float *params, const float *x, int32_t batch,
+                                          int32_t n_wrt, float *y, float *J, void *work,
+                                          size_t work_bytes, int32_t n_in, int32_t hidden,
+                                          int32_t n_out, void *stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif
