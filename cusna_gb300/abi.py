@@ -134,6 +134,9 @@ def load_library(path: str | None = None):
     lib.cusna_mlp_train_step.argtypes = [_p, _p, _p, _p, _p, _p, _p, i32, i32, f32, f32, f32,
                                          f32, _p, _p, sz, i32, i32, i32, _p]
     lib.cusna_mlp_train_step.restype = i32
+    lib.cusna_mlp_train_steps.argtypes = [_p, _p, _p, _p, _p, _p, _p, i32, i32, _p, _p, _p, sz,
+                                          i32, i32, i32, i32, _p]
+    lib.cusna_mlp_train_steps.restype = i32
     lib.cusna_mlp_jacobian.argtypes = [_p, _p, i32, i32, _p, _p, _p, sz, i32, i32, i32, _p]
     lib.cusna_mlp_jacobian.restype = i32
     if path is None:
@@ -149,8 +152,19 @@ EXPORTED_SYMBOLS = [
     "cusna_network_stats_gpu", "cusna_behavior_stats_gpu", "cusna_measure_fp64_tflops",
     "cusna_saom_simulate_period_static",
     "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",
-    "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_jacobian",
+    "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_train_steps", "cusna_mlp_jacobian",
 ]
+
+# cusna_adam_hyper: int32 step, float lr, beta1, beta2, eps, c1, c2
+ADAM_HYPER = np.dtype([("step", "<i4"), ("lr", "<f4"), ("beta1", "<f4"), ("beta2", "<f4"),
+                       ("eps", "<f4"), ("c1", "<f4"), ("c2", "<f4")])
+
+
+def adam_hyper_bytes(step=0, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8) -> np.ndarray:
+    """The bytes of a cusna_adam_hyper block (uint8 array) for a device copy."""
+    h = np.zeros(1, dtype=ADAM_HYPER)
+    h["step"], h["lr"], h["beta1"], h["beta2"], h["eps"] = step, lr, beta1, beta2, eps
+    return h.view(np.uint8).copy()
 
 
 def ptr(a) -> int | None:

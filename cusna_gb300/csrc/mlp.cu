@@ -14,6 +14,8 @@
 
 #include <cstdint>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "libcusna.h"
 #include "saom_common.cuh"
@@ -234,6 +236,29 @@ __global__ void adam_step(float *__restrict__ p, const float *__restrict__ g, fl
   }
 }
 
+// Device-side Adam bookkeeping, so that a sequence of steps has no host
+// arguments that change from step to step (and can be replayed as a graph).
+__global__ void adam_bump(cusna_adam_hyper *h) {
+  const int step = h->step + 1;
+  h->step = step;
+  h->c1 = 1.f - powf(h->beta1, (float)step);
+  h->c2 = 1.f - powf(h->beta2, (float)step);
+}
+
+__global__ void adam_step_dev(float *__restrict__ p, const float *__restrict__ g,
+                              float *__restrict__ m, float *__restrict__ v, size_t n,
+                              const cusna_adam_hyper *__restrict__ h) {
+  const float lr = h->lr, b1 = h->beta1, b2 = h->beta2, eps = h->eps, c1 = h->c1, c2 = h->c2;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
 // Gaussian initialisation N(0, scale^2) from the Philox generator (Box-Muller).
 __global__ void init_normal(float *p, size_t n, float scale, uint32_t k0, uint32_t k1, uint32_t tag) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -435,6 +460,89 @@ cusna_status grad_impl(const float *params, const float *x, const float *t, cons
   return CUSNA_OK;
 }
 
+struct TrainArgs {
+  float *params, *grad, *m, *v;
+  const float *x, *t;
+  const int32_t *rows;
+  int B, n_steps;
+  cusna_adam_hyper *hyper;
+  float *losses;
+  void *work;
+  size_t work_bytes;
+  int n_in, H, n_out;
+  bool operator==(const TrainArgs &o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
+};
+
+// n_steps minibatch steps: step s uses rows[s*B .. (s+1)*B) (rows NULL: rows
+// 0..B every step), then Adam with the device-side step counter.
+cusna_status train_steps_impl(const TrainArgs &a, cudaStream_t st) {
+  const size_t n = (size_t)a.H * a.n_in + a.H + (size_t)a.H * a.H + a.H + (size_t)a.n_out * a.H + a.n_out;
+  for (int s = 0; s < a.n_steps; ++s) {
+    cusna_status r = grad_impl(a.params, a.x, a.t, a.rows ? a.rows + (size_t)s * a.B : nullptr, a.B,
+                               a.grad, a.losses ? a.losses + s : nullptr, a.work, a.work_bytes,
+                               a.n_in, a.H, a.n_out, st);
+    if (r != CUSNA_OK) return r;
+    adam_bump<<<1, 1, 0, st>>>(a.hyper);
+    adam_step_dev<<<blocks_for(n), 256, 0, st>>>(a.params, a.grad, a.m, a.v, n, a.hyper);
+    MCU(cudaGetLastError());
+  }
+  return CUSNA_OK;
+}
+
+// Instantiated graphs of train_steps_impl, one per distinct argument set
+// (pointers and sizes; the values behind the pointers may change between
+// replays). A few entries, oldest evicted first.
+struct GraphEntry {
+  int device;
+  TrainArgs args;
+  cudaGraphExec_t exec;
+};
+constexpr size_t kMaxGraphs = 8;
+std::mutex g_graph_mu;
+std::vector<GraphEntry> g_graphs;
+
+cusna_status replay_train_graph(const TrainArgs &a, cudaStream_t st) {
+  int dev = 0;
+  MCU(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_graph_mu);
+  for (auto &e : g_graphs)
+    if (e.device == dev && e.args == a) {
+      MCU(cudaGraphLaunch(e.exec, st));
+      return CUSNA_OK;
+    }
+  cudaStream_t cap = nullptr;
+  MCU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaError_t e0 = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e0 != cudaSuccess) {
+    cudaStreamDestroy(cap);
+    set_last_error(cudaGetErrorString(e0));
+    return CUSNA_ERR_CUDA;
+  }
+  cusna_status r = train_steps_impl(a, cap);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e1 = cudaStreamEndCapture(cap, &graph);   // ends the capture on every path
+  cudaStreamDestroy(cap);
+  if (r != CUSNA_OK || e1 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    if (r == CUSNA_OK) set_last_error(cudaGetErrorString(e1));
+    return r != CUSNA_OK ? r : CUSNA_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e2 = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e2 != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e2));
+    return CUSNA_ERR_CUDA;
+  }
+  if (g_graphs.size() >= kMaxGraphs) {
+    cudaGraphExecDestroy(g_graphs.front().exec);
+    g_graphs.erase(g_graphs.begin());
+  }
+  g_graphs.push_back(GraphEntry{dev, a, exec});
+  MCU(cudaGraphLaunch(exec, st));
+  return CUSNA_OK;
+}
+
 }  // namespace
 }  // namespace cusna
 
@@ -516,6 +624,26 @@ CUSNA_API cusna_status cusna_mlp_train_step(float *params, float *grad, float *a
                                            c1, c2);
   MCU(cudaGetLastError());
   return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_mlp_train_steps(float *params, float *grad, float *adam_m,
+                                             float *adam_v, const float *x, const float *t,
+                                             const int32_t *rows, int32_t batch, int32_t n_steps,
+                                             cusna_adam_hyper *hyper, float *losses, void *work,
+                                             size_t work_bytes, int32_t n_in, int32_t hidden,
+                                             int32_t n_out, int32_t use_graph, void *stream) {
+  if (!params || !grad || !adam_m || !adam_v || !x || !t || !hyper || !work)
+    return CUSNA_ERR_NULL_ARG;
+  if (n_steps < 1 || n_steps > (1 << 16)) return CUSNA_ERR_SHAPE;
+  cusna_status s = check_call(n_in, hidden, n_out, batch, true, work_bytes);
+  if (s != CUSNA_OK) return s;
+  TrainArgs a;
+  std::memset(&a, 0, sizeof(a));   // padding too: graphs are looked up by memcmp
+  a.params = params; a.grad = grad; a.m = adam_m; a.v = adam_v; a.x = x; a.t = t; a.rows = rows;
+  a.B = batch; a.n_steps = n_steps; a.hyper = hyper; a.losses = losses; a.work = work;
+  a.work_bytes = work_bytes; a.n_in = n_in; a.H = hidden; a.n_out = n_out;
+  cudaStream_t st = (cudaStream_t)stream;
+  return use_graph ? replay_train_graph(a, st) : train_steps_impl(a, st);
 }
 
 CUSNA_API cusna_status cusna_mlp_jacobian(const float *params, const float *x, int32_t batch,

@@ -39,7 +39,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import mom
-from .abi import check, load_library
+from .abi import adam_hyper_bytes, check, load_library
 
 N_IN = 16          # surrogate input width: period parameters + start-wave features
 HIDDEN = 256
@@ -93,6 +93,7 @@ class MlpSurrogate:
         self.n_group = 0
         self.r_sd = np.ones(self.n_out)
         self.alpha = np.ones(self.n_out)  # per-output gate of the network term
+        self.use_graph = True             # replay each training epoch from a CUDA graph
         self.history: list = []
 
     def _stream(self):
@@ -222,17 +223,22 @@ class MlpSurrogate:
         st = self._stream()
         t0 = time.perf_counter()
         best, best_params = np.inf, None
+        # one epoch = `steps` Adam steps replayed from a CUDA graph: the
+        # permutation buffer and the learning rate (device-side) change
+        # between replays, the arguments do not
+        perm = torch.empty(len(tr), dtype=torch.int32, device=self.dev)
+        hyper = torch.from_numpy(adam_hyper_bytes(self.step, lr)).to(self.dev)
         for ep in range(epochs):
-            perm = torch.from_numpy(rng.permutation(tr).astype(np.int32)).to(self.dev)
+            perm.copy_(torch.from_numpy(rng.permutation(tr).astype(np.int32)))
             lr_ep = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * ep / max(epochs, 1)))
-            for s in range(steps):
-                self.step += 1
-                st_ = self.lib.cusna_mlp_train_step(
-                    self.params.data_ptr(), self.grad.data_ptr(), self.adam_m.data_ptr(),
-                    self.adam_v.data_ptr(), Xs.data_ptr(), Ys.data_ptr(),
-                    perm.data_ptr() + 4 * s * batch, batch, self.step, float(lr_ep), 0.9, 0.999,
-                    1e-8, losses.data_ptr() + 4 * s, wp, wb, self.n_in, self.hidden, self.n_out, st)
-                check(st_, "cusna_mlp_train_step", self.lib)
+            hyper[4:8].copy_(torch.from_numpy(np.array([lr_ep], dtype=np.float32).view(np.uint8)))
+            st_ = self.lib.cusna_mlp_train_steps(
+                self.params.data_ptr(), self.grad.data_ptr(), self.adam_m.data_ptr(),
+                self.adam_v.data_ptr(), Xs.data_ptr(), Ys.data_ptr(), perm.data_ptr(), batch,
+                steps, hyper.data_ptr(), losses.data_ptr(), wp, wb, self.n_in, self.hidden,
+                self.n_out, 1 if self.use_graph else 0, st)
+            check(st_, "cusna_mlp_train_steps", self.lib)
+            self.step += steps
             rec = dict(epoch=ep, lr=lr_ep, train=float(losses.mean().item()))
             if n_val:
                 rec["val"] = self._std_mse(Xs[val_idx], Ys[val_idx])
@@ -354,8 +360,7 @@ class Stage:
     epochs: int = 40
 
 
-DEFAULT_STAGES = (Stage(0.25, "iso", 0.5, 80), Stage(0.25, "se", 4.0, 80),
-                  Stage(0.5, "se", 2.0, 120))
+DEFAULT_STAGES = (Stage(0.25, "iso", 0.5, 80), Stage(0.75, "se", 2.0, 100))
 
 
 @dataclass
@@ -368,7 +373,9 @@ class SurrogateControl:
     lr: float = 2e-3
     bound: float = 0.1            # judge bound on surrogate error and t-ratios
     max_takeovers: int = 3        # plain Newton corrections after the judge fails
-    pilot: int = 1000             # chains of the plain pilot between stages
+    pilot: int = 1000             # chains of each plain pilot between stages
+    max_pilots: int = 4           # pilots between two stages at most
+    pilot_tol: float = 1.0        # stop piloting once a step is below this many SEs
     seed: int = 4321
 
 
@@ -445,17 +452,17 @@ def training_pairs(est: mom.Estimator, theta, rng, engine, feats):
 
 def pilot_correction(est: mom.Estimator, sur: PanelSurrogate, theta, M, rng, engine, box):
     """Plain simulation between stages: M chains at theta give the simulated
-    mean and the covariance S of the summed statistics. Returns the Newton
-    point theta - D^-1 (mean - targets) with D the surrogate's Jacobian
-    (guarded, and kept within the surrogate's trust region `box` widened by
-    its own width on each side), and the Cholesky factor of D^-1 S D^-T (the
-    sandwich covariance, one simulation's) that scales the next stage's
-    design; falls back to its diagonal when it is not positive definite."""
+    mean, the covariance S of the summed statistics and the score-function
+    derivative D (R/mom.R:173-182, as plain phase 1 estimates it). Returns the
+    Newton point theta - D^-1 (mean - targets) (guarded, and kept within the
+    surrogate's trust region `box` widened by its own width on each side),
+    the Cholesky factor of D^-1 S D^-T (the sandwich covariance, one
+    simulation's) that scales the next stage's design (its diagonal when not
+    positive definite), the simulated mean and the statistics' SDs."""
     s = mom.mom_simulate(est, theta, M, rng, engine)
     mean = s.stats.mean(axis=0)
     S = np.atleast_2d(np.cov(s.stats, rowvar=False))
-    _, Dm = sur.mean_and_jacobian(theta)
-    Di = mom.safe_solve(Dm)
+    Di = mom.safe_solve(mom.mom_derivative(s.pieces))
     lo, hi = box
     nxt = np.clip(theta - mom.guard_step(est, theta, Di @ (mean - est.targets)),
                   lo - (hi - lo), hi + (hi - lo))
@@ -542,11 +549,21 @@ def mom_run_surrogate(est: mom.Estimator, centre, scontrol: SurrogateControl | N
                    train_seconds=info["seconds"], val=info.get("best_val"),
                    gate=net.alpha.copy())
         if i + 1 < len(sc.stages):
+            # plain pilots with the surrogate's Jacobian (quasi-Newton) until
+            # the step is below pilot_tol standard errors in every coordinate
             ta = time.perf_counter()
-            theta, chol, pmean, psd = pilot_correction(est, sur, theta, sc.pilot, rng, engine, box)
+            rec["pilot_steps"] = []
+            for _ in range(sc.max_pilots):
+                prev = theta
+                theta, chol, pmean, psd = pilot_correction(est, sur, theta, sc.pilot, rng, engine, box)
+                n_pilot += sc.pilot
+                step_se = float(np.max(np.abs(theta - prev) / np.sqrt(np.diag(chol @ chol.T)).clip(1e-300)))
+                rec["pilot_steps"].append(step_se)
+                if "pilot_error" not in rec:
+                    rec["pilot_error"] = np.abs(pmean - sur.mean(prev)) / psd
+                if step_se < sc.pilot_tol:
+                    break
             times["pilot"] = times.get("pilot", 0.0) + time.perf_counter() - ta
-            n_pilot += sc.pilot
-            rec["pilot_error"] = np.abs(pmean - sur.mean(rec["theta"])) / psd
             rec["theta_corrected"] = theta.copy()
         stages.append(rec)
         if verbose:

@@ -312,6 +312,29 @@ CUSNA_API cusna_status cusna_mlp_train_step(float *params, float *grad, float *a
                                             float *loss, void *work, size_t work_bytes,
                                             int32_t n_in, int32_t hidden, int32_t n_out,
                                             void *stream);
+/* Adam hyperparameters and step counter in device memory: each step adds one
+ * to `step` and writes the bias corrections c1 = 1 - beta1^step and
+ * c2 = 1 - beta2^step on the device, so the host may change lr between calls
+ * by writing it, without changing any argument. */
+typedef struct cusna_adam_hyper {
+    int32_t step;
+    float lr, beta1, beta2, eps;
+    float c1, c2;
+} cusna_adam_hyper;
+/* n_steps Adam steps on consecutive minibatches: step s uses rows
+ * rows[s*batch .. (s+1)*batch) of x and t (rows NULL: rows 0..batch each
+ * step); losses[s] (device, may be NULL) receives step s's loss. With
+ * use_graph != 0 the sequence is captured once into a CUDA graph per distinct
+ * argument set (a few are cached, oldest evicted) and replayed on `stream`;
+ * the contents of rows, x, t and *hyper may change between replays. Graph
+ * capture uses a private stream: the first call with a new argument set must
+ * not itself run inside a stream capture. */
+CUSNA_API cusna_status cusna_mlp_train_steps(float *params, float *grad, float *adam_m,
+                                             float *adam_v, const float *x, const float *t,
+                                             const int32_t *rows, int32_t batch, int32_t n_steps,
+                                             cusna_adam_hyper *hyper, float *losses, void *work,
+                                             size_t work_bytes, int32_t n_in, int32_t hidden,
+                                             int32_t n_out, int32_t use_graph, void *stream);
 /* Outputs y[batch x n_out] and their Jacobian J[batch x n_out x n_wrt] with
  * respect to the first n_wrt inputs (forward-mode, float32). */
 CUSNA_API cusna_status cusna_mlp_jacobian(const float *params, const float *x, int32_t batch,

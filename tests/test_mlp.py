@@ -237,3 +237,55 @@ def test_gpu_training_learns_a_smooth_map():
     Yt = np.tanh(Xt @ A) + 0.5 * (Xt[:, :8] ** 2)
     r2 = 1 - ((net.predict(Xt) - Yt) ** 2).sum() / ((Yt - Yt.mean(axis=0)) ** 2).sum()
     assert r2 > 0.9, r2
+
+
+@pytest.mark.gpu
+def test_gpu_train_steps_graph_replay_is_identical_to_direct_launches():
+    """cusna_mlp_train_steps replayed from its CUDA graph gives bit-identical
+    parameters to the same steps launched directly, across two replays with
+    new minibatch rows and a new learning rate written between them; both
+    agree with the single-step entry point up to float32 rounding of the
+    bias corrections (device powf against host powf)."""
+    from cusna_gb300.abi import adam_hyper_bytes
+    g = _Gpu()
+    B, S = 32, 3
+    p, X, T = _problem(seed=13, B=256)
+    w, nb = g.work(B)
+    rng = np.random.Generator(np.random.PCG64(2))
+    rows1 = rng.permutation(256)[:B * S].astype(np.int32)
+    rows2 = rng.permutation(256)[:B * S].astype(np.int32)
+    Xd, Td = g.t(X), g.t(T)
+    out = []
+    for graph in (1, 0):
+        P = g.t(p)
+        grad, m, v = (g.torch.zeros(len(p), device=g.dev) for _ in range(3))
+        rows = g.torch.empty(B * S, dtype=g.torch.int32, device=g.dev)
+        hyper = g.torch.from_numpy(adam_hyper_bytes(0, 1e-3)).to(g.dev)
+        losses = g.torch.zeros(S, device=g.dev)
+        for rr, lr in ((rows1, 1e-3), (rows2, 5e-4)):
+            rows.copy_(g.torch.from_numpy(rr))
+            hyper[4:8].copy_(g.torch.from_numpy(np.array([lr], np.float32).view(np.uint8)))
+            st = g.lib.cusna_mlp_train_steps(P.data_ptr(), grad.data_ptr(), m.data_ptr(),
+                                             v.data_ptr(), Xd.data_ptr(), Td.data_ptr(),
+                                             rows.data_ptr(), B, S, hyper.data_ptr(),
+                                             losses.data_ptr(), w.data_ptr(), nb, N_IN, H, N_OUT,
+                                             graph, None)
+            assert st == 0
+        g.torch.cuda.synchronize()
+        assert int(hyper[:4].cpu().numpy().view(np.int32)[0]) == 2 * S
+        out.append(P.double().cpu().numpy())
+    np.testing.assert_array_equal(out[0], out[1])
+    # the single-step entry point, host-side bias corrections
+    P = g.t(p)
+    grad, m, v = (g.torch.zeros(len(p), device=g.dev) for _ in range(3))
+    step = 0
+    for rr, lr in ((rows1, 1e-3), (rows2, 5e-4)):
+        rows = g.t(rr, g.torch.int32)
+        for s in range(S):
+            step += 1
+            assert g.lib.cusna_mlp_train_step(P.data_ptr(), grad.data_ptr(), m.data_ptr(),
+                                              v.data_ptr(), Xd.data_ptr(), Td.data_ptr(),
+                                              rows.data_ptr() + 4 * s * B, B, step, lr, 0.9,
+                                              0.999, 1e-8, None, w.data_ptr(), nb, N_IN, H,
+                                              N_OUT, None) == 0
+    np.testing.assert_allclose(P.double().cpu().numpy(), out[0], rtol=0, atol=1e-6)
