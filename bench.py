@@ -19,6 +19,11 @@ Under torchrun each rank simulates its own chains (chain offset rank*M, one
 Philox key), so the work per GPU is fixed (weak scaling); value is the sum of
 the ranks' ministeps over the slowest rank's time.
 
+  mom_fit  (1 GPU, unless --no-mom) the second metric: MoM fit wall time on
+         the n=300 panel, plain GPU Robbins-Monro against the surrogate-assisted
+         fit, with both fits' convergence t-ratios, their estimates' agreement
+         in SE units and the number of period simulations each needed
+
 --impl reference times the reference's CPU engine on the host cores on a
 bounded sample of the same workload (oracle/_ref where it was compiled from
 the reference sources, else the oracle's C restatement).
@@ -199,6 +204,51 @@ def cpu_baseline(args, inp, M, seed, lam, theta, lamb, thetab):
             "sample": f"{sample} of the {M} chains ({st} ministeps, {dt:.1f} s)"}
 
 
+def mom_fit_comparison(n3_check=True):
+    """MoM fit wall time on the n=300 surrogate panel: plain GPU Robbins-Monro
+    (phases 1-3 of R/mom.R) against the surrogate-assisted fit, both started
+    from the same prior estimate (the data-generating theta, which the
+    surrogate's first training design is centred on). Both paths are warmed up
+    first (simulator, network kernels, graph capture); each fit is timed once
+    on the host clock."""
+    from cusna_gb300 import data as D
+    from cusna_gb300 import mom
+    from cusna_gb300 import surrogate as S
+    eng = mom.GpuEngine()
+    waves, cov = WL.c5_panel(eng)
+    est = mom.mom_estimator(D.build_saom_data(waves), WL.c5_effects(cov), None, None, False,
+                            dict(mom.DEFAULT_CONTROL), engine=eng)
+    centre = WL.c5_theta_true()
+    # warm-up: one small simulation round and a tiny network fit
+    mom.mom_simulate(est, centre, 256, np.random.default_rng(0), eng)
+    r = np.random.default_rng(0)
+    S.MlpSurrogate(S.N_IN, est.k + 1, S.HIDDEN).fit(r.standard_normal((2048, S.N_IN)),
+                                                      r.standard_normal((2048, est.k + 1)),
+                                                      epochs=2, n_group=S.N_IN - est.k - 1)
+    sf = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng)
+    plain = mom.mom_run(est, theta0=centre, engine=eng)
+    fs = sf.fit
+    ctl = est.control
+    return {
+        "workload": "c5: n=300, 3 waves (wave 1 Bernoulli(0.03), waves 2-3 simulated at rate 7 "
+                    "and theta_true), 7 evaluation effects + 2 rates, unconditional MoM",
+        "metric": "MoM fit wall time", "unit": "s", "higher_is_better": False,
+        "plain_s": plain.wall_time, "surrogate_s": fs.wall_time,
+        "speedup": plain.wall_time / fs.wall_time,
+        "max_abs_tconv": {"plain": float(np.abs(plain.tconv).max()),
+                          "surrogate": float(np.abs(fs.tconv).max())},
+        "max_abs_theta_diff_over_se": float(np.max(np.abs(fs.theta - plain.theta) / plain.se)),
+        "period_simulations": {"plain": int(plain.n_sims * est.P),
+                               "surrogate": int(sf.n_period_sims)},
+        "takeovers": sf.takeovers,
+        "surrogate_max_error_sd": float(np.max(sf.judge[0]["error"])),
+        "phase_times_s": {"plain": plain.phase_times, "surrogate": fs.phase_times},
+        "training_pairs": int(sum(s["n_theta"] for s in sf.stages) * est.P),
+        "control": {"n1": ctl["n1"], "nsub": ctl["nsub"], "n2": list(ctl["n2"]),
+                    "batch2": ctl["batch2"], "nD": ctl["nD"], "n3": ctl["n3"]},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -210,6 +260,8 @@ def main():
     ap.add_argument("--cpu-chains", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mom", action="store_true",
+                    help="skip the MoM fit comparison (plain vs surrogate) on the n=300 panel")
     args = ap.parse_args()
     if args.chains == 0:
         args.chains = 4096 if args.workload == "c2" else 1024
@@ -334,6 +386,13 @@ def main():
     if not args.no_cpu_baseline and ws == 1:
         cpu = cpu_baseline(args, inp, M, seed, lam, theta, lamb, thetab)
 
+    mom_fit = None
+    if not args.no_mom and ws == 1:
+        try:
+            mom_fit = mom_fit_comparison()
+        except Exception as exc:   # the simulator line is reported regardless
+            mom_fit = {"error": f"{type(exc).__name__}: {exc}"}
+
     clk = clocks.summary(local)
     line = {
         "metric": "ministeps/s", "value": value, "unit": "ministeps/s", "n_gpus": ws,
@@ -348,6 +407,7 @@ def main():
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(sum(launches)), "clocks": clk,
         "wall_s_timed_region": t_wall,
+        "mom_fit": mom_fit,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
