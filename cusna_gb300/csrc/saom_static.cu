@@ -1,8 +1,7 @@
 // saom_static.cu -- cusna_saom_simulate_period_static: the period simulator for
 // callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc. Code running while a stream is being
-// captured into a CUDA graph may not allocate. Hosts whose device memory is
+// Some callers cannot call cudaMalloc. Hosts whose device memory is
 // handed out by another allocator may have none left for a second allocator:
 // an R session that pre-reserves the GPU for a framework is one case, an
 // embedding application with a fixed memory budget another. Latency-sensitive

@@ -251,9 +251,10 @@ CUSNA_API cusna_status cusna_behavior_stats_gpu(
 
 /* cusna_saom_simulate_period for callers that cannot allocate device memory.
  * No counterpart in the reference. Callers that cannot call cudaMalloc
- * include code running while a stream is captured into a CUDA graph, hosts
- * whose device memory belongs to another allocator, and latency-bound loops
- * that must not enter the allocator. The call allocates nothing. Every problem
+ * include hosts whose device memory belongs to another allocator and
+ * latency-bound loops that must not enter the allocator. The call allocates
+ * nothing. It is not safe inside a stream capture: it waits for its own work
+ * before returning and copies a few small host arrays. Every problem
  * and result pointer must be a device pointer (as with device_ptrs in
  * cusna_gpu_options), and the work runs on `stream` (a cudaStream_t; NULL for
  * the default stream). The call returns once the results are written.
@@ -261,8 +262,8 @@ CUSNA_API cusna_status cusna_behavior_stats_gpu(
  * the library holds that array until the process exits. A problem that needs
  * more scratch is refused with CUSNA_ERR_UNSUPPORTED and the size in
  * cusna_last_error(). The first call on each device looks up the array's
- * device address, so make that first call before any stream capture begins.
- * All calls share the array: calls whose GPU work overlaps, from two streams
+ * device address (once). All calls share the array: calls whose GPU work
+ * overlaps, from two streams
  * or two threads, race on it and must be serialised by the caller. */
 CUSNA_API cusna_status cusna_saom_simulate_period_static(
     const cusna_saom_problem *problem, cusna_saom_result *result, void *stream);
