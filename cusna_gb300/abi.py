@@ -120,6 +120,16 @@ def load_library(path: str | None = None):
     lib.cusna_saom_simulate_period_static.restype = i32
     lib.cusna_measure_fp64_tflops.argtypes = [P(C.c_double)]
     lib.cusna_measure_fp64_tflops.restype = i32
+    lib.cusna_saom_plan_create.argtypes = [P(SaomProblem), P(SaomResult), i32, i32, P(_p)]
+    lib.cusna_saom_plan_create.restype = i32
+    lib.cusna_saom_plan_launch.argtypes = [_p, _p, i32]
+    lib.cusna_saom_plan_launch.restype = i32
+    lib.cusna_saom_plan_set_epoch.argtypes = [_p, C.c_uint64]
+    lib.cusna_saom_plan_set_epoch.restype = i32
+    lib.cusna_saom_plan_shape.argtypes = [_p, P(i32), P(i32), P(i32)]
+    lib.cusna_saom_plan_shape.restype = i32
+    lib.cusna_saom_plan_destroy.argtypes = [_p]
+    lib.cusna_saom_plan_destroy.restype = None
     sz, f32 = C.c_size_t, C.c_float
     lib.cusna_mlp_param_count.argtypes = [i32, i32, i32]
     lib.cusna_mlp_param_count.restype = sz
@@ -151,6 +161,8 @@ EXPORTED_SYMBOLS = [
     "cusna_saom_simulate_period_ex", "cusna_saom_simulate_batch",
     "cusna_network_stats_gpu", "cusna_behavior_stats_gpu", "cusna_measure_fp64_tflops",
     "cusna_saom_simulate_period_static",
+    "cusna_saom_plan_create", "cusna_saom_plan_launch", "cusna_saom_plan_set_epoch",
+    "cusna_saom_plan_shape", "cusna_saom_plan_destroy",
     "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",
     "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_train_steps", "cusna_mlp_jacobian",
 ]

@@ -113,6 +113,7 @@ struct Facts {
   std::vector<int> tid, i0, i1, i2, rk;
   int flags = 0;
   std::vector<int> kind, cfn, offd, offt;  // effect plan, k each
+  std::vector<int> tsize;                  // theta-table length per effect (0: none)
   std::vector<double> pool;                // its tables
   int zlo = 0, zR = 1;
 };
@@ -157,8 +158,8 @@ double dyad_value(int t, double vi, double vj, double q1, double q2) {
 // forms d and theta*d, and the tables it reads. Term tables (theta * magnitude)
 // are built when every chain has the same theta, the usual case; otherwise the
 // kernel multiplies.
-cusna_status build_plan(const cusna_saom_problem *p, bool dev, Facts &F) {
-  const int n = p->n, k = p->k, M = p->M;
+cusna_status build_plan(const cusna_saom_problem *p, bool dev, Facts &F, bool one_row) {
+  const int n = p->n, k = p->k, M = one_row ? 1 : p->M;
   cusna_status s;
   std::vector<float> th;
   if ((s = fetch_vec(p->theta, (size_t)M * k, dev, th)) != CUSNA_OK) return s;
@@ -189,12 +190,14 @@ cusna_status build_plan(const cusna_saom_problem *p, bool dev, Facts &F) {
   F.zlo = (int)lo;
   F.zR = (int)std::max<long long>(1, std::min<long long>(zR, 65536));
   F.kind.assign(k, K_GEN); F.cfn.assign(k, 0); F.offd.assign(k, 0); F.offt.assign(k, 0);
+  F.tsize.assign(k, 0);
   F.pool.clear();
   auto add = [&](size_t cnt) { const size_t o = F.pool.size(); F.pool.resize(o + cnt, 0.0); return (int)o; };
   auto cnt_table = [&](int e, int cfn, size_t size) {
     F.kind[e] = K_CNT; F.cfn[e] = cfn;
     if (uniform) {
       F.offt[e] = add(size);
+      F.tsize[e] = (int)size;
       for (size_t c = 0; c < size; ++c) F.pool[F.offt[e] + c] = (double)th[e] * (double)c;
     }
   };
@@ -204,6 +207,7 @@ cusna_status build_plan(const cusna_saom_problem *p, bool dev, Facts &F) {
     for (size_t x = 0; x < size; ++x) F.pool[F.offd[e] + x] = value(x);
     if (uniform) {
       F.offt[e] = add(size);
+      F.tsize[e] = (int)size;
       for (size_t x = 0; x < size; ++x) F.pool[F.offt[e] + x] = (double)th[e] * F.pool[F.offd[e] + x];
     }
   };
@@ -265,8 +269,9 @@ cusna_status build_plan(const cusna_saom_problem *p, bool dev, Facts &F) {
   return CUSNA_OK;
 }
 
+// one_row: the parameter arrays hold one row shared by every chain (plans).
 cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, bool dev,
-                      Facts &F) {
+                      Facts &F, bool one_row = false) {
   if (!p || !r) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
   if (p->struct_version != CUSNA_ABI_VERSION) {
     set_err("struct_version %d != %d", p->struct_version, CUSNA_ABI_VERSION);
@@ -337,7 +342,7 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
     }
   }
   F.flags = fl;
-  if ((s = build_plan(p, dev, F)) != CUSNA_OK) return s;
+  if ((s = build_plan(p, dev, F, one_row)) != CUSNA_OK) return s;
   // gwdsp change statistics index the weight table at p+1 with p <= n-2 on a
   // network without self-ties; a self-tie in the start network could push p to
   // n and read past the table, so such problems are rejected
@@ -589,6 +594,7 @@ cusna_status prepare(Job &J, bool dev, DevProblem &D, uint32_t chain_offset) {
   D.keepT = at<uint32_t>(B.keepT); D.forceT = at<uint32_t>(B.forceT);
   D.keepcT = at<uint32_t>(B.keepcT); D.forcecT = at<uint32_t>(B.forcecT);
   D.lam = lam; D.theta = theta; D.lamb = lamb; D.thetab = thetab;
+  D.prow = 1;
   CU(cudaMemcpyAsync(at<int>(B.ekind), J.F.kind.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<int>(B.ecfn), J.F.cfn.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<int>(B.eoffd), J.F.offd.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
@@ -781,6 +787,8 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
   return CUSNA_OK;
 }
 
+void order_longest_first(std::vector<Job> &jobs);
+
 cusna_status simulate(const cusna_saom_problem *problems, cusna_saom_result *results, int count,
                       cusna_gpu_options *opts) {
   if (!problems || !results) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
@@ -801,6 +809,7 @@ cusna_status simulate(const cusna_saom_problem *problems, cusna_saom_result *res
     if ((s = validate(&problems[q], &results[q], dev, jobs[q].F)) != CUSNA_OK) return s;
   }
   if ((s = ensure_ctx()) != CUSNA_OK) return s;
+  order_longest_first(jobs);
   s = run_jobs(jobs, dev, opts);
   if (s == CUSNA_OK && opts) {
     long long tot = 0;
@@ -811,6 +820,204 @@ cusna_status simulate(const cusna_saom_problem *problems, cusna_saom_result *res
     opts->ministeps = tot;
   }
   return s;
+}
+
+// Relative cost of one chain of a problem, for ordering the persistent
+// kernel's work longest first: ministeps grow with n and each ministep visits
+// n alters with k effects.
+double chain_cost(const cusna_saom_problem *p) {
+  return (double)p->n * (double)p->n * (double)(p->k + 4);
+}
+
+void order_longest_first(std::vector<Job> &jobs) {
+  std::stable_sort(jobs.begin(), jobs.end(),
+                   [](const Job &a, const Job &b) { return chain_cost(a.p) > chain_cost(b.p); });
+}
+
+}  // namespace
+
+}  // namespace cusna
+
+// ---- replayable plans ----------------------------------------------------------
+// A plan holds everything a launch reads in device memory of its own, so a
+// launch only enqueues kernels: no allocation, no host copy, no wait. Launches
+// can therefore be captured into a CUDA graph and replayed.
+struct cusna_saom_plan {
+  int device = -1;
+  void *mem = nullptr;
+  cusna::LaunchShape sh{};
+  cusna::DevProblem *probs = nullptr;
+  long long *units = nullptr;
+  unsigned long long *counter = nullptr, *epoch = nullptr, *seeds = nullptr;
+  cusna::PlanTable *tabs = nullptr;
+  int count = 0, n_tabs = 0;
+  long long total = 0;
+  uint32_t *cols = nullptr, *rows = nullptr;
+  size_t cols_words = 0;
+  cudaGraphExec_t graph = nullptr;
+};
+
+namespace cusna {
+namespace {
+
+void plan_free(cusna_saom_plan *P) {
+  if (!P) return;
+  if (P->graph) cudaGraphExecDestroy(P->graph);
+  if (P->mem) cudaFree(P->mem);
+  delete P;
+}
+
+cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *results, int count,
+                         int shared_params, cusna_saom_plan **out) {
+  if (!problems || !results || !out) { set_err("problems, results and plan are required"); return CUSNA_ERR_NULL_ARG; }
+  *out = nullptr;
+  if (count < 1) { set_err("count %d < 1", count); return CUSNA_ERR_SHAPE; }
+  if (shared_params != 0 && shared_params != 1) { set_err("shared_params must be 0 or 1"); return CUSNA_ERR_SHAPE; }
+  cusna_status s;
+  if ((s = ensure_ctx()) != CUSNA_OK) return s;
+  const bool one = shared_params == 1;
+  std::vector<Job> jobs(count);
+  for (int q = 0; q < count; ++q) {
+    jobs[q].p = &problems[q];
+    jobs[q].r = &results[q];
+    if ((s = validate(&problems[q], &results[q], true, jobs[q].F, one)) != CUSNA_OK) return s;
+    // with a row per chain the kernel multiplies (rows may differ at a later launch)
+    if (!one) jobs[q].F.flags &= ~F_THETA_TAB;
+  }
+  order_longest_first(jobs);
+  int nmax = 0, Wmax = 0, kmax = 0, kbmax = 0, nrmax = 0;
+  bool tp = false, gw = false, tq = false;
+  long long total = 0;
+  for (auto &J : jobs) {
+    nmax = std::max(nmax, J.p->n); Wmax = std::max(Wmax, J.p->W); kmax = std::max(kmax, J.p->k);
+    kbmax = std::max(kbmax, J.p->kb); nrmax = std::max(nrmax, J.p->nrate);
+    tp |= (J.F.flags & F_NEED_TP) != 0;
+    gw |= (J.F.flags & (F_NEED_GW29 | F_NEED_TP)) != 0;
+    tq |= (J.F.flags & F_NEED_GW30) != 0;
+    total += J.p->M;
+  }
+  const LaunchShape sh = choose_shape(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, 0, 0);
+  if (sh.G == 0) { set_err("no launch shape fits n=%d", nmax); return CUSNA_ERR_UNSUPPORTED; }
+  std::vector<PlanTable> tabs;
+  for (int q = 0; q < count; ++q) {
+    const Facts &F = jobs[q].F;
+    if (!(F.flags & F_THETA_TAB)) continue;
+    for (int e = 0; e < jobs[q].p->k; ++e)
+      if (F.tsize[e] > 0) tabs.push_back(PlanTable{q, e, F.kind[e], F.offt[e], F.offd[e], F.tsize[e]});
+  }
+  Planner pl;
+  for (auto &J : jobs) plan_problem(pl, J, true);
+  const size_t o_probs = pl.take(sizeof(DevProblem) * count);
+  const size_t o_units = pl.take(sizeof(long long) * (count + 1));
+  const size_t o_counter = pl.take(8), o_epoch = pl.take(8), o_seeds = pl.take(8 * (size_t)count);
+  const size_t o_tabs = pl.take(sizeof(PlanTable) * std::max<size_t>(1, tabs.size()));
+  const size_t teams = (size_t)sh.ctas * sh.teams_per_cta;
+  const size_t cols_words = (size_t)Wmax * nmax;
+  const size_t o_cols = sh.cols_in_smem ? NONE : pl.take(teams * cols_words * 4);
+  const size_t o_rows = sh.rows_in_smem ? NONE : pl.take(teams * cols_words * 4);
+
+  cusna_saom_plan *P = new cusna_saom_plan();
+  P->device = g_ctx.device;
+  if (cudaMalloc(&P->mem, pl.off) != cudaSuccess) {
+    cudaGetLastError();
+    plan_free(P);
+    set_err("plan: cudaMalloc of %zu bytes failed", pl.off);
+    return CUSNA_ERR_CUDA;
+  }
+  // prepare() places each problem in the thread's arena: point the arena at the
+  // plan's memory for the duration
+  struct ArenaSwap {
+    void *arena; size_t cap;
+    ~ArenaSwap() { g_ctx.arena = arena; g_ctx.cap = cap; }
+  } restore{g_ctx.arena, g_ctx.cap};
+  g_ctx.arena = P->mem;
+  g_ctx.cap = pl.off;
+  std::vector<DevProblem> hp(count);
+  std::vector<long long> units(count + 1, 0);
+  std::vector<unsigned long long> seeds(count);
+  for (int q = 0; q < count; ++q) {
+    if ((s = prepare(jobs[q], true, hp[q], 0)) != CUSNA_OK) { plan_free(P); return s; }
+    hp[q].prow = one ? 0 : 1;
+    units[q + 1] = units[q] + jobs[q].p->M;
+    seeds[q] = (unsigned long long)jobs[q].p->seed;
+  }
+  cudaStream_t st = g_ctx.stream;
+  auto up = [&](size_t off, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(at<char>(off), src, bytes, cudaMemcpyHostToDevice, st);
+  };
+  cudaError_t e = up(o_probs, hp.data(), sizeof(DevProblem) * count);
+  if (e == cudaSuccess) e = up(o_units, units.data(), sizeof(long long) * units.size());
+  if (e == cudaSuccess) e = up(o_seeds, seeds.data(), 8 * seeds.size());
+  if (e == cudaSuccess && !tabs.empty()) e = up(o_tabs, tabs.data(), sizeof(PlanTable) * tabs.size());
+  if (e == cudaSuccess) e = cudaMemsetAsync(at<char>(o_counter), 0, 8, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(at<char>(o_epoch), 0, 8, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    set_err("plan: staging failed: %s", cudaGetErrorString(e));
+    plan_free(P);
+    return CUSNA_ERR_CUDA;
+  }
+  P->sh = sh;
+  P->probs = at<DevProblem>(o_probs);
+  P->units = at<long long>(o_units);
+  P->counter = at<unsigned long long>(o_counter);
+  P->epoch = at<unsigned long long>(o_epoch);
+  P->seeds = at<unsigned long long>(o_seeds);
+  P->tabs = at<PlanTable>(o_tabs);
+  P->count = count;
+  P->n_tabs = (int)tabs.size();
+  P->total = total;
+  P->cols = o_cols == NONE ? nullptr : at<uint32_t>(o_cols);
+  P->rows = o_rows == NONE ? nullptr : at<uint32_t>(o_rows);
+  P->cols_words = cols_words;
+  *out = P;
+  return CUSNA_OK;
+}
+
+// Kernel launches only (capture-safe): epoch and term tables, work counter,
+// the persistent period kernel.
+cusna_status plan_enqueue(cusna_saom_plan *P, cudaStream_t st) {
+  CU(launch_plan_prologue(P->probs, P->seeds, P->count, P->epoch, P->tabs, P->n_tabs, st));
+  CU(cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), st));
+  CU(launch_period(P->sh, P->probs, P->units, P->count, P->total, P->counter, P->cols, P->rows,
+                   P->cols_words, st));
+  return CUSNA_OK;
+}
+
+cusna_status plan_launch(cusna_saom_plan *P, cudaStream_t st, bool graph) {
+  if (!P) { set_err("plan is NULL"); return CUSNA_ERR_NULL_ARG; }
+  int dev = -1;
+  CU(cudaGetDevice(&dev));
+  if (dev != P->device) { set_err("plan belongs to device %d, current is %d", P->device, dev); return CUSNA_ERR_UNSUPPORTED; }
+  if (!graph) return plan_enqueue(P, st);
+  if (!P->graph) {
+    cudaStream_t cap = nullptr;
+    CU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+      cudaStreamDestroy(cap);
+      set_err("plan: begin capture failed: %s", cudaGetErrorString(e));
+      return CUSNA_ERR_CUDA;
+    }
+    cusna_status s = plan_enqueue(P, cap);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(cap, &g);   // ends the capture on every path
+    cudaStreamDestroy(cap);
+    if (s != CUSNA_OK || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (s == CUSNA_OK) set_err("plan: capture failed: %s", cudaGetErrorString(e));
+      return s != CUSNA_OK ? s : CUSNA_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&P->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      P->graph = nullptr;
+      set_err("plan: graph instantiation failed: %s", cudaGetErrorString(e));
+      return CUSNA_ERR_CUDA;
+    }
+  }
+  CU(cudaGraphLaunch(P->graph, st));
+  return CUSNA_OK;
 }
 
 }  // namespace
@@ -844,6 +1051,40 @@ CUSNA_API cusna_status cusna_saom_simulate_batch(const cusna_saom_problem *probl
                                                  cusna_gpu_options *opts) {
   g_err.clear();
   return simulate(problems, results, count, opts);
+}
+
+CUSNA_API cusna_status cusna_saom_plan_create(const cusna_saom_problem *problems,
+                                             cusna_saom_result *results, int32_t count,
+                                             int32_t shared_params, cusna_saom_plan **plan) {
+  g_err.clear();
+  return plan_create(problems, results, count, shared_params, plan);
+}
+
+CUSNA_API cusna_status cusna_saom_plan_launch(cusna_saom_plan *plan, void *stream,
+                                             int32_t use_graph) {
+  g_err.clear();
+  return plan_launch(plan, (cudaStream_t)stream, use_graph != 0);
+}
+
+CUSNA_API cusna_status cusna_saom_plan_set_epoch(cusna_saom_plan *plan, uint64_t epoch) {
+  g_err.clear();
+  if (!plan) { set_err("plan is NULL"); return CUSNA_ERR_NULL_ARG; }
+  CU(cudaMemcpy(plan->epoch, &epoch, sizeof(epoch), cudaMemcpyHostToDevice));
+  return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_saom_plan_shape(const cusna_saom_plan *plan, int32_t *warps_per_chain,
+                                            int32_t *chains_per_cta, int32_t *ctas) {
+  if (!plan) return CUSNA_ERR_NULL_ARG;
+  if (warps_per_chain) *warps_per_chain = plan->sh.G;
+  if (chains_per_cta) *chains_per_cta = plan->sh.teams_per_cta;
+  if (ctas) *ctas = plan->sh.ctas;
+  return CUSNA_OK;
+}
+
+CUSNA_API void cusna_saom_plan_destroy(cusna_saom_plan *plan) {
+  if (plan) cudaDeviceSynchronize();   // no launch of the plan may still be running
+  plan_free(plan);
 }
 
 CUSNA_API cusna_status cusna_pack_bits(const uint8_t *dense, int32_t n, uint32_t *out_rows,

@@ -16,7 +16,7 @@ __device__ __forceinline__ void chain_init(const Team &T, const DevProblem &P, c
     S.colsT[x] = P.simcT[x];
   }
   for (int e = T.tl; e < k; e += L) {
-    S.th[e] = (double)P.theta[(size_t)c * k + e];
+    S.th[e] = (double)P.theta[(size_t)c * P.prow * k + e];
     S.sc[e] = 0.0;
     S.tid[e] = P.type_ids[e];
     S.ety[e] = P.etypes[e];
@@ -33,7 +33,7 @@ __device__ __forceinline__ void chain_init(const Team &T, const DevProblem &P, c
   }
   for (int x = T.tl; x < 64; x += L) S.exptab[x] = kExp2Frac64[x];
   for (int e = T.tl; e < P.kb; e += L) {
-    S.thb[e] = P.thetab ? (double)P.thetab[(size_t)c * P.kb + e] : 0.0;
+    S.thb[e] = P.thetab ? (double)P.thetab[(size_t)c * P.prow * P.kb + e] : 0.0;
     S.bsc[e] = 0.0;
     S.bty[e] = P.bty[e];
   }
@@ -281,8 +281,8 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
   const uint32_t chain = P.chain_offset + (uint32_t)c;
   chain_init(T, P, S, c);
 
-  const double lam = (double)P.lam[c];
-  const double lamb = P.lamb ? (double)P.lamb[c] : 0.0;
+  const double lam = (double)P.lam[c * P.prow];
+  const double lamb = P.lamb ? (double)P.lamb[c * P.prow] : 0.0;
   // the reference's constant-rate expressions (src/libcusna_saom_cpu.cpp:195,197)
   const double den = __dmul_rn((double)P.nact, __dadd_rn(lam, lamb));
   const double pnet = __ddiv_rn(lam, __dadd_rn(lam, lamb));

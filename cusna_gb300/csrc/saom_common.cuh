@@ -75,8 +75,10 @@ struct DevProblem {
   const uint32_t *x0T, *x0cT, *simT, *simcT, *kdistT, *permT;
   const uint32_t *keepT, *forceT, *keepcT, *forcecT;       // statistic masks
 
-  // per-chain parameters
+  // per-chain parameters: chain c reads row c * prow (prow 1: one row per
+  // chain, as the ABI lays them out; 0: one row shared by every chain)
   const float *lam, *theta, *lamb, *thetab;
+  int prow;
 
   // effect plan (k each) and its table pool
   const int *ekind, *ecfn, *eoffd, *eofft;

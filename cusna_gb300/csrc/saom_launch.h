@@ -25,6 +25,17 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
                           uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
                           cudaStream_t st);
 int period_blocks_per_sm(int threads, size_t dyn_smem);
+
+// One theta-premultiplied term table of a plan's problem q, effect e (pool
+// offsets of the table and, for lookup tables, of its values).
+struct PlanTable {
+  int q, e, kind, offt, offd, size;
+};
+// Before each launch of a plan: advance the epoch (Philox keys) and rebuild the
+// term tables from the current parameters.
+cudaError_t launch_plan_prologue(DevProblem *probs, const unsigned long long *base_seed, int count,
+                                 unsigned long long *epoch, const PlanTable *tabs, int n_tabs,
+                                 cudaStream_t st);
 long long kernel_launches();  // kernels launched so far by the calling thread
 void set_last_error(const char *msg);  // text of cusna_last_error() for this thread
 cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,

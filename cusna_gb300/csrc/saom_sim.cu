@@ -361,6 +361,48 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
   return counted(cudaGetLastError());
 }
 
+// ---- replayable plans --------------------------------------------------------
+// Each launch of a plan simulates with Philox key = the problem's seed plus the
+// plan's epoch (64-bit, so epoch 0 is the plain call), then advances the epoch.
+__global__ void plan_epoch_kernel(DevProblem *probs, const unsigned long long *base_seed,
+                                  int count, unsigned long long *epoch) {
+  __shared__ unsigned long long e;
+  if (threadIdx.x == 0) e = *epoch;
+  __syncthreads();
+  for (int q = threadIdx.x; q < count; q += blockDim.x) {
+    const unsigned long long s = base_seed[q] + e;
+    probs[q].k0 = (uint32_t)(s & 0xFFFFFFFFull);
+    probs[q].k1 = (uint32_t)(s >> 32);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *epoch = e + 1;
+}
+
+// Rebuilds the theta-premultiplied term tables of a plan's problems from the
+// current parameter row (one block per table): entry x of effect e's table is
+// theta_e * x for a count table and theta_e * value_x for a lookup table,
+// rounded as the host builds them.
+__global__ void plan_retheta_kernel(const DevProblem *probs, const PlanTable *tabs) {
+  const PlanTable T = tabs[blockIdx.x];
+  const DevProblem &P = probs[T.q];
+  const double th = (double)P.theta[T.e];
+  double *tab = const_cast<double *>(P.tab);
+  for (int x = threadIdx.x; x < T.size; x += blockDim.x) {
+    const double v = T.kind == K_CNT ? (double)x : tab[T.offd + x];
+    tab[T.offt + x] = __dmul_rn(th, v);
+  }
+}
+
+cudaError_t launch_plan_prologue(DevProblem *probs, const unsigned long long *base_seed, int count,
+                                 unsigned long long *epoch, const PlanTable *tabs, int n_tabs,
+                                 cudaStream_t st) {
+  plan_epoch_kernel<<<1, 256, 0, st>>>(probs, base_seed, count, epoch);
+  cudaError_t e = counted(cudaGetLastError());
+  if (e != cudaSuccess || n_tabs == 0) return e;
+  plan_retheta_kernel<<<n_tabs, 128, 0, st>>>(probs, tabs);
+  return counted(cudaGetLastError());
+}
+
 cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
                             cudaStream_t st) {
   const size_t slice = al16((size_t)2 * D.W * D.n * 4 + (size_t)2 * D.n * 4) + 32 * 8 + 64;

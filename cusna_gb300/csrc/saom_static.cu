@@ -323,6 +323,7 @@ extern "C" CUSNA_API cusna_status cusna_saom_simulate_period_static(
   D.kdistT = U32(oK); D.permT = U32(oP); D.keepT = U32(oKp); D.forceT = U32(oF);
   D.keepcT = U32(oKc); D.forcecT = U32(oFc);
   D.lam = p->lam; D.theta = p->theta; D.lamb = p->lamb; D.thetab = kb ? p->thetab : nullptr;
+  D.prow = 1;
   D.ekind = I32(oKind); D.ecfn = I32(oCfn); D.eoffd = I32(oOffd); D.eofft = I32(oOffd);
   D.tab = F64(oTab);
   D.stats = r->stats; D.ntim = r->ntim; D.scores = r->scores; D.dist = r->dist;

@@ -53,6 +53,135 @@ def simulate_batch(ms: list[Marshalled], opts: GpuOptions | None = None) -> list
     return [result_dict(m) for m in ms]
 
 
+PARAM_FIELDS = ("theta", "lam", "lamb", "thetab")
+
+
+class SimPlan:
+    """Replayable simulation of many marshalled problems (cusna_saom_plan_*).
+
+    Every input moves to device memory once. The parameters (theta, lam, lamb,
+    thetab) live in contiguous device buffers holding one row per problem
+    (shared by its M chains; `per_chain=True` keeps a row per chain), which
+    `set_params` rewrites between launches. Outputs go to contiguous device
+    buffers, one per output name, which `outputs` copies back in one transfer
+    each. `launch` re-simulates every problem in one persistent kernel, the
+    first time with Philox key = the problem's seed and then seed + 1, seed +
+    2, ... (the epoch advances on the device); with `use_graph` the launch is
+    replayed from a CUDA graph. Device buffers are torch tensors (allocation
+    only); the simulation is the library's."""
+
+    def __init__(self, ms: list[Marshalled], per_chain: bool = False, use_graph: bool = True):
+        import torch
+        self.torch = torch
+        self.lib = load_library()
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.use_graph = bool(use_graph)
+        self.count = len(ms)
+        self.M = [int(m.problem.M) for m in ms]
+        probs = (SaomProblem * self.count)()
+        ress = (SaomResult * self.count)()
+        self._keep = []
+        self.params, self.outs = {}, {}
+        for q, m in enumerate(ms):
+            probs[q] = SaomProblem.from_buffer_copy(m.problem)
+            ress[q] = SaomResult.from_buffer_copy(m.result)
+        keys = {k for k in ms[0].keep if k.startswith("out_") or k in PARAM_FIELDS}
+        for q, m in enumerate(ms):
+            if {k for k in m.keep if k.startswith("out_") or k in PARAM_FIELDS} != keys:
+                raise ValueError("a plan's problems must carry the same parameters and outputs")
+            # every host pointer of the struct copy is replaced by a device one
+            for name, a in m.keep.items():
+                if not (name.startswith("out_") or name in PARAM_FIELDS):
+                    setattr(probs[q], name, self._upload(a).data_ptr())
+        # parameter buffers: rows of each problem back to back
+        for name in PARAM_FIELDS:
+            if name not in ms[0].keep:
+                continue
+            rows = []
+            for m in ms:
+                a = np.asarray(m.keep[name], dtype=np.float32).reshape(int(m.problem.M), -1)
+                rows.append(a if per_chain else a[:1])
+            width = rows[0].shape[1]
+            host = np.concatenate(rows, axis=0)
+            t = self._upload(host)
+            off = np.cumsum([0] + [r.shape[0] for r in rows])
+            for q in range(self.count):
+                setattr(probs[q], name, t.data_ptr() + 4 * width * int(off[q]))
+            self.params[name] = (t, width, off)
+        for name in [k for k in ms[0].keep if k.startswith("out_")]:
+            arrs = [np.asarray(m.keep[name]) for m in ms]
+            sizes = [a.size for a in arrs]
+            off = np.cumsum([0] + sizes)
+            t = torch.empty(int(off[-1]) * arrs[0].itemsize, dtype=torch.uint8, device=self.dev)
+            self._keep.append(t)
+            for q in range(self.count):
+                setattr(ress[q], name[4:], t.data_ptr() + arrs[0].itemsize * int(off[q]))
+            self.outs[name[4:]] = (t, arrs[0].dtype, [a.shape for a in arrs], off)
+        self._probs, self._ress = probs, ress
+        plan = C.c_void_p()
+        check(self.lib.cusna_saom_plan_create(probs, ress, self.count, 0 if per_chain else 1,
+                                              C.byref(plan)), "cusna_saom_plan_create", self.lib)
+        self.plan = plan
+
+    def _upload(self, a):
+        a = np.ascontiguousarray(a)
+        t = self.torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).to(self.dev)
+        self._keep.append(t)
+        return t
+
+    def _stream(self):
+        return self.torch.cuda.current_stream(self.dev).cuda_stream
+
+    def set_params(self, **rows):
+        """Write parameters for the next launch: name=(count, width) rows, or
+        one row broadcast to every problem (rows of a per-chain plan:
+        (sum of M, width))."""
+        for name, val in rows.items():
+            t, width, off = self.params[name]
+            n_rows = int(off[-1])
+            a = np.asarray(val, dtype=np.float32).reshape(-1, width)
+            if a.shape[0] == 1 and n_rows > 1:
+                a = np.repeat(a, n_rows, axis=0)
+            if a.shape[0] != n_rows:
+                raise ValueError(f"{name}: {a.shape[0]} rows for {n_rows}")
+            t.copy_(self.torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)))
+
+    def set_epoch(self, epoch: int):
+        check(self.lib.cusna_saom_plan_set_epoch(self.plan, int(epoch)),
+              "cusna_saom_plan_set_epoch", self.lib)
+
+    def launch(self):
+        check(self.lib.cusna_saom_plan_launch(self.plan, self._stream(), 1 if self.use_graph else 0),
+              "cusna_saom_plan_launch", self.lib)
+
+    def shape(self):
+        g, t, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self.lib.cusna_saom_plan_shape(self.plan, C.byref(g), C.byref(t), C.byref(c))
+        return g.value, t.value, c.value
+
+    def outputs(self, names=None) -> list[dict]:
+        """Per problem, the named outputs of the last launch (host arrays)."""
+        names = names or list(self.outs)
+        res = [dict() for _ in range(self.count)]
+        for name in names:
+            t, dt, shapes, off = self.outs[name]
+            host = t.cpu().numpy().view(dt)
+            for q in range(self.count):
+                res[q][name] = host[int(off[q]):int(off[q + 1])].reshape(shapes[q])
+        return res
+
+    def close(self):
+        if getattr(self, "plan", None) is not None and self.plan.value:
+            self.lib.cusna_saom_plan_destroy(self.plan)
+            self.plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def network_stats(a, n, k, type_ids, p1, p2, vmat, vmiss, dyn_flags, vb, od0, id0, wtab,
                   symflag) -> np.ndarray:
     """Statistics of one or more networks on the GPU (a: (n,n) or (M,n,n))."""

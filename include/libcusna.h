@@ -268,6 +268,42 @@ CUSNA_API cusna_status cusna_behavior_stats_gpu(
 CUSNA_API cusna_status cusna_saom_simulate_period_static(
     const cusna_saom_problem *problem, cusna_saom_result *result, void *stream);
 
+/* ---- replayable plans (no counterpart in the reference) ---------------------
+ * A plan prepares `count` problems once and then simulates all of them again at
+ * every launch, in one persistent kernel, with the work ordered longest chain
+ * first. It is built for loops that simulate the same problems many times with
+ * new parameters: Robbins-Monro rounds over many periods or groups.
+ *
+ * cusna_saom_plan_create: every problem and result pointer is a DEVICE pointer
+ * (as with device_ptrs in cusna_gpu_options) and must stay valid for the plan's
+ * lifetime. The start networks and descriptors are copied into the plan;
+ * type_ids, od0, id0, vmiss, bty and rkind are read in place. theta, lam, lamb
+ * and thetab are read again at every launch, so the caller may rewrite them
+ * between launches. With shared_params = 1 each of them holds ONE row used by
+ * all M chains (theta k floats, lam 1 float, ...); with 0 they hold a row per
+ * chain, as in cusna_saom_problem. Each launch overwrites the results.
+ * Launch e (counting from 0, or from cusna_saom_plan_set_epoch) uses Philox key
+ * seed + e for each problem, so launch 0 reproduces cusna_saom_simulate_batch.
+ *
+ * cusna_saom_plan_launch only enqueues kernels on `stream`: no allocation, no
+ * host copy, no wait, so it may run inside a stream capture. With use_graph != 0
+ * the launch is captured once into a CUDA graph (on a private stream; the first
+ * such call must not itself be inside a capture) and replayed afterwards.
+ * Launches of one plan must not overlap. */
+typedef struct cusna_saom_plan cusna_saom_plan;
+CUSNA_API cusna_status cusna_saom_plan_create(const cusna_saom_problem *problems,
+                                             cusna_saom_result *results, int32_t count,
+                                             int32_t shared_params, cusna_saom_plan **plan);
+CUSNA_API cusna_status cusna_saom_plan_launch(cusna_saom_plan *plan, void *stream,
+                                             int32_t use_graph);
+CUSNA_API cusna_status cusna_saom_plan_set_epoch(cusna_saom_plan *plan, uint64_t epoch);
+/* The launch shape the autotuner chose for the plan. */
+CUSNA_API cusna_status cusna_saom_plan_shape(const cusna_saom_plan *plan,
+                                            int32_t *warps_per_chain, int32_t *chains_per_cta,
+                                            int32_t *ctas);
+/* Waits for the device, then frees the plan and its device memory. */
+CUSNA_API void cusna_saom_plan_destroy(cusna_saom_plan *plan);
+
 /* Measured float64 FMA throughput of the current device in TFLOP/s (an FMA
  * counts 2 flops): the peak against which the simulator's float64 work is
  * reported. Runs a short synthetic kernel. */
