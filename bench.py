@@ -23,6 +23,10 @@ the ranks' ministeps over the slowest rank's time.
          the n=300 panel, plain GPU Robbins-Monro against the surrogate-assisted
          fit, with both fits' convergence t-ratios, their estimates' agreement
          in SE units and the number of period simulations each needed
+  batching (1 GPU, unless --no-batching) one Robbins-Monro round of the
+         512-group workload (1024 problems of n = 20..400) through one-shot
+         batch calls, a replayable plan, and the plan replayed from a CUDA
+         graph; --c3-fit adds the joint conditional MoM fit
 
 --impl reference times the reference's CPU engine on the host cores on a
 bounded sample of the same workload (oracle/_ref where it was compiled from
@@ -249,6 +253,56 @@ def mom_fit_comparison(n3_check=True):
     }
 
 
+def batching_comparison(full_fit=False):
+    """One Robbins-Monro round of the uneven multi-group workload (512 groups,
+    n ~ U{20..400}, 2 periods each: 1024 problems, one chain each): through
+    one-shot batch calls that marshal and upload every problem each round,
+    through a replayable plan (prepared once; a round writes theta and launches),
+    and through the same plan replayed from a CUDA graph. Host wall clock per
+    round, median of 5 after one warm-up round. With full_fit, the joint
+    conditional MoM fit through the graph-replayed plans as well."""
+    from cusna_gb300 import data as D
+    from cusna_gb300 import mom
+    eng = mom.GpuEngine()
+    groups = WL.c3_groups(eng)
+    datas = [D.build_saom_data(w) for w, _ in groups]
+    effs = [WL.c3_effects(c) for _, c in groups]
+    ctl = dict(mom.DEFAULT_CONTROL)
+    ctl.update(n1=50, nD=50, batch2=1, n3=500)
+    est = mom.mom_estimator_groups(datas, effs, ctl, engine=eng)
+    theta = np.array([-2.4, 1.9, 0.35, 0.45])
+    rng = np.random.default_rng(1)
+    rounds = {}
+    shape = None
+    for name, engine in (("batch_calls", mom.GpuEngine()),
+                         ("plan", mom.PlanEngine(use_graph=False)),
+                         ("plan_graph", mom.PlanEngine(use_graph=True))):
+        ts = []
+        for _ in range(6):
+            t0 = time.perf_counter()
+            mom.mom_simulate(est, theta, 1, rng, engine)
+            ts.append(time.perf_counter() - t0)
+        rounds[name] = 1e3 * float(np.median(ts[1:]))
+        if name == "plan_graph":
+            shape = next(iter(engine._plans.values())).shape()
+            engine.close()
+    out = {"workload": "c3: 512 groups, n ~ U{20..400}, wave-1 density ~ U[0.02,0.10], binary "
+                       "covariate; density, recip, transTrip, sameX; conditional; 1024 "
+                       "(group, period) problems per round",
+           "round_ms": rounds, "chains_per_round": est.P,
+           "plan_shape": {"warps_per_chain": shape[0], "chains_per_cta": shape[1],
+                          "ctas": shape[2]}}
+    if full_fit:
+        eng = mom.PlanEngine(use_graph=True)
+        fit = mom.mom_run(est, engine=eng)
+        out["fit"] = {"wall_s": fit.wall_time, "phase_times_s": fit.phase_times,
+                      "theta": fit.theta.tolist(), "se": fit.se.tolist(),
+                      "tconv": fit.tconv.tolist(),
+                      "control": {"n1": 50, "nD": 50, "batch2": 1, "n3": 500}}
+        eng.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -262,6 +316,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mom", action="store_true",
                     help="skip the MoM fit comparison (plain vs surrogate) on the n=300 panel")
+    ap.add_argument("--no-batching", action="store_true",
+                    help="skip the multi-group round timing (batch calls vs replayed plans)")
+    ap.add_argument("--c3-fit", action="store_true",
+                    help="also run the joint conditional MoM fit of the 512-group workload")
     args = ap.parse_args()
     if args.chains == 0:
         args.chains = 4096 if args.workload == "c2" else 1024
@@ -386,6 +444,13 @@ def main():
     if not args.no_cpu_baseline and ws == 1:
         cpu = cpu_baseline(args, inp, M, seed, lam, theta, lamb, thetab)
 
+    batching = None
+    if not args.no_batching and ws == 1:
+        try:
+            batching = batching_comparison(args.c3_fit)
+        except Exception as exc:   # the simulator line is reported regardless
+            batching = {"error": f"{type(exc).__name__}: {exc}"}
+
     mom_fit = None
     if not args.no_mom and ws == 1:
         try:
@@ -408,6 +473,7 @@ def main():
         "gpu_launches": int(sum(launches)), "clocks": clk,
         "wall_s_timed_region": t_wall,
         "mom_fit": mom_fit,
+        "batching": batching,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

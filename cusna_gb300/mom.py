@@ -44,6 +44,47 @@ class GpuEngine:
         return sim.behavior_stats(*args)
 
 
+class PlanEngine(GpuEngine):
+    """GpuEngine whose simulation rounds run as replayable plans
+    (cusna_gb300.sim.SimPlan), one per chain count M: every (period or group)
+    problem is marshalled and moved to the device once; a round writes the new
+    parameters into the plan's device buffers and replays its CUDA graph, and
+    only the moment outputs come back. Round r of a plan simulates with Philox
+    keys seed + r, seeds drawn once per plan from the estimator's stream."""
+
+    OUTPUTS = ("stats", "scores", "ntim", "dist_stat", "bdist", "bscores", "z_end")
+
+    def __init__(self, use_graph: bool = True):
+        self.use_graph = use_graph
+        self._plans = {}
+
+    def simulate_round(self, est, theta, M: int, rng) -> list:
+        from . import sim
+        lam, th, lamb, thb, _ = split_theta(est, theta)
+        key = (id(est), int(M))
+        plan = self._plans.get(key)
+        if plan is None:
+            ms = [marshal_period(d["inp"], M, int(rng.integers(1, np.iinfo(np.int32).max)), lam[q], th,
+                                 lamb=lamb[q], thetab=thb if est.kb else None)
+                  for q, d in enumerate(est.per)]
+            plan = sim.SimPlan(ms, use_graph=self.use_graph)
+            self._plans[key] = plan
+        else:
+            rows = dict(theta=np.asarray(th, dtype=np.float32)[None, :],
+                        lam=np.asarray(lam, dtype=np.float32)[:, None])
+            if est.kb:
+                rows.update(lamb=np.asarray(lamb, dtype=np.float32)[:, None],
+                            thetab=np.asarray(thb, dtype=np.float32)[None, :])
+            plan.set_params(**rows)
+        plan.launch()
+        return plan.outputs([o for o in self.OUTPUTS if o in plan.outs])
+
+    def close(self):
+        for p in self._plans.values():
+            p.close()
+        self._plans.clear()
+
+
 def pinv(m, tol=np.sqrt(np.finfo(float).eps)):
     """Moore-Penrose pseudo-inverse by SVD (R/mom.R:15-19)."""
     u, s, vt = np.linalg.svd(m)
@@ -135,6 +176,27 @@ def mom_estimator(data: D.SaomData, effects, beh_effects=None, rate_effects=None
                      mt.target_vector, names, rate_consts, dists, bty, per, coevol, mt)
 
 
+def mom_estimator_groups(datas, effects_list, control=None, engine=None) -> Estimator:
+    """Joint conditional Method of Moments over independent groups that share
+    the model's parameters. The reference has no multi-group estimator; groups
+    are treated exactly as extra periods of one estimator (R/mom.R:143-182 sum
+    statistics and derivatives over periods): the targets are summed over every
+    group's periods, each (group, period) is one simulated unit with its own
+    conditional target distance, and one round simulates all units."""
+    ests = [mom_estimator(d, effs, None, None, True, control, engine)
+            for d, effs in zip(datas, effects_list)]
+    e0 = ests[0]
+    for e in ests[1:]:
+        if e.k != e0.k or e.param_names != e0.param_names:
+            raise ValueError("every group needs the same effects")
+    per = [u for e in ests for u in e.per]
+    P = len(per)
+    return Estimator(e0.data, e0.effects, None, True, e0.control, max(e.n for e in ests), P,
+                     e0.k, 0, e0.p, e0.symflag, np.sum([e.targets for e in ests], axis=0),
+                     list(e0.param_names), np.zeros(P),
+                     np.concatenate([e.dists for e in ests]), e0.bty, per, False, None)
+
+
 def split_theta(est: Estimator, theta):
     """(lam per period, theta_eval, lamb per period, theta_beh, offset), R/mom.R:131-138."""
     P, k, p = est.P, est.k, est.p
@@ -162,21 +224,24 @@ def mom_simulate(est: Estimator, theta, M: int, rng, engine, keep_nets=False,
     per-chain theta; used to generate surrogate training data)."""
     P, p, k, kb = est.P, est.p, est.k, est.kb
     lam, th, lamb, thb, off = split_theta(est, theta)
-    ms = []
-    for q in range(P):
-        seed = int(rng.integers(1, np.iinfo(np.int32).max))
-        d = est.per[q]
-        if theta_rows is not None:
-            tr = np.asarray(theta_rows, dtype=np.float64).reshape(M, p)
-            lam_arg = np.ones(M) if est.conditional else tr[:, q]
-            th_arg = tr[:, off:off + k]
-            lamb_arg = tr[:, P + q] if est.coevol else 0.0
-            thb_arg = tr[:, off + k:p] if kb else None
-        else:
-            lam_arg, th_arg, lamb_arg, thb_arg = lam[q], th, lamb[q], (thb if kb else None)
-        ms.append(marshal_period(d["inp"], M, seed, lam_arg, th_arg, lamb=lamb_arg,
-                                 thetab=thb_arg, want_ends=keep_nets))
-    outs = engine.simulate_batch(ms)
+    if theta_rows is None and not keep_nets and hasattr(engine, "simulate_round"):
+        outs = engine.simulate_round(est, theta, M, rng)
+    else:
+        ms = []
+        for q in range(P):
+            seed = int(rng.integers(1, np.iinfo(np.int32).max))
+            d = est.per[q]
+            if theta_rows is not None:
+                tr = np.asarray(theta_rows, dtype=np.float64).reshape(M, p)
+                lam_arg = np.ones(M) if est.conditional else tr[:, q]
+                th_arg = tr[:, off:off + k]
+                lamb_arg = tr[:, P + q] if est.coevol else 0.0
+                thb_arg = tr[:, off + k:p] if kb else None
+            else:
+                lam_arg, th_arg, lamb_arg, thb_arg = lam[q], th, lamb[q], (thb if kb else None)
+            ms.append(marshal_period(d["inp"], M, seed, lam_arg, th_arg, lamb=lamb_arg,
+                                     thetab=thb_arg, want_ends=keep_nets))
+        outs = engine.simulate_batch(ms)
     stats_acc = np.zeros((M, p))
     pieces, nets, z_ends = [], ([] if keep_nets else None), ([] if keep_nets and est.coevol else None)
     ntim = np.zeros((M, P))

@@ -260,3 +260,35 @@ def c5_theta_true() -> np.ndarray:
     """The data-generating parameter vector in the unconditional estimator's
     layout (rate per period, then the evaluation effects)."""
     return np.concatenate([[C5_LAMBDA, C5_LAMBDA], C5_THETA])
+
+
+# ---- C3: uneven multi-group panel --------------------------------------------
+C3_THETA = np.array([-2.5, 2.0, 0.4, 0.5])
+C3_EFFECTS = ["density", "recip", "transTrip", "sameX"]
+
+
+def c3_effects(cov):
+    """density, recip, transTrip and sameX of the group's binary covariate."""
+    return [E.make_effect_spec(nm, cov if nm == "sameX" else None) for nm in C3_EFFECTS]
+
+
+def c3_groups(engine, n_groups: int = 512, seed: int = 4, lam: float = 6.0):
+    """Groups of n ~ Uniform{20..400} actors with wave-1 density ~ Uniform[0.02,
+    0.10] and a binary covariate ~ Bernoulli(0.5) (numpy PCG64 streams from
+    `seed`); waves 2 and 3 simulated for all groups in one batched call per wave
+    with rate `lam` and C3_THETA (Philox seeds 31 + group, 41 + group).
+    Returns a list of (waves, covariate) per group."""
+    from .glue import marshal_period
+    r = np.random.Generator(np.random.PCG64(seed))
+    ns = r.integers(20, 401, size=n_groups)
+    dens = r.uniform(0.02, 0.10, size=n_groups)
+    covs = [(r.random(int(n)) < 0.5).astype(np.float64) for n in ns]
+    waves = [[bernoulli_net(int(n), float(p), seed=seed * 100003 + g).astype(np.int64)]
+             for g, (n, p) in enumerate(zip(ns, dens))]
+    for w, base in ((1, 31), (2, 41)):
+        ms = [marshal_period(period_inputs(waves[g][-1], c3_effects(covs[g])), 1, base + g, lam,
+                             C3_THETA, want_ends=True) for g in range(n_groups)]
+        outs = engine.simulate_batch(ms)
+        for g in range(n_groups):
+            waves[g].append(outs[g]["a_ends"][0].astype(np.int64))
+    return [(waves[g], covs[g]) for g in range(n_groups)]

@@ -85,3 +85,48 @@ def test_gpu_mom_agrees_with_oracle_mom(gpu_lib, port):
     g, c = fits["gpu"], fits["cpu"]
     np.testing.assert_array_equal(g.targets, c.targets)
     assert (np.abs(g.theta - c.theta) < np.maximum(g.se, c.se)).all(), (g.theta, c.theta)
+
+
+@pytest.mark.gpu
+def test_gpu_mom_through_replayed_plans(gpu_lib):
+    """The estimator over PlanEngine (each round a CUDA-graph replay of a plan
+    prepared once) reaches the estimates of the estimator over one-shot batch
+    calls within their standard errors; on 24 uneven groups too."""
+    waves = WL.c1_panel(mom.GpuEngine())
+    d = D.build_saom_data(waves)
+    effs = [ES(x) for x in ("density", "recip", "transTrip")]
+    fits = {}
+    for label, eng in (("batch", mom.GpuEngine()), ("plan", mom.PlanEngine())):
+        est = mom.mom_estimator(d, effs, None, None, True, SCHEDULE, engine=eng)
+        fits[label] = mom.mom_run(est, engine=eng)
+    a, b = fits["batch"], fits["plan"]
+    assert (np.abs(a.theta - b.theta) < np.maximum(a.se, b.se)).all(), (a.theta, b.theta)
+    groups = WL.c3_groups(mom.GpuEngine(), n_groups=24, seed=5)
+    datas = [D.build_saom_data(w) for w, _ in groups]
+    geffs = [WL.c3_effects(c) for _, c in groups]
+    ctl = dict(SCHEDULE, batch2=1)
+    eng = mom.PlanEngine()
+    est = mom.mom_estimator_groups(datas, geffs, ctl, engine=eng)
+    fit = mom.mom_run(est, engine=eng)
+    assert (np.abs(fit.theta - WL.C3_THETA) < 6 * fit.se + 0.05).all(), (fit.theta, fit.se)
+    eng.close()
+
+
+def test_joint_estimator_over_groups_sums_periods(port):
+    """Groups as extra periods (R/mom.R:143-182): targets are the sum of the
+    groups' targets, every (group, period) is one unit with its own target
+    distance, and a simulation round covers all units."""
+    groups = WL.c3_groups(port, n_groups=3, seed=11)
+    datas = [D.build_saom_data(w) for w, _ in groups]
+    effs = [WL.c3_effects(c) for _, c in groups]
+    ctl = dict(mom.DEFAULT_CONTROL)
+    est = mom.mom_estimator_groups(datas, effs, ctl, engine=port)
+    singles = [mom.mom_estimator(d, e, None, None, True, ctl, engine=port) for d, e in zip(datas, effs)]
+    assert est.P == 6 and est.p == 4 and est.conditional
+    np.testing.assert_allclose(est.targets, np.sum([s.targets for s in singles], axis=0))
+    np.testing.assert_array_equal(est.dists, np.concatenate([s.dists for s in singles]))
+    rng = np.random.Generator(np.random.PCG64(2))
+    s = mom.mom_simulate(est, WL.C3_THETA, 3, rng, port)
+    assert s.stats.shape == (3, 4) and len(s.pieces) == 6
+    # conditional: every unit stopped at its own observed distance
+    assert (s.ntim > 0).all()
