@@ -374,7 +374,7 @@ struct ProbBufs {
   size_t x0T, x0cT, simT, simcT, kdistT, permT, keepT, forceT, keepcT, forcecT;
   size_t vmat, wtab, p1, p2, vb, ralpha, ru;
   size_t etypes, dyn, i0, i1, i2, act, z0, bkdist, inact, vmiss;
-  size_t ekind, ecfn, eoffd, eofft, pool;
+  size_t ekind, ecfn, eoffd, eofft, pool, pool32;
   // raw copies (host mode)
   size_t r_x0, r_sim, r_kd, r_pm, r_keep, r_force, r_theta, r_lam, r_lamb, r_thetab, r_tid,
       r_ety, r_dyn, r_i0, r_i1, r_i2, r_vmat64, r_vmat32, r_wtab64, r_wtab32, r_p164, r_p132,
@@ -416,6 +416,7 @@ void plan_problem(Planner &pl, Job &J, bool dev) {
   B.vmiss = NONE;
   B.ekind = pl.take(k * 4); B.ecfn = pl.take(k * 4); B.eoffd = pl.take(k * 4);
   B.eofft = pl.take(k * 4); B.pool = pl.take(J.F.pool.size() * 8);
+  B.pool32 = pl.take(J.F.pool.size() * 4);
   if (!dev) {
     B.r_x0 = pl.take(n * W * 4);
     B.r_sim = maybe(pl, p->sim_out, n * W * 4);
@@ -600,8 +601,15 @@ cusna_status prepare(Job &J, bool dev, DevProblem &D, uint32_t chain_offset) {
   CU(cudaMemcpyAsync(at<int>(B.eoffd), J.F.offd.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<int>(B.eofft), J.F.offt.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<double>(B.pool), J.F.pool.data(), J.F.pool.size() * 8, cudaMemcpyHostToDevice, st));
+  {
+    // float32 lookup values for the float32 pass (a pageable copy is staged
+    // before cudaMemcpyAsync returns, so the local vector may go)
+    std::vector<float> p32(J.F.pool.size());
+    for (size_t x = 0; x < p32.size(); ++x) p32[x] = (float)J.F.pool[x];
+    CU(cudaMemcpyAsync(at<float>(B.pool32), p32.data(), p32.size() * 4, cudaMemcpyHostToDevice, st));
+  }
   D.ekind = at<int>(B.ekind); D.ecfn = at<int>(B.ecfn); D.eoffd = at<int>(B.eoffd);
-  D.eofft = at<int>(B.eofft); D.tab = at<double>(B.pool);
+  D.eofft = at<int>(B.eofft); D.tab = at<double>(B.pool); D.tab32 = at<float>(B.pool32);
   auto out = [&](void *user, size_t off) -> void * {
     if (!user) return nullptr;
     return dev ? user : (off == NONE ? nullptr : at<char>(off));

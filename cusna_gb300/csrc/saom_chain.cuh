@@ -16,7 +16,8 @@ __device__ __forceinline__ void chain_init(const Team &T, const DevProblem &P, c
     S.colsT[x] = P.simcT[x];
   }
   for (int e = T.tl; e < k; e += L) {
-    S.th[e] = (double)P.theta[(size_t)c * P.prow * k + e];
+    S.th32[e] = P.theta[(size_t)c * P.prow * k + e];
+    S.th[e] = (double)S.th32[e];
     S.sc[e] = 0.0;
     S.tid[e] = P.type_ids[e];
     S.ety[e] = P.etypes[e];
@@ -31,7 +32,6 @@ __device__ __forceinline__ void chain_init(const Team &T, const DevProblem &P, c
     S.eoffd[e] = P.eoffd[e];
     S.eofft[e] = P.eofft[e];
   }
-  for (int x = T.tl; x < 64; x += L) S.exptab[x] = kExp2Frac64[x];
   for (int e = T.tl; e < P.kb; e += L) {
     S.thb[e] = P.thetab ? (double)P.thetab[(size_t)c * P.prow * P.kb + e] : 0.0;
     S.bsc[e] = 0.0;
@@ -209,51 +209,59 @@ __device__ int rate_draw(const Team &T, const DevProblem &P, const Slice &S, con
   return focal;
 }
 
-// Top-2 of the float32 Gumbel estimates: best value b1 at alter j1 (ties to
-// the smaller j) and the largest value b2 of every other alter.
-struct Top2 {
-  float b1, b2;
+// Best float32 Gumbel key b1 at alter j1 with its error bound e1, and the
+// largest upper bound (key + its error bound) of every other alter. The
+// float32 keys certify the choice when b1 - e1 > ub2.
+struct KeyTop {
+  float b1, e1, ub2;
   int j1;
 };
-__device__ __forceinline__ void top2_merge(Top2 &a, const Top2 &c) {
+// alters reach a lane in ascending j: a key equal to the best is not better
+// (its upper bound then reaches b1, which sends the choice to float64)
+__device__ __forceinline__ void keytop_add(KeyTop &t, float g, float E, int j) {
+  if (g > t.b1) {
+    t.ub2 = fmaxf(t.ub2, __fadd_rn(t.b1, t.e1));
+    t.b1 = g;
+    t.e1 = E;
+    t.j1 = j;
+  } else {
+    t.ub2 = fmaxf(t.ub2, __fadd_rn(g, E));   // fmaxf drops a NaN key
+  }
+}
+__device__ __forceinline__ void keytop_merge(KeyTop &a, const KeyTop &c) {
   if (c.b1 > a.b1 || (c.b1 == a.b1 && c.j1 < a.j1)) {
-    a.b2 = fmaxf(c.b2, a.b1);
+    a.ub2 = fmaxf(fmaxf(a.ub2, c.ub2), __fadd_rn(a.b1, a.e1));
     a.b1 = c.b1;
+    a.e1 = c.e1;
     a.j1 = c.j1;
   } else {
-    a.b2 = fmaxf(a.b2, c.b1);
+    a.ub2 = fmaxf(fmaxf(a.ub2, c.ub2), __fadd_rn(c.b1, c.e1));
   }
 }
-__device__ __forceinline__ Top2 team_top2(const Team &T, Top2 x, double *red) {
+__device__ __forceinline__ KeyTop team_keytop(const Team &T, KeyTop x, double *red) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    Top2 y;
+    KeyTop y;
     y.b1 = __shfl_xor_sync(kFull, x.b1, o);
-    y.b2 = __shfl_xor_sync(kFull, x.b2, o);
+    y.e1 = __shfl_xor_sync(kFull, x.e1, o);
+    y.ub2 = __shfl_xor_sync(kFull, x.ub2, o);
     y.j1 = __shfl_xor_sync(kFull, x.j1, o);
-    top2_merge(x, y);
+    keytop_merge(x, y);
   }
   if (T.G == 1) return x;
-  float *rb = (float *)red;
-  int *rj = (int *)(red + T.G);
+  float *rb = (float *)red;          // 3 floats per warp
+  int *rj = (int *)(rb + 3 * T.G);   // 1 int per warp
   T.sync();
-  if (T.lane == 0) { rb[2 * T.warp] = x.b1; rb[2 * T.warp + 1] = x.b2; rj[T.warp] = x.j1; }
+  if (T.lane == 0) {
+    rb[3 * T.warp] = x.b1;
+    rb[3 * T.warp + 1] = x.e1;
+    rb[3 * T.warp + 2] = x.ub2;
+    rj[T.warp] = x.j1;
+  }
   T.sync();
-  Top2 a{rb[0], rb[1], rj[0]};
-  for (int w = 1; w < T.G; ++w) top2_merge(a, Top2{rb[2 * w], rb[2 * w + 1], rj[w]});
+  KeyTop a{rb[0], rb[1], rb[2], rj[0]};
+  for (int w = 1; w < T.G; ++w) keytop_merge(a, KeyTop{rb[3 * w], rb[3 * w + 1], rb[3 * w + 2], rj[w]});
   return a;
-}
-
-// float32 image of y (finite, <= 0) truncated toward zero: relative error
-// below 2^-23, formed on the integer pipes. Values below -1e4 (never in the
-// Gumbel shortlist, whose members have y >= -26.1) become -inf.
-__device__ __forceinline__ float shortlist_f32(double y) {
-  if (!(y > -1e4)) return -INFINITY;
-  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
-  const int fe = (int)((b >> 52) & 0x7FF) - 1023 + 127;
-  if (fe <= 0) return 0.0f;
-  const unsigned m = (unsigned)((b >> 29) & 0x7FFFFFu);
-  return __uint_as_float((unsigned)((b >> 63) << 31) | ((unsigned)fe << 23) | m);
 }
 
 __device__ __forceinline__ bool is_nan64(double x) {
@@ -261,18 +269,19 @@ __device__ __forceinline__ bool is_nan64(double x) {
   return ((b >> 52) & 0x7FF) == 0x7FF && (b & 0xFFFFFFFFFFFFFull) != 0;
 }
 
-// Team sums of sume and wsum[0..k-1]: warp recursive halving over V >= k+1
-// values, then one slot per (quantity, warp) in red[q*G + warp].
+// Team sums of sume and wsum[0..k-1] (float32): warp recursive halving over
+// V >= k+1 values, then one float64 slot per (quantity, warp) in
+// red[q*G + warp], summed across warps in float64 by the score update.
 template <int V>
-__device__ __forceinline__ void lse_reduce(const Team &T, const Slice &S, double sume,
-                                           const double *wsum, int k) {
-  double v[V];
+__device__ __forceinline__ void lse_reduce(const Team &T, const Slice &S, float sume,
+                                           const float *wsum, int k) {
+  float v[V];
   v[0] = sume;
 #pragma unroll
-  for (int q = 1; q < V; ++q) v[q] = (q - 1 < k) ? wsum[q - 1] : 0.0;
+  for (int q = 1; q < V; ++q) v[q] = (q - 1 < k) ? wsum[q - 1] : 0.f;
   const int q = warp_multi_sum<V>(v, T.lane);
   const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
-  if (writer && q <= k) S.red[q * T.G + T.warp] = v[0];
+  if (writer && q <= k) S.red[q * T.G + T.warp] = (double)v[0];
 }
 
 // One chain: the ministep loop and the chain's outputs.
@@ -288,7 +297,8 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
   const double pnet = __ddiv_rn(lam, __dadd_rn(lam, lamb));
   long long dist = 0, bdist = 0, ms = 0, msb = 0;
   double t = 0.0, rho = 0.0;
-  double d[24], wsum[24], dbest[24];
+  double d[24];
+  float d32[24], wsum[24];
 
   for (;;) {
     int i;
@@ -350,95 +360,92 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
       T.sync();
     }
 
-    // ---- pass 1: change statistics, f_j, lmax ------------------------------
-    long long kmax = dkey(-1e30);
+    // ---- one pass over the alters ------------------------------------------
+    // Lane by lane, alters in ascending j: integer change statistics, the
+    // float32 predictor f32_j (change_stats32), the float32 Gumbel key
+    // g_j = f32_j - loglog_est(u_j) with u_j from the reference's counters
+    // (msteps, chain, 1, j), and an online log-sum-exp (a running maximum m,
+    // the weight sums rescaled when it rises). The key is within
+    //   E_j = (k + 10) 2^-24 absf_j + 6e-6
+    // of the float64 key f_j - log(-log u_j): (k + 8) u absf_j for f32_j, 4e-6
+    // for loglog_est and u (absf_j + 23) for the subtraction (|f32_j| <= absf_j,
+    // |log(-log u)| < 23). gbuf[j] keeps the upper bound g_j + E_j.
+    float m = -INFINITY, sume = 0.f;
+    for (int e = 0; e < k; ++e) wsum[e] = 0.f;
+    KeyTop best{-INFINITY, 0.f, -INFINITY, 0x7FFFFFFF};
+    const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
     for (int jb = 32 * T.warp; jb < n; jb += L) {
       const int j = jb + T.lane;
       bool ok = false;
       if (j < n) {
         const int aij = bit_of(S.rowsT, n, i, j);
-        double f = 0.0;
-        if (j == i) {
-          ok = true;
-        } else {
-          ok = bit_of(P.permT, n, i, j) &&
-               !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg);
-          if (ok) {
-            const int aji = bit_of(S.colsT, n, i, j);
-            f = change_stats<true>(P, S, X, j, aij, aji, d);
+        float ub = -INFINITY;
+        ok = (j == i) || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
+        if (ok) {
+          float f = 0.f, absf = 0.f;
+          const bool stay = j == i;
+          if (!stay) f = change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+          // a NaN predictor turns the sums into NaN, as exp(NaN - lmax) does
+          // in the reference, and never wins the choice (its key compares false)
+          if (f > m) {
+            const float r = expf(__fsub_rn(m, f));   // 0 while m = -inf
+            sume = __fadd_rn(__fmul_rn(sume, r), 1.f);
+            for (int e = 0; e < k; ++e)
+              wsum[e] = __fadd_rn(__fmul_rn(wsum[e], r), stay ? 0.f : d32[e]);
+            m = f;
+          } else {
+            const float w = expf(__fsub_rn(f, m));
+            sume = __fadd_rn(sume, w);
+            if (!stay)
+              for (int e = 0; e < k; ++e) wsum[e] = __fadd_rn(wsum[e], __fmul_rn(w, d32[e]));
           }
+          uint32_t ph[4];
+          philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
+          const float g = __fsub_rn(f, loglog_est(ph[0]));
+          const float E = __fadd_rn(__fmul_rn(ecoef, absf), 6e-6f);
+          ub = __fadd_rn(g, E);
+          keytop_add(best, g, E, j);
         }
-        S.fbuf[j] = f;
-        // a NaN predictor never raises the maximum (the reference compares
-        // f > lmax) and is never chosen (its Gumbel key compares false)
-        if (ok && !is_nan64(f)) {
-          const long long kf = dkey(f);
-          kmax = kf > kmax ? kf : kmax;
-        }
+        S.gbuf[j] = ub;
       }
       const uint32_t okb = __ballot_sync(kFull, ok);
       if (T.lane == 0) S.okbits[jb >> 5] = okb;
     }
-    const double lmax = dunkey(team_max_ll(T, kmax, S.red));
-    T.sync();
-
-    // ---- pass 2: log-sum-exp sums and float32 Gumbel estimates --------------
-    // The estimate of g_j - lmax, shortlist_f32(f_j - lmax) - loglog_est(u_j),
-    // is within 2^-23*26.1 + 2.2e-6 + 2^-24*23 < 7e-6 of the float64 value for
-    // every alter that can be the argmax (those have f_j - lmax >= -26.1, as
-    // their key is at least the key of the lmax alter, >= -3.2).
-    double sume = 0.0;
-    for (int e = 0; e < k; ++e) wsum[e] = 0.0;
-    Top2 best{-INFINITY, -INFINITY, 0x7FFFFFFF};
-    for (int j = T.tl; j < n; j += L) {
-      if (!((S.okbits[j >> 5] >> (j & 31)) & 1u)) {
-        S.gbuf[j] = -INFINITY;
-        continue;
-      }
-      const double y = __dsub_rn(S.fbuf[j], lmax);
-      const double wj = exp_weight(y, S.exptab);
-      sume = __dadd_rn(sume, wj);
-      if (j != i) {
-        const int aij = bit_of(S.rowsT, n, i, j);
-        const int aji = bit_of(S.colsT, n, i, j);
-        change_stats<false>(P, S, X, j, aij, aji, d);
-        for (int e = 0; e < k; ++e) wsum[e] = fma(wj, d[e], wsum[e]);
-      }
-      uint32_t ph[4];
-      philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-      const float gt = shortlist_f32(y) - loglog_est(ph[0]);
-      S.gbuf[j] = gt;
-      if (gt > best.b1) {  // j ascending within a lane: ties keep the earlier j
-        best.b2 = best.b1;
-        best.b1 = gt;
-        best.j1 = j;
-        if (j != i)
-          for (int e = 0; e < k; ++e) dbest[e] = d[e];
-      } else {
-        best.b2 = fmaxf(best.b2, gt);
-      }
+    // log-sum-exp sums: each lane rescaled to the team maximum, then summed
+    {
+      const float M = team_max_f(T, m, S.red);
+      const float r = (m == M) ? 1.f : expf(__fsub_rn(m, M));
+      sume = __fmul_rn(sume, r);
+      for (int e = 0; e < k; ++e) wsum[e] = __fmul_rn(wsum[e], r);
     }
-    const int jsaved = best.j1;
+    T.sync();
     if (k + 1 <= 8) lse_reduce<8>(T, S, sume, wsum, k);
     else if (k + 1 <= 16) lse_reduce<16>(T, S, sume, wsum, k);
     else lse_reduce<32>(T, S, sume, wsum, k);
-    const Top2 top = team_top2(T, best, S.red + 26 * T.G);
+    const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
 
     // ---- the chosen alter ---------------------------------------------------
-    // The float estimates decide unless the top two are within the window;
-    // then the shortlist's exact float64 keys decide, ties to the smaller j.
+    // The float32 keys decide when the best key's lower bound exceeds every
+    // other alter's upper bound. Otherwise every alter whose upper bound
+    // reaches that lower bound gets its exact float64 key (the reference's
+    // f_j - log(-log u_j)) and those decide, ties to the smaller j.
     int jstar;
-    if (top.b1 - top.b2 > kGumbelWindow) {
+    const float lb = __fsub_rn(top.b1, top.e1);
+    if (lb > top.ub2) {
       jstar = top.j1;
     } else {
       long long bk = dkey(-1e300);
       int bj = 0x7FFFFFFF;
-      const float thr = top.b1 - kGumbelWindow;
       for (int j = T.tl; j < n; j += L) {
-        if (S.gbuf[j] >= thr) {
+        if (S.gbuf[j] >= lb) {
+          double f = 0.0;
+          if (j != i) {
+            const int aij = bit_of(S.rowsT, n, i, j);
+            f = change_stats<true>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
+          }
           uint32_t ph[4];
           philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-          const double g = __dsub_rn(S.fbuf[j], log(-log(unif01(ph[0]))));
+          const double g = __dsub_rn(f, log(-log(unif01(ph[0]))));
           if (is_nan64(g)) continue;
           const long long kg = dkey(g);
           if (kg > bk || (kg == bk && j < bj)) { bk = kg; bj = j; }
@@ -448,11 +455,10 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
     }
 
     // ---- score update (lane e updates effect e) and toggle ----------------
+    // the chosen alter's change statistics in float64, as the reference adds them
     if (T.tl == jstar % L) {
       if (jstar == i) {
         for (int e = 0; e < k; ++e) S.dstar[e] = 0.0;
-      } else if (jsaved == jstar) {
-        for (int e = 0; e < k; ++e) S.dstar[e] = dbest[e];
       } else {
         const int aij = bit_of(S.rowsT, n, i, jstar);
         const int aji = bit_of(S.colsT, n, i, jstar);

@@ -83,6 +83,7 @@ struct DevProblem {
   // effect plan (k each) and its table pool
   const int *ekind, *ecfn, *eoffd, *eofft;
   const double *tab;
+  const float *tab32;  // float32 copy of tab's lookup values (the float32 pass)
 
   // outputs (chain-major), any may be null
   double *stats, *ntim;
@@ -150,58 +151,5 @@ __device__ __forceinline__ float loglog_est(uint32_t x) {
   return logf(L);
 }
 
-// exp(y) for the log-sum-exp weights, y = f_j - lmax <= 0: the table-driven
-// method of P. T. P. Tang (ACM TOMS 15(2):144-157, 1989). y = (64 N + j) ln2/64
-// + r with |r| <= ln2/128; exp(r) - 1 by its degree-5 Taylor polynomial
-// (truncation < 4e-17 relative); the result 2^(j/64) (1 + p) scaled by 2^N in
-// the exponent field. Ten float64 operations. Weights below e^-700 (invisible
-// next to the weight 1 of the maximum) are returned as 0; NaN propagates.
-// 2^(j/64), j = 0..63, correctly rounded (computed at 60 digits). Kernels copy
-// it to shared memory: lanes index it with different j.
-__device__ const double kExp2Frac64[64] = {
-    1.0, 1.0108892860517005, 1.0218971486541166, 1.0330248790212284,
-    1.0442737824274138, 1.0556451783605572, 1.0671404006768237, 1.0787607977571199,
-    1.0905077326652577, 1.102382583307841, 1.1143867425958924, 1.1265216186082418,
-    1.1387886347566916, 1.1511892299529827, 1.1637248587775775, 1.1763969916502812,
-    1.189207115002721, 1.202156731452703, 1.215247359980469, 1.22848053610687,
-    1.241857812073484, 1.255380757024691, 1.2690509571917332, 1.2828700160787783,
-    1.2968395546510096, 1.3109612115247644, 1.3252366431597413, 1.339667524053303,
-    1.3542555469368927, 1.3690024229745905, 1.383909881963832, 1.3989796725383112,
-    1.4142135623730951, 1.42961333839197, 1.4451808069770467, 1.460917794180647,
-    1.4768261459394993, 1.4929077282912648, 1.5091644275934228, 1.5255981507445384,
-    1.5422108254079407, 1.559004400237837, 1.5759808451078865, 1.593142151342267,
-    1.6104903319492543, 1.6280274218573478, 1.645755478153965, 1.6636765803267364,
-    1.681792830507429, 1.7001063537185235, 1.718619298122478, 1.7373338352737062,
-    1.7562521603732995, 1.7753764925265212, 1.7947090750031072, 1.8142521755003989,
-    1.8340080864093424, 1.8539791250833855, 1.8741676341103, 1.8945759815869656,
-    1.9152065613971474, 1.9360617934922943, 1.9571441241754002, 1.978456026387951};
-
-__device__ __forceinline__ double exp_weight(double y, const double *tab64) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
-  if (((b >> 52) & 0x7FF) == 0x7FF)                      // NaN propagates, -inf -> 0
-    return (b & 0xFFFFFFFFFFFFFull) ? y : ((b >> 63) ? 0.0 : y);
-  if (b > 0xC085E00000000000ull) return 0.0;              // y < -700
-  const double kInv = 92.33248261689366;                  // 64 / ln2
-  const double kShift = 6755399441055744.0;               // 1.5 * 2^52
-  const double kHi = 0.010830424667801708;                // ln2/64, 29 significant bits
-  const double kLo = 2.8447437476627285e-11;              // ln2/64 - kHi
-  const double t = __fma_rn(y, kInv, kShift);
-  const int m = __double2loint(t);                        // round(y * 64 / ln2)
-  const double kd = __dsub_rn(t, kShift);
-  double r = __fma_rn(kd, -kHi, y);                       // exact: |kd| < 2^16
-  r = __fma_rn(kd, -kLo, r);
-  double p = __fma_rn(r, 1.0 / 120.0, 1.0 / 24.0);
-  p = __fma_rn(p, r, 1.0 / 6.0);
-  p = __fma_rn(p, r, 0.5);
-  p = __fma_rn(p, __dmul_rn(r, r), r);
-  const double s = tab64[m & 63];
-  const double res = __fma_rn(s, p, s);
-  return __longlong_as_double(__double_as_longlong(res) + ((long long)(m >> 6) << 52));
-}
-
-// Candidate window of the Gumbel-max shortlist. The float estimate of
-// g - lmax is within 8e-6 of the float64 value for every alter that can be
-// the argmax (error analysis in the kernel); 1e-4 leaves a 6x margin.
-constexpr float kGumbelWindow = 1e-4f;
 
 }  // namespace cusna

@@ -6,18 +6,17 @@
 // team owns a slice of dynamic shared memory: the chain's out-rows and in-rows
 // as word-major bitsets, degrees, behaviour values and per-alter scratch.
 //
-// A network ministep (src/libcusna_saom_cpu.cpp:229-287) runs in three passes
-// over the alters j, which the team's lanes split in strides of 32*G:
-//   pass 1  change statistics d_je from popcounts of the bitsets, the float64
-//           linear predictor f_j = sum_e theta_e * d_je in the reference's
-//           e-order, and the maximum lmax of f over permitted alters;
-//   pass 2  w_j = exp(f_j - lmax) with the float64 sums sum_j w_j and
-//           sum_j w_j d_je (the log-sum-exp score), plus a float32 estimate of
-//           the Gumbel key g_j = f_j - log(-log u_j) for a shortlist;
-//   pass 3  the exact float64 Gumbel key of each shortlisted alter and the
-//           argmax with ties to the smaller j, as the reference chooses.
-// u_j comes from the reference's Philox counters (msteps, chain, 1, j), so the
-// chosen alter, and therefore the whole trajectory, equals the CPU engine's.
+// A network ministep (src/libcusna_saom_cpu.cpp:229-287) is one pass over the
+// alters j, which the team's lanes split in strides of 32*G: change statistics
+// d_je from popcounts of the bitsets, the linear predictor f_j = sum_e theta_e
+// d_je in float32 with a rigorous error bound, the float32 Gumbel key
+// g_j = f_j - log(-log u_j) with its bound, and an online log-sum-exp of the
+// score sums. The keys decide the chosen alter when the best key's lower bound
+// beats every other key's upper bound; otherwise the exact float64 keys of the
+// alters still in range decide, ties to the smaller j, as the reference
+// chooses. u_j comes from the reference's Philox counters (msteps, chain, 1,
+// j), so the chosen alter, and therefore the whole trajectory, equals the CPU
+// engine's.
 #pragma once
 #include "saom_common.cuh"
 
@@ -38,8 +37,7 @@ struct Slice {
   uint32_t *colsT;   // W*n (shared or global scratch)
   short *indeg, *outdeg;  // n each (degrees < 2^15 as n <= 8192)
   int *z;
-  double *fbuf;      // n
-  float *gbuf;       // n
+  float *gbuf;       // n   upper bounds of the float32 Gumbel keys
   uint32_t *okbits;  // W
   int *tp;           // n   (transTies / gwdsp)
   int *tq;           // n   (gwdspFB)
@@ -47,6 +45,7 @@ struct Slice {
   double *crate;     // n   (non-basic rates)
   double *red;       // 32*G reduction scratch
   double *th;        // k  parameters of the current chain
+  float *th32;       // k  the same parameters (they are float32 inputs)
   double *sc;        // k  scores
   double *dstar;     // k  change statistics of the chosen alter
   double *thb, *bsc; // kb
@@ -59,14 +58,14 @@ struct Slice {
   uint32_t *rr3;     //   behaviour uniform
   int *ekind, *ecfn, *eoffd, *eofft;  // k  effect plan
   double *stepd, *stept;  // 4k  per-ministep K_STEP magnitudes and terms
-  double *exptab;    // 64  2^(j/64) for exp_weight
+  float *stepd32, *stept32;  // 4k  their float32 images
 };
 
 struct SliceLayout {
   size_t bytes;  // per team
-  size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_f, o_g, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
+  size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_g, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
       o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc, o_rtau, o_rnet, o_rfocal, o_rr3, o_ekind, o_ecfn, o_eoffd, o_eofft,
-      o_stepd, o_stept, o_exptab;
+      o_stepd, o_stept, o_th32, o_stepd32, o_stept32;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -83,7 +82,6 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_indeg, (size_t)n * 2);
   put(s.o_outdeg, (size_t)n * 2);
   put(s.o_z, (size_t)n * 4);
-  put(s.o_f, (size_t)n * 8);
   put(s.o_g, (size_t)n * 4);
   put(s.o_ok, (size_t)W * 4);
   put(s.o_tp, need_tp || need_gw ? (size_t)n * 4 : 0);
@@ -118,7 +116,9 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_eofft, (size_t)k * 4);
   put(s.o_stepd, (size_t)k * 4 * 8);
   put(s.o_stept, (size_t)k * 4 * 8);
-  put(s.o_exptab, 64 * 8);
+  put(s.o_th32, (size_t)k * 4);
+  put(s.o_stepd32, (size_t)k * 4 * 4);
+  put(s.o_stept32, (size_t)k * 4 * 4);
   s.bytes = al16(o);
   return s;
 }
@@ -131,7 +131,6 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   s.indeg = (short *)(base + L.o_indeg);
   s.outdeg = (short *)(base + L.o_outdeg);
   s.z = (int *)(base + L.o_z);
-  s.fbuf = (double *)(base + L.o_f);
   s.gbuf = (float *)(base + L.o_g);
   s.okbits = (uint32_t *)(base + L.o_ok);
   s.tp = (int *)(base + L.o_tp);
@@ -166,7 +165,9 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   s.eofft = (int *)(base + L.o_eofft);
   s.stepd = (double *)(base + L.o_stepd);
   s.stept = (double *)(base + L.o_stept);
-  s.exptab = (double *)(base + L.o_exptab);
+  s.th32 = (float *)(base + L.o_th32);
+  s.stepd32 = (float *)(base + L.o_stepd32);
+  s.stept32 = (float *)(base + L.o_stept32);
   return s;
 }
 
@@ -179,8 +180,11 @@ __device__ __forceinline__ int bit_of(const uint32_t *T, int n, int row, int col
 // exchanges half of the remaining values with the lane 16>>s away, so a lane
 // does V-1 + (5 - log2 V) additions instead of 5V. Afterwards the lane holds the
 // warp total of quantity q(lane) in v[0]; lanes with bit 0 clear report it.
-template <int V>
-__device__ __forceinline__ int warp_multi_sum(double (&v)[V], int lane) {
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+
+template <int V, class R>
+__device__ __forceinline__ int warp_multi_sum(R (&v)[V], int lane) {
   int q = 0;
   int cnt = V;
 #pragma unroll
@@ -190,10 +194,10 @@ __device__ __forceinline__ int warp_multi_sum(double (&v)[V], int lane) {
     const bool up = (lane & o) != 0;
 #pragma unroll
     for (int x = 0; x < half; ++x) {
-      double send = up ? v[x] : v[x + half];
-      double keep = up ? v[x + half] : v[x];
-      double got = __shfl_xor_sync(kFull, send, o);
-      v[x] = __dadd_rn(keep, got);
+      const R send = up ? v[x] : v[x + half];
+      const R keep = up ? v[x + half] : v[x];
+      const R got = __shfl_xor_sync(kFull, send, o);
+      v[x] = radd(keep, got);
     }
     if (up) q += half;
     cnt = half;
@@ -203,7 +207,7 @@ __device__ __forceinline__ int warp_multi_sum(double (&v)[V], int lane) {
 #pragma unroll
   for (int s = 0; s < 5; ++s) {
     const int o = 16 >> s;
-    if ((1 << s) >= V) v[0] = __dadd_rn(v[0], __shfl_xor_sync(kFull, v[0], o));
+    if ((1 << s) >= V) v[0] = radd(v[0], __shfl_xor_sync(kFull, v[0], o));
   }
   return q;
 }
@@ -410,6 +414,8 @@ __device__ __forceinline__ void step_values(const Team &T, const DevProblem &P, 
     }
     S.stepd[x] = v;
     S.stept[x] = __dmul_rn(S.th[e], v);
+    S.stepd32[x] = (float)v;
+    S.stept32[x] = (float)S.stept[x];
   }
 }
 
@@ -509,6 +515,109 @@ __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice 
     d[e] = v;
     if (has_term) f = __dadd_rn(f, term);
   }
+  return f;
+}
+
+// float32 image of change_stats<true> for the shortlist pass: d32[e] is the
+// float32 rounding of the change statistic d_e (exact for the integer counts;
+// an interaction is the float32 product of its components), and the return
+// value is f32 = sum_e fl32(theta_e * d32[e]), added in the reference's e-order
+// in float32; *absf = sum_e |fl32(theta_e * d32[e])|. With u = 2^-24 each term
+// differs from theta_e d_e by at most 7u|term| (at most five roundings in an
+// interaction product, one in the product with theta) and the k additions add
+// at most (k-1)u absf, so |f32 - f| <= (k + 8) u absf for the float64 predictor
+// f of change_stats<true> (itself within 2^-50 absf of the exact sum).
+__device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice &S,
+                                                const StepCtx &X, int j, int aij, int aji,
+                                                float *d32, float *absf) {
+  const int n = P.n, W = P.W, k = P.k, i = X.i;
+  const int fl = P.flags;
+  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;
+  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
+    const uint32_t *R = S.rowsT, *Cc = S.colsT;
+    for (int w = 0; w < W; ++w) {
+      const uint32_t ri = R[w * n + i], rj = R[w * n + j];
+      const uint32_t ci = Cc[w * n + i], cj = Cc[w * n + j];
+      if (fl & F_PC_RI_CJ) ri_cj += __popc(ri & cj);
+      if (fl & F_PC_RI_RJ) ri_rj += __popc(ri & rj);
+      if (fl & F_PC_RJ_CI) rj_ci += __popc(rj & ci);
+      if (fl & F_PC_CI_CJ) ci_cj += __popc(ci & cj);
+      if (fl & F_PC_CI_RJ) ci_rj += __popc(ci & rj);
+      if (fl & F_PC_RICIRJ) ricirj += __popc(ri & ci & rj);
+    }
+  }
+  const uint32_t sg = aij ? 0x80000000u : 0u;
+  float f = 0.f, a = 0.f;
+#pragma unroll 1
+  for (int e = 0; e < k; ++e) {
+    const int kind = S.ekind[e], cfn = S.ecfn[e];
+    float v, term = 0.f;
+    bool has_term = true;
+    if (kind == K_CNT) {
+      int c;
+      switch (cfn) {
+        case 0: c = 1; break;
+        case 1: c = aji; break;
+        case 2: c = ri_cj + ri_rj; break;
+        case 3: c = rj_ci; break;
+        case 4: c = S.indeg[j] + 1 - aij; break;
+        case 5: {
+          c = 0;
+          const uint32_t *eq = S.tpeq + (aij ? W : 0);
+          for (int w = 0; w < W; ++w)
+            c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);
+          if (S.tp[j] > 0) ++c;
+          break;
+        }
+        case 6: c = (aji ? ri_cj : 0) + ricirj; break;
+        default: c = S.outdeg[j]; break;  // 7
+      }
+      v = __uint_as_float(__float_as_uint((float)c) ^ sg);
+      term = __fmul_rn(S.th32[e], v);
+    } else if (kind == K_LOOK) {
+      int idx;
+      switch (cfn) {
+        case 4: idx = S.indeg[j] + 1 - aij; break;
+        case 7: idx = S.outdeg[j]; break;
+        case 8: idx = ri_cj; break;
+        case 9: idx = ri_rj; break;
+        case 10: idx = ci_cj; break;
+        case 11: idx = ci_rj; break;
+        case 12: idx = j; break;
+        case 13: idx = S.z[j] - P.zlo; break;
+        case 14: idx = i * n + j; break;
+        default: idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo); break;  // 15
+      }
+      v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[e] + idx]) ^ sg);
+      term = __fmul_rn(S.th32[e], v);
+    } else if (kind == K_STEP) {
+      const int q = 2 * aij + aji;
+      v = S.stepd32[4 * e + q];
+      term = S.stept32[4 * e + q];
+    } else if (kind == K_ZERO) {
+      v = 0.f;
+      has_term = false;
+    } else if (S.tid[e] == 32) {
+      const int c2 = S.i2[e];
+      v = __fmul_rn(d32[S.i0[e]], d32[S.i1[e]]);
+      if (c2 >= 0) v = __fmul_rn(v, d32[c2]);
+      else if (aij) v = -v;
+      term = __fmul_rn(S.th32[e], v);
+    } else {
+      v = (float)gen_stat(P, S, X, e, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, nullptr);
+      term = __fmul_rn(S.th32[e], v);
+    }
+    if ((S.ety[e] == 1 && aij) || (S.ety[e] == 2 && !aij)) {
+      v = 0.f;
+      has_term = false;
+    }
+    d32[e] = v;
+    if (has_term) {
+      f = __fadd_rn(f, term);
+      a = __fadd_rn(a, fabsf(term));
+    }
+  }
+  *absf = a;
   return f;
 }
 
