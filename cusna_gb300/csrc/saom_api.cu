@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -674,12 +675,11 @@ cusna_status fetch_outputs(Job &J) {
 // memory, registers and warps all count). The score is the number of warps that
 // will be busy: min(resident teams, chains) * G per SM, capped at 48; ties go to
 // smaller teams (fewer barriers) and to in-rows in shared memory.
-LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bool gw,
-                         bool tq, long long total_units, int force_G, int force_tpc) {
+std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp,
+                                     bool gw, bool tq, long long total_units, int force_G,
+                                     int force_tpc) {
   const Ctx &c = g_ctx;
-  LaunchShape best{};
-  best.G = 0;
-  double best_score = -1.0;
+  std::vector<std::pair<double, LaunchShape>> all;
   const int Gs[5] = {1, 2, 4, 8, 16};
   for (int gi = 0; gi < 5; ++gi) {
     const int G = Gs[gi];
@@ -693,6 +693,7 @@ LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, boo
       sh.rows_in_smem = rows_smem;
       sh.lay = make_layout(nmax, Wmax, kmax, kbmax, nrmax, G, rows_smem, cols_smem, tp, gw, tq);
       if (sh.lay.bytes > (size_t)c.smem_optin) continue;
+      bool any = false;
       for (int tpc = 1; tpc <= 16; tpc *= 2) {
         if (force_tpc && tpc != force_tpc) continue;
         const int threads = 32 * G * tpc;
@@ -704,20 +705,114 @@ LaunchShape choose_shape(int nmax, int Wmax, int kmax, int kbmax, int nrmax, boo
         const double teams_sm = (double)per_sm * tpc;
         const double chains_sm = (double)total_units / c.sms;
         const double busy_warps = std::min(teams_sm, std::max(chains_sm, 1.0)) * G;
+        // ties: smaller teams (fewer barriers), state on chip, then larger CTAs
         const double score = std::min(busy_warps, 48.0) * 100.0 - G - (cols_smem ? 0.0 : 50.0) -
-                             (rows_smem ? 0.0 : 50.0) - tpc * 0.01;
-        if (score > best_score) {
-          best_score = score;
-          best = sh;
-          best.teams_per_cta = tpc;
-          const long long want = (total_units + tpc - 1) / tpc;
-          best.ctas = (int)std::max<long long>(1, std::min<long long>((long long)c.sms * per_sm, want));
-        }
+                             (rows_smem ? 0.0 : 50.0) + tpc * 0.01;
+        LaunchShape x = sh;
+        x.teams_per_cta = tpc;
+        const long long want = (total_units + tpc - 1) / tpc;
+        x.ctas = (int)std::max<long long>(1, std::min<long long>((long long)c.sms * per_sm, want));
+        all.push_back({score, x});
+        any = true;
       }
-      if (best.G == G && best.cols_in_smem == cols_smem && best.rows_in_smem == rows_smem) break;
+      if (any) break;   // the first placement that fits is the one used for this G
     }
   }
-  return best;
+  std::stable_sort(all.begin(), all.end(),
+                   [](const std::pair<double, LaunchShape> &a, const std::pair<double, LaunchShape> &b) {
+                     return a.first > b.first;
+                   });
+  std::vector<LaunchShape> out;
+  for (auto &x : all) out.push_back(x.second);
+  return out;
+}
+
+// ---- empirical autotuner ---------------------------------------------------------
+// The occupancy model ranks shapes, but the best team size depends on how the
+// per-ministep team work (reductions, barriers) trades against the per-alter
+// work, which it does not model. Results do not depend on the shape (every
+// output is bit-identical for every shape), so the tuner explores on real
+// calls: successive calls with the same signature each try one of the model's
+// two best shapes of each team size (G = 1, 2, 4, 8, 16, in the model's
+// order), timed with events, and later calls use the fastest.
+// CUSNA_AUTOTUNE=0 keeps the model's choice.
+struct TuneKey {
+  int dev, nmax, Wmax, kmax, kbmax, nrmax, flags, pad;
+  long long units;
+};
+struct TuneEntry {
+  TuneKey key;
+  std::vector<LaunchShape> cand;
+  std::vector<float> ms;
+  size_t next = 0;
+  int best = -1;
+};
+std::mutex g_tune_mu;
+std::vector<TuneEntry> g_tune;
+
+bool tuning_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("CUSNA_AUTOTUNE");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+TuneKey tune_key(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bool gw, bool tq,
+                 long long units) {
+  TuneKey k;
+  std::memset(&k, 0, sizeof k);
+  k.dev = g_ctx.device; k.nmax = nmax; k.Wmax = Wmax; k.kmax = kmax; k.kbmax = kbmax;
+  k.nrmax = nrmax; k.flags = (tp ? 1 : 0) | (gw ? 2 : 0) | (tq ? 4 : 0); k.units = units;
+  return k;
+}
+
+// the model's two best shapes of each team size, in the model's order
+std::vector<LaunchShape> tuning_candidates(const std::vector<LaunchShape> &ranked) {
+  std::vector<LaunchShape> c;
+  for (const LaunchShape &s : ranked) {
+    int seen = 0;
+    for (const LaunchShape &x : c) seen += x.G == s.G;
+    if (seen < 2) c.push_back(s);
+  }
+  return c;
+}
+
+TuneEntry &tune_entry(const TuneKey &key, const std::vector<LaunchShape> &cand) {
+  for (auto &e : g_tune)
+    if (std::memcmp(&e.key, &key, sizeof key) == 0) return e;
+  TuneEntry e;
+  e.key = key;
+  e.cand = cand;
+  e.ms.assign(cand.size(), INFINITY);
+  if (!tuning_enabled() || cand.size() < 2) { e.next = cand.size(); e.best = 0; }
+  g_tune.push_back(e);
+  return g_tune.back();
+}
+
+// The shape for this call; *trial is the candidate being timed, or -1.
+LaunchShape tuner_pick(const TuneKey &key, const std::vector<LaunchShape> &cand, int *trial) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  TuneEntry &e = tune_entry(key, cand);
+  if (e.next < e.cand.size()) {
+    *trial = (int)e.next++;
+    return e.cand[*trial];
+  }
+  *trial = -1;
+  return e.cand[e.best >= 0 ? e.best : 0];
+}
+
+void tuner_record(const TuneKey &key, int trial, float ms) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (auto &e : g_tune)
+    if (std::memcmp(&e.key, &key, sizeof key) == 0) {
+      if (trial >= 0 && (size_t)trial < e.ms.size()) e.ms[trial] = ms;
+      int b = 0;
+      for (size_t x = 1; x < e.ms.size(); ++x)
+        if (e.ms[x] < e.ms[b]) b = (int)x;
+      e.best = b;
+      return;
+    }
 }
 
 // Register limit check of a shape: the kernel is compiled for 512 threads with
@@ -746,12 +841,18 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
     tq |= (J.F.flags & F_NEED_GW30) != 0;
     total += J.p->M;
   }
-  LaunchShape sh = choose_shape(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total,
-                                opts ? opts->warps_per_chain : 0, opts ? opts->chains_per_cta : 0);
-  if (sh.G == 0) {
+  const int fG = opts ? opts->warps_per_chain : 0, fT = opts ? opts->chains_per_cta : 0;
+  const std::vector<LaunchShape> ranked =
+      rank_shapes(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, fG, fT);
+  if (ranked.empty()) {
     set_err("no launch shape fits n=%d in shared memory", nmax);
     return CUSNA_ERR_UNSUPPORTED;
   }
+  // a forced shape is used as given; otherwise the autotuner picks (and may be
+  // timing one of its candidates in this call)
+  int trial = -1;
+  const TuneKey tkey = tune_key(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total);
+  const LaunchShape sh = (fG || fT) ? ranked[0] : tuner_pick(tkey, tuning_candidates(ranked), &trial);
   Planner pl;
   for (auto &J : jobs) plan_problem(pl, J, dev);
   const size_t o_probs = pl.take(sizeof(DevProblem) * jobs.size());
@@ -784,9 +885,10 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
     for (auto &J : jobs)
       if ((s = fetch_outputs(J)) != CUSNA_OK) return s;
   CU(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  CU(cudaEventElapsedTime(&ms, g_ctx.ev0, g_ctx.ev1));
+  if (trial >= 0) tuner_record(tkey, trial, ms);
   if (opts) {
-    float ms = 0.f;
-    CU(cudaEventElapsedTime(&ms, g_ctx.ev0, g_ctx.ev1));
     opts->elapsed_ms = ms;
     opts->warps_per_chain = sh.G;
     opts->chains_per_cta = sh.teams_per_cta;
@@ -863,6 +965,12 @@ struct cusna_saom_plan {
   uint32_t *cols = nullptr, *rows = nullptr;
   size_t cols_words = 0;
   cudaGraphExec_t graph = nullptr;
+  // autotuning over the first launches (one timed trial per candidate shape)
+  std::vector<cusna::LaunchShape> cand;
+  std::vector<float> cand_ms;
+  size_t trial = 0;
+  bool pending = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 namespace cusna {
@@ -871,6 +979,8 @@ namespace {
 void plan_free(cusna_saom_plan *P) {
   if (!P) return;
   if (P->graph) cudaGraphExecDestroy(P->graph);
+  if (P->ev0) cudaEventDestroy(P->ev0);
+  if (P->ev1) cudaEventDestroy(P->ev1);
   if (P->mem) cudaFree(P->mem);
   delete P;
 }
@@ -904,8 +1014,27 @@ cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *
     tq |= (J.F.flags & F_NEED_GW30) != 0;
     total += J.p->M;
   }
-  const LaunchShape sh = choose_shape(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, 0, 0);
-  if (sh.G == 0) { set_err("no launch shape fits n=%d", nmax); return CUSNA_ERR_UNSUPPORTED; }
+  const std::vector<LaunchShape> ranked =
+      rank_shapes(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, 0, 0);
+  if (ranked.empty()) { set_err("no launch shape fits n=%d", nmax); return CUSNA_ERR_UNSUPPORTED; }
+  std::vector<LaunchShape> cand = tuning_candidates(ranked);
+  {
+    // a signature the tuner has settled needs no exploration
+    const TuneKey key = tune_key(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto &e : g_tune)
+      if (std::memcmp(&e.key, &key, sizeof key) == 0 && e.next >= e.cand.size() && e.best >= 0)
+        cand = {e.cand[e.best]};
+  }
+  if (!tuning_enabled()) cand.resize(1);
+  const LaunchShape sh = cand[0];
+  size_t teams = 0;
+  bool cols_global = false, rows_global = false;
+  for (const LaunchShape &x : cand) {
+    teams = std::max(teams, (size_t)x.ctas * x.teams_per_cta);
+    cols_global |= !x.cols_in_smem;
+    rows_global |= !x.rows_in_smem;
+  }
   std::vector<PlanTable> tabs;
   for (int q = 0; q < count; ++q) {
     const Facts &F = jobs[q].F;
@@ -919,12 +1048,21 @@ cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *
   const size_t o_units = pl.take(sizeof(long long) * (count + 1));
   const size_t o_counter = pl.take(8), o_epoch = pl.take(8), o_seeds = pl.take(8 * (size_t)count);
   const size_t o_tabs = pl.take(sizeof(PlanTable) * std::max<size_t>(1, tabs.size()));
-  const size_t teams = (size_t)sh.ctas * sh.teams_per_cta;
   const size_t cols_words = (size_t)Wmax * nmax;
-  const size_t o_cols = sh.cols_in_smem ? NONE : pl.take(teams * cols_words * 4);
-  const size_t o_rows = sh.rows_in_smem ? NONE : pl.take(teams * cols_words * 4);
+  const size_t o_cols = cols_global ? pl.take(teams * cols_words * 4) : NONE;
+  const size_t o_rows = rows_global ? pl.take(teams * cols_words * 4) : NONE;
 
   cusna_saom_plan *P = new cusna_saom_plan();
+  P->cand = cand;
+  P->cand_ms.assign(cand.size(), INFINITY);
+  P->trial = cand.size() > 1 ? 0 : cand.size();
+  if (cand.size() > 1 &&
+      (cudaEventCreate(&P->ev0) != cudaSuccess || cudaEventCreate(&P->ev1) != cudaSuccess)) {
+    cudaGetLastError();
+    plan_free(P);
+    set_err("plan: cudaEventCreate failed");
+    return CUSNA_ERR_CUDA;
+  }
   P->device = g_ctx.device;
   if (cudaMalloc(&P->mem, pl.off) != cudaSuccess) {
     cudaGetLastError();
@@ -984,10 +1122,11 @@ cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *
 
 // Kernel launches only (capture-safe): epoch and term tables, work counter,
 // the persistent period kernel.
-cusna_status plan_enqueue(cusna_saom_plan *P, cudaStream_t st) {
+cusna_status plan_enqueue(cusna_saom_plan *P, const LaunchShape &sh, cudaStream_t st) {
   CU(launch_plan_prologue(P->probs, P->seeds, P->count, P->epoch, P->tabs, P->n_tabs, st));
   CU(cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), st));
-  CU(launch_period(P->sh, P->probs, P->units, P->count, P->total, P->counter, P->cols, P->rows,
+  CU(launch_period(sh, P->probs, P->units, P->count, P->total, P->counter,
+                   sh.cols_in_smem ? nullptr : P->cols, sh.rows_in_smem ? nullptr : P->rows,
                    P->cols_words, st));
   return CUSNA_OK;
 }
@@ -997,7 +1136,31 @@ cusna_status plan_launch(cusna_saom_plan *P, cudaStream_t st, bool graph) {
   int dev = -1;
   CU(cudaGetDevice(&dev));
   if (dev != P->device) { set_err("plan belongs to device %d, current is %d", P->device, dev); return CUSNA_ERR_UNSUPPORTED; }
-  if (!graph) return plan_enqueue(P, st);
+  // autotuning: the first launches are timed trials of the candidate shapes
+  // (never inside a stream capture); the fastest is kept, before any graph
+  if (P->pending) {
+    float ms = 0.f;
+    CU(cudaEventSynchronize(P->ev1));
+    CU(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
+    P->cand_ms[P->trial - 1] = ms;
+    P->pending = false;
+    size_t b = 0;
+    for (size_t x = 1; x < P->cand_ms.size(); ++x)
+      if (P->cand_ms[x] < P->cand_ms[b]) b = x;
+    P->sh = P->cand[b];
+  }
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  CU(cudaStreamIsCapturing(st, &cap_status));
+  if (P->trial < P->cand.size() && cap_status == cudaStreamCaptureStatusNone) {
+    const LaunchShape sh = P->cand[P->trial];
+    CU(cudaEventRecord(P->ev0, st));
+    const cusna_status s = plan_enqueue(P, sh, st);
+    CU(cudaEventRecord(P->ev1, st));
+    ++P->trial;
+    P->pending = s == CUSNA_OK;
+    return s;
+  }
+  if (!graph) return plan_enqueue(P, P->sh, st);
   if (!P->graph) {
     cudaStream_t cap = nullptr;
     CU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -1007,7 +1170,7 @@ cusna_status plan_launch(cusna_saom_plan *P, cudaStream_t st, bool graph) {
       set_err("plan: begin capture failed: %s", cudaGetErrorString(e));
       return CUSNA_ERR_CUDA;
     }
-    cusna_status s = plan_enqueue(P, cap);
+    cusna_status s = plan_enqueue(P, P->sh, cap);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(cap, &g);   // ends the capture on every path
     cudaStreamDestroy(cap);

@@ -269,19 +269,21 @@ __device__ __forceinline__ bool is_nan64(double x) {
   return ((b >> 52) & 0x7FF) == 0x7FF && (b & 0xFFFFFFFFFFFFFull) != 0;
 }
 
-// Team sums of sume and wsum[0..k-1] (float32): warp recursive halving over
-// V >= k+1 values, then one float64 slot per (quantity, warp) in
-// red[q*G + warp], summed across warps in float64 by the score update.
+// Sums of one block of 32 alters (one per lane): quantity 0 is the weight w
+// of the lane's alter, quantity 1+e its weight times d_e (0 for the "no change"
+// alter and for non-permitted alters); the fixed recursive-halving warp
+// reduction leaves quantity q's block sum on the lanes reporting q, which
+// store it in rec[q].
 template <int V>
-__device__ __forceinline__ void lse_reduce(const Team &T, const Slice &S, float sume,
-                                           const float *wsum, int k) {
+__device__ __forceinline__ void block_lse(float *rec, float w, const float *d32, bool weighted,
+                                          int k, int lane) {
   float v[V];
-  v[0] = sume;
+  v[0] = w;
 #pragma unroll
-  for (int q = 1; q < V; ++q) v[q] = (q - 1 < k) ? wsum[q - 1] : 0.f;
-  const int q = warp_multi_sum<V>(v, T.lane);
-  const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
-  if (writer && q <= k) S.red[q * T.G + T.warp] = (double)v[0];
+  for (int q = 1; q < V; ++q) v[q] = (weighted && q - 1 < k) ? __fmul_rn(w, d32[q - 1]) : 0.f;
+  const int q = warp_multi_sum<V>(v, lane);
+  const bool writer = (V >= 32) || ((lane & ((32 / V) - 1)) == 0);
+  if (writer && q <= k) rec[q] = v[0];
 }
 
 // One chain: the ministep loop and the chain's outputs.
@@ -298,7 +300,7 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
   long long dist = 0, bdist = 0, ms = 0, msb = 0;
   double t = 0.0, rho = 0.0;
   double d[24];
-  float d32[24], wsum[24];
+  float d32[24];
 
   for (;;) {
     int i;
@@ -362,43 +364,32 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
 
     // ---- one pass over the alters ------------------------------------------
     // Lane by lane, alters in ascending j: integer change statistics, the
-    // float32 predictor f32_j (change_stats32), the float32 Gumbel key
+    // float32 predictor f32_j (change_stats32) and the float32 Gumbel key
     // g_j = f32_j - loglog_est(u_j) with u_j from the reference's counters
-    // (msteps, chain, 1, j), and an online log-sum-exp (a running maximum m,
-    // the weight sums rescaled when it rises). The key is within
+    // (msteps, chain, 1, j). The key is within
     //   E_j = (k + 10) 2^-24 absf_j + 6e-6
     // of the float64 key f_j - log(-log u_j): (k + 8) u absf_j for f32_j, 4e-6
     // for loglog_est and u (absf_j + 23) for the subtraction (|f32_j| <= absf_j,
     // |log(-log u)| < 23). gbuf[j] keeps the upper bound g_j + E_j.
-    float m = -INFINITY, sume = 0.f;
-    for (int e = 0; e < k; ++e) wsum[e] = 0.f;
+    // The log-sum-exp sums are formed per block of 32 alters (alter j on lane
+    // j mod 32, whatever the team size): the block maximum and the block's
+    // sums of exp(f - max) and exp(f - max) d_e with a fixed warp reduction,
+    // stored per block and combined in block order after the pass, so the
+    // scores do not depend on the launch shape.
     KeyTop best{-INFINITY, 0.f, -INFINITY, 0x7FFFFFFF};
     const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
     for (int jb = 32 * T.warp; jb < n; jb += L) {
       const int j = jb + T.lane;
-      bool ok = false;
+      bool ok = false, stay = false;
+      float f = 0.f;
       if (j < n) {
         const int aij = bit_of(S.rowsT, n, i, j);
         float ub = -INFINITY;
-        ok = (j == i) || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
+        stay = j == i;
+        ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
         if (ok) {
-          float f = 0.f, absf = 0.f;
-          const bool stay = j == i;
+          float absf = 0.f;
           if (!stay) f = change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
-          // a NaN predictor turns the sums into NaN, as exp(NaN - lmax) does
-          // in the reference, and never wins the choice (its key compares false)
-          if (f > m) {
-            const float r = expf(__fsub_rn(m, f));   // 0 while m = -inf
-            sume = __fadd_rn(__fmul_rn(sume, r), 1.f);
-            for (int e = 0; e < k; ++e)
-              wsum[e] = __fadd_rn(__fmul_rn(wsum[e], r), stay ? 0.f : d32[e]);
-            m = f;
-          } else {
-            const float w = expf(__fsub_rn(f, m));
-            sume = __fadd_rn(sume, w);
-            if (!stay)
-              for (int e = 0; e < k; ++e) wsum[e] = __fadd_rn(wsum[e], __fmul_rn(w, d32[e]));
-          }
           uint32_t ph[4];
           philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
           const float g = __fsub_rn(f, loglog_est(ph[0]));
@@ -410,18 +401,31 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
       }
       const uint32_t okb = __ballot_sync(kFull, ok);
       if (T.lane == 0) S.okbits[jb >> 5] = okb;
-    }
-    // log-sum-exp sums: each lane rescaled to the team maximum, then summed
-    {
-      const float M = team_max_f(T, m, S.red);
-      const float r = (m == M) ? 1.f : expf(__fsub_rn(m, M));
-      sume = __fmul_rn(sume, r);
-      for (int e = 0; e < k; ++e) wsum[e] = __fmul_rn(wsum[e], r);
+      // a NaN predictor turns the sums into NaN, as exp(NaN - lmax) does in
+      // the reference, and never wins the choice (its key compares false)
+      const float mb = warp_max_f(ok ? f : -INFINITY);
+      const float w = ok ? expf(__fsub_rn(f, mb)) : 0.f;
+      float *rec = S.blk + (size_t)(jb >> 5) * (k + 2);
+      if (T.lane == 0) rec[0] = mb;
+      if (k + 1 <= 8) block_lse<8>(rec + 1, w, d32, ok && !stay, k, T.lane);
+      else if (k + 1 <= 16) block_lse<16>(rec + 1, w, d32, ok && !stay, k, T.lane);
+      else block_lse<32>(rec + 1, w, d32, ok && !stay, k, T.lane);
     }
     T.sync();
-    if (k + 1 <= 8) lse_reduce<8>(T, S, sume, wsum, k);
-    else if (k + 1 <= 16) lse_reduce<16>(T, S, sume, wsum, k);
-    else lse_reduce<32>(T, S, sume, wsum, k);
+    // blocks combined in order: lane q <= k forms quantity q (0: sum of
+    // weights, 1+e: weighted sum of d_e) rescaled to the overall maximum
+    if (T.tl <= k) {
+      const int nb = (n + 31) >> 5, q = T.tl;
+      float M = -INFINITY;
+      for (int b = 0; b < nb; ++b) M = fmaxf(M, S.blk[(size_t)b * (k + 2)]);
+      double acc = 0.0;
+      for (int b = 0; b < nb; ++b) {
+        const float *rec = S.blk + (size_t)b * (k + 2);
+        const float r = rec[0] == M ? 1.f : expf(__fsub_rn(rec[0], M));
+        acc = __dadd_rn(acc, (double)__fmul_rn(rec[1 + q], r));
+      }
+      S.red[32 * T.G + q] = acc;   // past the warp slots the reductions below use
+    }
     const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
 
     // ---- the chosen alter ---------------------------------------------------
@@ -470,11 +474,7 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
     T.sync();
     if (T.tl < k) {
       const int e = T.tl;
-      double s0 = 0.0, se = 0.0;
-      for (int w = 0; w < T.G; ++w) {
-        s0 = __dadd_rn(s0, S.red[w]);
-        se = __dadd_rn(se, S.red[(e + 1) * T.G + w]);
-      }
+      const double s0 = S.red[32 * T.G], se = S.red[32 * T.G + 1 + e];
       S.sc[e] = __dadd_rn(S.sc[e], __dsub_rn(S.dstar[e], __ddiv_rn(se, s0)));
     }
     ++ms;

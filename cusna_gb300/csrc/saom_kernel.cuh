@@ -38,12 +38,13 @@ struct Slice {
   short *indeg, *outdeg;  // n each (degrees < 2^15 as n <= 8192)
   int *z;
   float *gbuf;       // n   upper bounds of the float32 Gumbel keys
+  float *blk;        // ceil(n/32)*(k+2)  per 32-alter block: max and log-sum-exp sums
   uint32_t *okbits;  // W
   int *tp;           // n   (transTies / gwdsp)
   int *tq;           // n   (gwdspFB)
   uint32_t *tpeq;    // 2W  (transTies masks tp==0, tp==1)
   double *crate;     // n   (non-basic rates)
-  double *red;       // 32*G reduction scratch
+  double *red;       // 32*G + 32 reduction scratch
   double *th;        // k  parameters of the current chain
   float *th32;       // k  the same parameters (they are float32 inputs)
   double *sc;        // k  scores
@@ -63,7 +64,7 @@ struct Slice {
 
 struct SliceLayout {
   size_t bytes;  // per team
-  size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_g, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
+  size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_g, o_blk, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
       o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc, o_rtau, o_rnet, o_rfocal, o_rr3, o_ekind, o_ecfn, o_eoffd, o_eofft,
       o_stepd, o_stept, o_th32, o_stepd32, o_stept32;
 };
@@ -83,12 +84,13 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_outdeg, (size_t)n * 2);
   put(s.o_z, (size_t)n * 4);
   put(s.o_g, (size_t)n * 4);
+  put(s.o_blk, (size_t)((n + 31) / 32) * (k + 2) * 4);
   put(s.o_ok, (size_t)W * 4);
   put(s.o_tp, need_tp || need_gw ? (size_t)n * 4 : 0);
   put(s.o_tq, need_tq ? (size_t)n * 4 : 0);
   put(s.o_tpeq, need_tp ? (size_t)W * 8 : 0);
   put(s.o_crate, nrate > 0 ? (size_t)n * 8 : 0);
-  put(s.o_red, (size_t)32 * G * 8 + 64);
+  put(s.o_red, (size_t)32 * G * 8 + 32 * 8);   // 32 slots per warp, then 32 team values
   put(s.o_th, (size_t)k * 8);
   put(s.o_sc, (size_t)k * 8);
   put(s.o_dstar, (size_t)k * 8);
@@ -132,6 +134,7 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   s.outdeg = (short *)(base + L.o_outdeg);
   s.z = (int *)(base + L.o_z);
   s.gbuf = (float *)(base + L.o_g);
+  s.blk = (float *)(base + L.o_blk);
   s.okbits = (uint32_t *)(base + L.o_ok);
   s.tp = (int *)(base + L.o_tp);
   s.tq = (int *)(base + L.o_tq);
