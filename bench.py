@@ -68,12 +68,58 @@ def workload(name, M):
     return inp, M, seed, lam, theta, lamb, thetab
 
 
-def fp64_flops_per_network_ministep(n, k):
-    """Algorithmic float64 work of one network ministep: per alter, the linear
+def flops_per_network_ministep(n, k):
+    """Algorithmic arithmetic of one network ministep: per alter, the linear
     predictor (k multiplies + k adds), the log-sum-exp shift, exponential and
     sum (1 + 10 + 1, an exponential counted as 10 flops) and the k weighted
-    score sums (k FMAs = 2k flops)."""
+    score sums (2k). The kernel does it in float32 (float64 only for the
+    chosen alter and for uncertified choices)."""
     return n * (4 * k + 12)
+
+
+def smem_bytes_per_network_ministep(n, W):
+    """Algorithmic on-chip traffic of one network ministep of the bench
+    workloads (transTrip and cycle3 present): per alter, the three popcounts
+    of W-word bit rows/columns (row_i & col_j, row_i & row_j, row_j & col_i,
+    4 bytes per word read for j) and the scalar reads (in-degree 4 B, the
+    alter's covariate value 8 B)."""
+    return (n - 1) * (4 * 3 * W + 12)
+
+
+# Warp-instructions the period kernel executes per network ministep, from the
+# ncu capture of the kernel on each workload (smsp__inst_executed.sum over the
+# launch's network ministeps): n=200, k=8, 1024 chains.
+INST_PER_MINISTEP = {"c2": 11400.0}
+
+
+def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk):
+    """The period kernel is latency-bound: its state is on chip (DRAM moves only
+    the problem and the outputs) and no pipe is busier than a quarter of its
+    peak, so its ceiling is the SMs' instruction issue rate (4 warp-instructions
+    per cycle per SM). achieved = network ministeps per second of kernel time
+    times the warp-instructions a ministep executes; peak = 4 x SMs x the SM
+    clock sampled under load. The algorithmic shared-memory and arithmetic
+    rates are reported beside it against their own ceilings."""
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    hz = mhz * 1e6
+    rate = net_steps / (kernel_ms / 1e3)
+    ipm = INST_PER_MINISTEP.get(workload)
+    peak = 4.0 * sm_count * hz / 1e9
+    achieved = rate * ipm / 1e9 if ipm else None
+    smem_peak = 128.0 * sm_count * hz / 1e12          # TB/s, 128 B per cycle per SM
+    fp32_peak = 256.0 * sm_count * hz / 1e12          # TFLOP/s, 128 FMA per cycle per SM
+    smem = smem_bytes_per_network_ministep(n, W) * rate / 1e12
+    flops = flops_per_network_ministep(n, k) * rate / 1e12
+    return {"bound": "issue", "achieved": achieved, "peak": peak,
+            "unit": "G warp-instructions/s", "frac": achieved / peak if achieved else None,
+            "traffic": None, "kernel_ms": kernel_ms, "network_ministeps_per_s": rate,
+            "inst_per_ministep": ipm, "sm_mhz": mhz,
+            "peak_source": "4 warp-instructions per cycle per SM x SMs x sampled SM clock",
+            "algorithmic": {
+                "smem_bytes_per_ministep": smem_bytes_per_network_ministep(n, W),
+                "smem_TBps": smem, "smem_peak_TBps": smem_peak, "smem_frac": smem / smem_peak,
+                "flops_per_ministep": flops_per_network_ministep(n, k),
+                "fp32_TFLOPs": flops, "fp32_peak_TFLOPs": fp32_peak, "fp32_frac": flops / fp32_peak}}
 
 
 class Clocks:
@@ -401,27 +447,16 @@ def main():
             torch.distributed.destroy_process_group()
         return
 
-    # ---- float64 roofline of the period kernel ---------------------------
-    fp64_peak = C.c_double(0.0)
-    lib.cusna_measure_fp64_tflops(C.byref(fp64_peak))
+    # ---- network ministeps of a launch (behaviour ministeps visit no alters) ----
     net_steps = ministeps
     if inp.kb > 0:
-        # behaviour ministeps do no per-alter work; count network ministeps only
         m_h = marshal_period(inp, min(M, 64), seed, lam, theta, lamb=lamb, thetab=thetab)
         r_h = G.simulate(m_h)
         tot = r_h["steps"].sum()
         # behaviour ministeps from the behaviour rate score: msb = (score + nact) * lamb
         beh = np.round((r_h["bscores"][:, 0].astype(np.float64) + inp.n) * lamb)
         net_steps = int(ministeps * (1.0 - float(beh.sum()) / float(tot)))
-    flops = fp64_flops_per_network_ministep(n, k) * net_steps
     kern_avg_ms = float(np.mean(kernel_ms))
-    achieved = flops / (kern_avg_ms / 1e3) / 1e12
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak.value,
-                "unit": "TFLOP/s", "frac": achieved / fp64_peak.value if fp64_peak.value else None,
-                "traffic": None,
-                "peak_source": "measured in this run: float64 FMA loop (cusna_measure_fp64_tflops)",
-                "algorithmic_flops_per_launch": flops,
-                "kernel_ms": kern_avg_ms}
 
     # ---- end to end through the reference-facing C ABI ---------------------
     e2e = None
@@ -463,6 +498,8 @@ def main():
             mom_fit = {"error": f"{type(exc).__name__}: {exc}"}
 
     clk = clocks.summary(local)
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    roofline = period_roofline(args.workload, n, inp.W, k, net_steps, kern_avg_ms, sm_count, clk)
     line = {
         "metric": "ministeps/s", "value": value, "unit": "ministeps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
