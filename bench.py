@@ -376,6 +376,7 @@ def main():
     from cusna_gb300 import build as B
     from cusna_gb300 import sim as G
     from cusna_gb300.abi import load_library
+    from cusna_gb300.replicas import chain_range, reduce_timing
 
     ws, rank, local = dist_info()
     if ws > 1:
@@ -387,6 +388,7 @@ def main():
     lib = load_library()
 
     inp, M, seed, lam, theta, lamb, thetab = workload(args.workload, args.chains)
+    off, _ = chain_range(rank, ws, M)
     n, k = inp.n, inp.k
     # device-resident inputs and outputs
     m_dev = marshal_period(inp, M, seed, lam, theta, lamb=lamb, thetab=thetab)
@@ -404,9 +406,9 @@ def main():
     # the library's autotuner times one candidate launch shape per call until it
     # settles (results do not depend on the shape); these calls are untimed
     for _ in range(10):
-        step(G.options(device_ptrs=True, chain_offset=rank * M, stream=stream.cuda_stream))
+        step(G.options(device_ptrs=True, chain_offset=off, stream=stream.cuda_stream))
     for _ in range(args.warmup):
-        step(G.options(device_ptrs=True, chain_offset=rank * M, stream=stream.cuda_stream))
+        step(G.options(device_ptrs=True, chain_offset=off, stream=stream.cuda_stream))
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -418,7 +420,7 @@ def main():
         t_wall0 = time.perf_counter()
         for s in range(args.steps):
             flush.zero_()
-            o = G.options(device_ptrs=True, chain_offset=rank * M, stream=stream.cuda_stream)
+            o = G.options(device_ptrs=True, chain_offset=off, stream=stream.cuda_stream)
             ev[s][0].record(stream)
             step(o)
             ev[s][1].record(stream)
@@ -432,14 +434,7 @@ def main():
     ministeps = int(steps_out.sum())           # identical every step (fixed seed)
     msb_frac = 0.0
     total_ms = float(sum(step_ms))
-    if ws > 1:
-        t = torch.tensor([total_ms, float(ministeps)], device=dev, dtype=torch.float64)
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        total_ms, all_ministeps = float(tmax[0]), float(t[1])
-    else:
-        all_ministeps = float(ministeps)
+    total_ms, all_ministeps = reduce_timing(total_ms, ministeps, dev)
     value = all_ministeps * args.steps / (total_ms / 1e3)
 
     if rank != 0:
