@@ -360,7 +360,7 @@ class Stage:
     epochs: int = 40
 
 
-DEFAULT_STAGES = (Stage(0.25, "iso", 0.5, 80), Stage(0.75, "se", 2.0, 100))
+DEFAULT_STAGES = (Stage(0.25, "iso", 0.5, 60), Stage(0.75, "se", 2.0, 30))
 
 
 @dataclass
