@@ -63,6 +63,26 @@ class SaomResult(C.Structure):
     ]
 
 
+class MultiProblem(C.Structure):
+    """cusna_saom_multi_problem (src/libcusna.h:238-267)."""
+    _fields_ = [
+        ("struct_version", C.c_int32), ("n", C.c_int32), ("W", C.c_int32), ("k", C.c_int32),
+        ("M", C.c_int32), ("D", C.c_int32), ("threads", C.c_int32),
+        ("x0_out", _p), ("x0_in", _p), ("lam", _p), ("theta", _p),
+        ("type_ids", _p), ("etypes", _p), ("netof", _p), ("netref", _p),
+        ("wtab", _p), ("p1", _p), ("p2", _p), ("vmat", _p), ("dyc", _p), ("dyc_idx", _p),
+        ("perm", _p), ("symf", _p), ("seed", C.c_uint64), ("act", _p), ("nact", C.c_int32),
+    ]
+
+
+class MultiResult(C.Structure):
+    """cusna_saom_multi_result (src/libcusna.h:271-278)."""
+    _fields_ = [
+        ("struct_version", C.c_int32), ("rscores", _p), ("scores", _p), ("ntim", _p),
+        ("steps", _p), ("a_ends", _p),
+    ]
+
+
 class GpuOptions(C.Structure):
     """cusna_gpu_options (extension, include/libcusna.h)."""
     _fields_ = [
@@ -149,6 +169,10 @@ def load_library(path: str | None = None):
     lib.cusna_mlp_train_steps.restype = i32
     lib.cusna_mlp_jacobian.argtypes = [_p, _p, i32, i32, _p, _p, _p, sz, i32, i32, i32, _p]
     lib.cusna_mlp_jacobian.restype = i32
+    lib.cusna_saom_simulate_multi.argtypes = [P(MultiProblem), P(MultiResult)]
+    lib.cusna_saom_simulate_multi.restype = i32
+    lib.cusna_cross_stats.argtypes = [_p, _p, i32, i32, i32, C.c_double, _p]
+    lib.cusna_cross_stats.restype = i32
     if path is None:
         _lib = lib
     return lib
@@ -165,6 +189,7 @@ EXPORTED_SYMBOLS = [
     "cusna_saom_plan_shape", "cusna_saom_plan_destroy",
     "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",
     "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_train_steps", "cusna_mlp_jacobian",
+    "cusna_saom_simulate_multi", "cusna_cross_stats",
 ]
 
 # cusna_adam_hyper: int32 step, float lr, beta1, beta2, eps, c1, c2

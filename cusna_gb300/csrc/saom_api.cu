@@ -115,6 +115,11 @@ struct Facts {
   int flags = 0;
   std::vector<int> kind, cfn, offd, offt;  // effect plan, k each
   std::vector<int> tsize;                  // theta-table length per effect (0: none)
+  // multi-network problems: one network's effects as a problem of their own
+  bool multi = false;
+  std::vector<int> cross_src;              // source network per effect (cross effects)
+  std::vector<int> dci;                    // dyadic covariate index per effect (-1 none)
+  std::vector<double> dyc;                 // the dyadic covariate, n*n (empty: none)
   std::vector<double> pool;                // its tables
   int zlo = 0, zR = 1;
 };
@@ -254,12 +259,31 @@ cusna_status build_plan(const cusna_saom_problem *p, bool dev, Facts &F, bool on
         }
         break;
       }
-      case 22: F.kind[e] = K_ZERO; break;
+      case 22:
+        // a dyadic covariate: the multi-network engine reads it
+        // (src/libcusna_saom_cpu.cpp:509), the single-network one zero-fills
+        if (F.multi && !F.dyc.empty() && F.dci[e] == 0)
+          look_table(e, 14, N * N, [&](size_t x) { return F.dyc[x]; });
+        else
+          F.kind[e] = K_ZERO;
+        break;
+      case 33: case 34: case 35: case 36: case 37:
+        // cross-network effects read another network of a multi-network
+        // problem; a single-network problem has none, and the reference's
+        // change statistic of these types there is 0
+        if (F.multi) { F.kind[e] = K_CROSS; F.cfn[e] = t; F.offd[e] = F.cross_src[e]; }
+        else F.kind[e] = K_ZERO;
+        break;
       case 24: look_table(e, 8, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
       case 26: look_table(e, 9, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
       case 27: look_table(e, 10, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
       case 28: look_table(e, 11, N + 1, [&](size_t c) { return wt[(size_t)e * (n + 1) + c]; }); break;
-      case 13: case 29: case 30: case 32: break;  // K_GEN
+      case 32:
+        // interactions are formed from their components in the single-network
+        // engine; the multi-network change statistic of the type is 0
+        if (F.multi) F.kind[e] = K_ZERO;
+        break;
+      case 13: case 29: case 30: break;  // K_GEN
       default: F.kind[e] = K_ZERO; break;       // unknown ids: the reference's 0
     }
   }
@@ -325,7 +349,11 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
       case 3: case 23: fl |= F_PC_RJ_CI; break;
       case 5: fl |= F_NEED_TP; break;
       case 6: fl |= F_PC_RI_CJ | F_PC_RICIRJ; break;
-      case 19: fl |= F_NEED_RDEG; break;
+      case 19:
+        // the multi-network engine passes a reciprocated degree of 0
+        // (src/libcusna_saom_cpu.cpp:510)
+        if (!F.multi) fl |= F_NEED_RDEG;
+        break;
       case 24: fl |= F_PC_RI_CJ; break;
       case 26: fl |= F_PC_RI_RJ; break;
       case 27: fl |= F_PC_CI_CJ; break;
@@ -333,6 +361,7 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
       case 29: fl |= F_NEED_GW29; break;
       case 30: fl |= F_NEED_GW30; break;
       case 32:
+        if (F.multi) break;
         fl |= F_HAS_INTER;
         if (F.i0[e] < 0 || F.i0[e] >= e || F.i1[e] < 0 || F.i1[e] >= e || F.i2[e] >= e) {
           set_err("interaction %d: components must be earlier effects", e);
@@ -677,7 +706,7 @@ cusna_status fetch_outputs(Job &J) {
 // smaller teams (fewer barriers) and to in-rows in shared memory.
 std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp,
                                      bool gw, bool tq, long long total_units, int force_G,
-                                     int force_tpc) {
+                                     int force_tpc, int nets = 1) {
   const Ctx &c = g_ctx;
   std::vector<std::pair<double, LaunchShape>> all;
   const int Gs[5] = {1, 2, 4, 8, 16};
@@ -692,15 +721,16 @@ std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, in
       sh.cols_in_smem = cols_smem;
       sh.rows_in_smem = rows_smem;
       sh.lay = make_layout(nmax, Wmax, kmax, kbmax, nrmax, G, rows_smem, cols_smem, tp, gw, tq);
-      if (sh.lay.bytes > (size_t)c.smem_optin) continue;
+      if (sh.lay.bytes * nets > (size_t)c.smem_optin) continue;
       bool any = false;
       for (int tpc = 1; tpc <= 16; tpc *= 2) {
         if (force_tpc && tpc != force_tpc) continue;
         const int threads = 32 * G * tpc;
         if (threads > 512 || (G > 1 && tpc > 15)) continue;
-        const size_t dyn = sh.lay.bytes * tpc;
+        const size_t dyn = sh.lay.bytes * nets * tpc;
         if (dyn > (size_t)c.smem_optin) continue;
-        const int per_sm = period_blocks_per_sm(threads, dyn);
+        const int per_sm = nets > 1 ? multi_blocks_per_sm(threads, dyn)
+                                    : period_blocks_per_sm(threads, dyn);
         if (per_sm < 1) continue;
         const double teams_sm = (double)per_sm * tpc;
         const double chains_sm = (double)total_units / c.sms;
@@ -942,6 +972,182 @@ double chain_cost(const cusna_saom_problem *p) {
 void order_longest_first(std::vector<Job> &jobs) {
   std::stable_sort(jobs.begin(), jobs.end(),
                    [](const Job &a, const Job &b) { return chain_cost(a.p) > chain_cost(b.p); });
+}
+
+// ---- multi-network periods (src/libcusna_saom_cpu.cpp:427-604) ----------------
+// Each network's effects become a single-network problem of their own (its
+// start network, permitted dyads, effect plan and tables), checked and
+// prepared by the single-network code; the multi kernel gives a team one
+// slice per network and picks the network of each ministep.
+struct MultiNet {
+  cusna_saom_problem q;
+  cusna_saom_result r;
+  std::vector<int> eidx;  // the network's effects, in the caller's order
+  std::vector<int> tid, ety;
+  std::vector<float> th, lam, p1, p2, vm, wt;
+};
+
+cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi_result *r) {
+  if (!pb || !r) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
+  if (pb->struct_version != CUSNA_ABI_VERSION || r->struct_version != CUSNA_ABI_VERSION) {
+    set_err("struct_version %d/%d != %d", pb->struct_version, r->struct_version, CUSNA_ABI_VERSION);
+    return CUSNA_ERR_SHAPE;
+  }
+  const int n = pb->n, W = pb->W, k = pb->k, M = pb->M, D = pb->D;
+  if (n < 1 || n > CUSNA_MAX_N || W != (n + 31) / 32 || k < 1 || k > CUSNA_MAXEFF || M < 1 ||
+      D < 2 || D > CUSNA_MAXNET) {
+    set_err("bad shape n=%d W=%d k=%d M=%d D=%d", n, W, k, M, D);
+    return CUSNA_ERR_SHAPE;
+  }
+  if (!pb->x0_out || !pb->lam || !pb->theta || !pb->type_ids || !pb->netof) {
+    set_err("x0_out, lam, theta, type_ids and netof are required");
+    return CUSNA_ERR_NULL_ARG;
+  }
+  if (pb->act) {
+    if (pb->nact < 1 || pb->nact > n) { set_err("nact %d out of range", pb->nact); return CUSNA_ERR_SHAPE; }
+    for (int x = 0; x < pb->nact; ++x)
+      if (pb->act[x] < 0 || pb->act[x] >= n) { set_err("act entry %d out of range", pb->act[x]); return CUSNA_ERR_SHAPE; }
+  }
+  std::vector<MultiNet> nets(D);
+  std::vector<int> gidx, goff(D + 1, 0);
+  bool any_dyc = false;
+  for (int e = 0; e < k; ++e) {
+    const int d = pb->netof[e], t = pb->type_ids[e];
+    if (d < 0 || d >= D) { set_err("netof[%d] = %d out of range", e, d); return CUSNA_ERR_SHAPE; }
+    if (t >= 33 && t <= 37) {
+      const int w = pb->netref ? pb->netref[e] : 0;
+      if (w < 0 || w >= D) { set_err("netref[%d] = %d out of range", e, w); return CUSNA_ERR_SHAPE; }
+    }
+    const int dci = pb->dyc_idx ? pb->dyc_idx[e] : -1;
+    // one dyadic covariate matrix: the reference indexes dyc[(idx*n + i)*n + j]
+    // within an n*n copy
+    if (dci < -1 || dci > 0) { set_err("dyc_idx[%d] = %d: one dyadic covariate", e, dci); return CUSNA_ERR_SHAPE; }
+    if (dci == 0 && !pb->dyc) { set_err("dyc_idx[%d] = 0 without dyc", e); return CUSNA_ERR_NULL_ARG; }
+    any_dyc |= dci == 0 && t == 22;
+    nets[d].eidx.push_back(e);
+  }
+  std::vector<double> dyc;
+  if (any_dyc) {
+    dyc.resize((size_t)n * n);
+    for (size_t x = 0; x < dyc.size(); ++x) dyc[x] = (double)pb->dyc[x];
+  }
+  std::vector<Job> jobs(D);
+  int kmax = 0;
+  bool tp = false, gw = false, tq = false;
+  for (int d = 0; d < D; ++d) {
+    MultiNet &N = nets[d];
+    goff[d + 1] = goff[d] + (int)N.eidx.size();
+    for (int e : N.eidx) gidx.push_back(e);
+    // a network without effects chooses uniformly: one zero effect stands in
+    const bool empty = N.eidx.empty();
+    const int kd = empty ? 1 : (int)N.eidx.size();
+    N.tid.assign(kd, 22); N.ety.assign(kd, 0);
+    N.p1.assign(kd, 0.f); N.p2.assign(kd, 0.f);
+    N.vm.assign((size_t)kd * n, 0.f); N.wt.assign((size_t)kd * (n + 1), 0.f);
+    N.th.assign((size_t)M * kd, 0.f); N.lam.resize(M);
+    Facts &F = jobs[d].F;
+    F.multi = true;
+    F.cross_src.assign(kd, 0);
+    F.dci.assign(kd, -1);
+    for (int q = 0; q < (int)N.eidx.size(); ++q) {
+      const int e = N.eidx[q];
+      N.tid[q] = pb->type_ids[e];
+      N.ety[q] = pb->etypes ? pb->etypes[e] : 0;
+      N.p1[q] = pb->p1 ? pb->p1[e] : 0.f;
+      N.p2[q] = pb->p2 ? pb->p2[e] : 0.f;
+      if (pb->vmat) std::memcpy(&N.vm[(size_t)q * n], pb->vmat + (size_t)e * n, (size_t)n * 4);
+      if (pb->wtab)
+        std::memcpy(&N.wt[(size_t)q * (n + 1)], pb->wtab + (size_t)e * (n + 1), (size_t)(n + 1) * 4);
+      for (int c = 0; c < M; ++c) N.th[(size_t)c * kd + q] = pb->theta[(size_t)c * k + e];
+      F.cross_src[q] = pb->netref ? pb->netref[e] : 0;
+      F.dci[q] = pb->dyc_idx ? pb->dyc_idx[e] : -1;
+    }
+    for (int c = 0; c < M; ++c) N.lam[c] = pb->lam[(size_t)c * D + d];
+    if (any_dyc) F.dyc = dyc;
+    cusna_saom_problem &q = N.q;
+    std::memset(&q, 0, sizeof q);
+    q.struct_version = CUSNA_ABI_VERSION;
+    q.n = n; q.W = W; q.k = kd; q.M = M;
+    q.x0_out = pb->x0_out + (size_t)d * n * W;
+    q.perm = pb->perm ? pb->perm + (size_t)d * n * W : nullptr;
+    q.lam = N.lam.data(); q.theta = N.th.data();
+    q.type_ids = N.tid.data(); q.etypes = N.ety.data();
+    q.p1 = N.p1.data(); q.p2 = N.p2.data(); q.vmat = N.vm.data(); q.wtab = N.wt.data();
+    q.symflag = pb->symf ? pb->symf[d] : 0;
+    q.seed = pb->seed;
+    q.act = pb->act; q.nact = pb->act ? pb->nact : n;
+    std::memset(&N.r, 0, sizeof N.r);
+    N.r.struct_version = CUSNA_ABI_VERSION;
+    jobs[d].p = &N.q;
+    jobs[d].r = &N.r;
+    cusna_status s = validate(&N.q, &N.r, false, F);
+    if (s != CUSNA_OK) return s;
+    kmax = std::max(kmax, kd);
+    tp |= (F.flags & F_NEED_TP) != 0;
+    gw |= (F.flags & (F_NEED_GW29 | F_NEED_TP)) != 0;
+    tq |= (F.flags & F_NEED_GW30) != 0;
+  }
+  cusna_status s;
+  if ((s = ensure_ctx()) != CUSNA_OK) return s;
+  cudaStream_t st = g_ctx.stream;
+  const std::vector<LaunchShape> ranked = rank_shapes(n, W, kmax, 0, 0, tp, gw, tq, M, 0, 0, D);
+  if (ranked.empty()) {
+    set_err("no launch shape fits %d networks of n=%d", D, n);
+    return CUSNA_ERR_UNSUPPORTED;
+  }
+  const LaunchShape sh = ranked[0];
+  Planner pl;
+  for (auto &J : jobs) plan_problem(pl, J, false);
+  const size_t o_probs = pl.take(sizeof(DevProblem) * D);
+  const size_t o_counter = pl.take(sizeof(unsigned long long));
+  const size_t o_lam = pl.take((size_t)M * D * 4);
+  const size_t o_gidx = pl.take((size_t)k * 4);
+  const size_t o_rs = r->rscores ? pl.take((size_t)M * D * 4) : NONE;
+  const size_t o_sc = r->scores ? pl.take((size_t)M * k * 4) : NONE;
+  const size_t o_nt = r->ntim ? pl.take((size_t)M * 8) : NONE;
+  const size_t o_st = r->steps ? pl.take((size_t)M * 4) : NONE;
+  const size_t o_ae = r->a_ends ? pl.take((size_t)M * D * n * n) : NONE;
+  const size_t teams = (size_t)sh.ctas * sh.teams_per_cta;
+  const size_t cols_words = (size_t)W * n;
+  const size_t o_cols = sh.cols_in_smem ? NONE : pl.take(teams * D * cols_words * 4);
+  const size_t o_rows = sh.rows_in_smem ? NONE : pl.take(teams * D * cols_words * 4);
+  if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
+  std::vector<DevProblem> hp(D);
+  for (int d = 0; d < D; ++d)
+    if ((s = prepare(jobs[d], false, hp[d], 0)) != CUSNA_OK) return s;
+  MultiDev md{};
+  md.D = D; md.n = n; md.W = W; md.k = k;
+  md.nact = pb->act ? pb->nact : n;
+  md.act = hp[0].act;
+  md.lam = at<float>(o_lam);
+  md.k0 = (uint32_t)(pb->seed & 0xFFFFFFFFu);
+  md.k1 = (uint32_t)(pb->seed >> 32);
+  for (int d = 0; d <= D; ++d) md.goff[d] = goff[d];
+  md.gidx = at<int>(o_gidx);
+  md.rscores = o_rs == NONE ? nullptr : at<float>(o_rs);
+  md.scores = o_sc == NONE ? nullptr : at<float>(o_sc);
+  md.ntim = o_nt == NONE ? nullptr : at<double>(o_nt);
+  md.steps = o_st == NONE ? nullptr : at<int>(o_st);
+  md.a_ends = o_ae == NONE ? nullptr : at<uint8_t>(o_ae);
+  CU(cudaMemcpyAsync(at<char>(o_probs), hp.data(), sizeof(DevProblem) * D, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(o_lam), pb->lam, (size_t)M * D * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(o_gidx), gidx.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
+  CU(cudaMemsetAsync(at<char>(o_counter), 0, sizeof(unsigned long long), st));
+  CU(launch_multi(sh, at<DevProblem>(o_probs), md, M, at<unsigned long long>(o_counter),
+                  o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
+                  o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
+  auto get = [&](void *dst, size_t off, size_t bytes) -> cusna_status {
+    if (!dst || off == NONE) return CUSNA_OK;
+    CU(cudaMemcpyAsync(dst, at<char>(off), bytes, cudaMemcpyDeviceToHost, st));
+    return CUSNA_OK;
+  };
+  if ((s = get(r->rscores, o_rs, (size_t)M * D * 4)) != CUSNA_OK) return s;
+  if ((s = get(r->scores, o_sc, (size_t)M * k * 4)) != CUSNA_OK) return s;
+  if ((s = get(r->ntim, o_nt, (size_t)M * 8)) != CUSNA_OK) return s;
+  if ((s = get(r->steps, o_st, (size_t)M * 4)) != CUSNA_OK) return s;
+  if ((s = get(r->a_ends, o_ae, (size_t)M * D * n * n)) != CUSNA_OK) return s;
+  CU(cudaStreamSynchronize(st));
+  return CUSNA_OK;
 }
 
 }  // namespace
@@ -1224,6 +1430,12 @@ CUSNA_API cusna_status cusna_saom_simulate_batch(const cusna_saom_problem *probl
   return simulate(problems, results, count, opts);
 }
 
+CUSNA_API cusna_status cusna_saom_simulate_multi(const cusna_saom_multi_problem *problem,
+                                                 cusna_saom_multi_result *result) {
+  g_err.clear();
+  return simulate_multi(problem, result);
+}
+
 CUSNA_API cusna_status cusna_saom_plan_create(const cusna_saom_problem *problems,
                                              cusna_saom_result *results, int32_t count,
                                              int32_t shared_params, cusna_saom_plan **plan) {
@@ -1337,6 +1549,35 @@ CUSNA_API cusna_status cusna_network_stats_gpu(
   D.n = n; D.W = (n + 31) / 32; D.k = k; D.symflag = symflag;
   CU(launch_netstats(at<uint8_t>(oa), M, D, at<double>(oout), g_ctx.sms, st));
   CU(cudaMemcpyAsync(out, at<char>(oout), (size_t)M * k * 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_cross_stats(const uint8_t *a_batch, const uint8_t *wp, int32_t n,
+                                         int32_t M, int32_t t, double parm, double *out) {
+  g_err.clear();
+  // the reference reports every argument error as a NULL argument
+  // (src/libcusna_saom_cpu.cpp:823-824) and an unknown type as unsupported
+  if (!a_batch || !wp || !out || n < 1 || n > CUSNA_MAX_N || M < 1) {
+    set_err("a_batch, wp and out are required; 1 <= n <= %d, M >= 1", CUSNA_MAX_N);
+    return CUSNA_ERR_NULL_ARG;
+  }
+  if (t < 33 || t > 37) { set_err("cross effect type %d", t); return CUSNA_ERR_UNSUPPORTED; }
+  cusna_status s = ensure_ctx();
+  if (s != CUSNA_OK) return s;
+  cudaStream_t st = g_ctx.stream;
+  const size_t nn = (size_t)n * n, W = (size_t)(n + 31) / 32;
+  Planner pl;
+  const size_t oa = pl.take(nn * M), ow = pl.take(nn), oout = pl.take((size_t)M * 8);
+  const size_t oar = t == 37 ? pl.take((size_t)M * n * W * 4) : NONE;
+  const size_t owr = t == 36 ? pl.take((size_t)n * W * 4) : NONE;
+  if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
+  CU(cudaMemcpyAsync(at<char>(oa), a_batch, nn * M, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(ow), wp, nn, cudaMemcpyHostToDevice, st));
+  CU(launch_cross_stats(at<uint8_t>(oa), at<uint8_t>(ow), n, M, t, parm,
+                        oar == NONE ? nullptr : at<uint32_t>(oar),
+                        owr == NONE ? nullptr : at<uint32_t>(owr), at<double>(oout), st));
+  CU(cudaMemcpyAsync(out, at<char>(oout), (size_t)M * 8, cudaMemcpyDeviceToHost, st));
   CU(cudaStreamSynchronize(st));
   return CUSNA_OK;
 }

@@ -90,7 +90,7 @@ __device__ __forceinline__ void step_helpers(const Team &T, const DevProblem &P,
 
 // Behaviour ministep (src/libcusna_saom_cpu.cpp:202-227), run by the team's
 // lane 0 in the reference's order. Returns nothing; updates z, bsc, *bdist.
-__device__ void beh_step(const DevProblem &P, const Slice &S, int i, uint32_t r3,
+static __device__ void beh_step(const DevProblem &P, const Slice &S, int i, uint32_t r3,
                          long long *bdist) {
   const int n = P.n, W = P.W, kb = P.kb;
   const int zi = S.z[i];
@@ -149,7 +149,7 @@ __device__ void beh_step(const DevProblem &P, const Slice &S, int i, uint32_t r3
 // computed in parallel; lane 0 then forms S0, the rate-score sums and the focal
 // actor in the reference's sequential order. Returns the focal actor, or -1
 // when an unconditional period ends.
-__device__ int rate_draw(const Team &T, const DevProblem &P, const Slice &S, const uint32_t rr[4],
+static __device__ int rate_draw(const Team &T, const DevProblem &P, const Slice &S, const uint32_t rr[4],
                          double lam, double &t, double &rho) {
   const int n = P.n, nr = P.nrate;
   for (int idx = T.tl; idx < P.nact; idx += T.L) {
@@ -286,9 +286,143 @@ __device__ __forceinline__ void block_lse(float *rec, float w, const float *d32,
   if (writer && q <= k) rec[q] = v[0];
 }
 
-// One chain: the ministep loop and the chain's outputs.
-__device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, int c) {
+// One network ministep of focal actor i on the network of slice S, up to the
+// choice: change statistics, float32 keys and log-sum-exp, the certified or
+// exact float64 choice, and the chosen alter's float64 change statistics in
+// S.dstar. Returns j*. The log-sum-exp sums are left in S.red[32G + q] for the
+// score update. d (float64) and d32 are per-thread scratch of k values.
+__device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, const Slice &S,
+                                          int i, long long ms, uint32_t chain, double *d,
+                                          float *d32) {
   const int n = P.n, W = P.W, k = P.k, L = T.L;
+  step_helpers(T, P, S, i);
+  StepCtx X;
+  X.i = i;
+  X.od_i = S.outdeg[i];
+  X.id_i = S.indeg[i];
+  X.rdeg_i = 0;
+  if (P.flags & F_NEED_RDEG)
+    for (int w = 0; w < W; ++w) X.rdeg_i += __popc(S.rowsT[w * n + i] & S.colsT[w * n + i]);
+  X.zvi = (P.flags & F_HAS_Z) ? __dsub_rn((double)S.z[i], P.zbar) : 0.0;
+  if (P.flags & F_HAS_STEP) {
+    step_values(T, P, S, X);
+    T.sync();
+  }
+
+  // ---- one pass over the alters ------------------------------------------
+  // Lane by lane, alters in ascending j: integer change statistics, the
+  // float32 predictor f32_j (change_stats32) and the float32 Gumbel key
+  // g_j = f32_j - loglog_est(u_j) with u_j from the reference's counters
+  // (msteps, chain, 1, j). The key is within
+  //   E_j = (k + 10) 2^-24 absf_j + 6e-6
+  // of the float64 key f_j - log(-log u_j): (k + 8) u absf_j for f32_j, 4e-6
+  // for loglog_est and u (absf_j + 23) for the subtraction (|f32_j| <= absf_j,
+  // |log(-log u)| < 23). gbuf[j] keeps the upper bound g_j + E_j.
+  // The log-sum-exp sums are formed per block of 32 alters (alter j on lane
+  // j mod 32, whatever the team size): the block maximum and the block's
+  // sums of exp(f - max) and exp(f - max) d_e with a fixed warp reduction,
+  // stored per block and combined in block order after the pass, so the
+  // scores do not depend on the launch shape.
+  KeyTop best{-INFINITY, 0.f, -INFINITY, 0x7FFFFFFF};
+  const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
+  for (int jb = 32 * T.warp; jb < n; jb += L) {
+    const int j = jb + T.lane;
+    bool ok = false, stay = false;
+    float f = 0.f;
+    if (j < n) {
+      const int aij = bit_of(S.rowsT, n, i, j);
+      float ub = -INFINITY;
+      stay = j == i;
+      ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
+      if (ok) {
+        float absf = 0.f;
+        if (!stay) f = change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+        uint32_t ph[4];
+        philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
+        const float g = __fsub_rn(f, loglog_est(ph[0]));
+        const float E = __fadd_rn(__fmul_rn(ecoef, absf), 6e-6f);
+        ub = __fadd_rn(g, E);
+        keytop_add(best, g, E, j);
+      }
+      S.gbuf[j] = ub;
+    }
+    const uint32_t okb = __ballot_sync(kFull, ok);
+    if (T.lane == 0) S.okbits[jb >> 5] = okb;
+    // a NaN predictor turns the sums into NaN, as exp(NaN - lmax) does in
+    // the reference, and never wins the choice (its key compares false)
+    const float mb = warp_max_f(ok ? f : -INFINITY);
+    const float w = ok ? expf(__fsub_rn(f, mb)) : 0.f;
+    float *rec = S.blk + (size_t)(jb >> 5) * (k + 2);
+    if (T.lane == 0) rec[0] = mb;
+    if (k + 1 <= 8) block_lse<8>(rec + 1, w, d32, ok && !stay, k, T.lane);
+    else if (k + 1 <= 16) block_lse<16>(rec + 1, w, d32, ok && !stay, k, T.lane);
+    else block_lse<32>(rec + 1, w, d32, ok && !stay, k, T.lane);
+  }
+  T.sync();
+  // blocks combined in order: lane q <= k forms quantity q (0: sum of
+  // weights, 1+e: weighted sum of d_e) rescaled to the overall maximum
+  if (T.tl <= k) {
+    const int nb = (n + 31) >> 5, q = T.tl;
+    float M = -INFINITY;
+    for (int b = 0; b < nb; ++b) M = fmaxf(M, S.blk[(size_t)b * (k + 2)]);
+    double acc = 0.0;
+    for (int b = 0; b < nb; ++b) {
+      const float *rec = S.blk + (size_t)b * (k + 2);
+      const float r = rec[0] == M ? 1.f : expf(__fsub_rn(rec[0], M));
+      acc = __dadd_rn(acc, (double)__fmul_rn(rec[1 + q], r));
+    }
+    S.red[32 * T.G + q] = acc;   // past the warp slots the reductions below use
+  }
+  const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
+
+  // ---- the chosen alter ---------------------------------------------------
+  // The float32 keys decide when the best key's lower bound exceeds every
+  // other alter's upper bound. Otherwise every alter whose upper bound
+  // reaches that lower bound gets its exact float64 key (the reference's
+  // f_j - log(-log u_j)) and those decide, ties to the smaller j.
+  int jstar;
+  const float lb = __fsub_rn(top.b1, top.e1);
+  if (lb > top.ub2) {
+    jstar = top.j1;
+  } else {
+    long long bk = dkey(-1e300);
+    int bj = 0x7FFFFFFF;
+    for (int j = T.tl; j < n; j += L) {
+      if (S.gbuf[j] >= lb) {
+        double f = 0.0;
+        if (j != i) {
+          const int aij = bit_of(S.rowsT, n, i, j);
+          f = change_stats<true>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
+        }
+        uint32_t ph[4];
+        philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
+        const double g = __dsub_rn(f, log(-log(unif01(ph[0]))));
+        if (is_nan64(g)) continue;
+        const long long kg = dkey(g);
+        if (kg > bk || (kg == bk && j < bj)) { bk = kg; bj = j; }
+      }
+    }
+    jstar = team_argmax(T, bk, bj, S.red + 29 * T.G);
+  }
+
+  // ---- score update (lane e updates effect e) and toggle ----------------
+  // the chosen alter's change statistics in float64, as the reference adds them
+  if (T.tl == jstar % L) {
+    if (jstar == i) {
+      for (int e = 0; e < k; ++e) S.dstar[e] = 0.0;
+    } else {
+      const int aij = bit_of(S.rowsT, n, i, jstar);
+      const int aji = bit_of(S.colsT, n, i, jstar);
+      change_stats<false>(P, S, X, jstar, aij, aji, d);
+      for (int e = 0; e < k; ++e) S.dstar[e] = d[e];
+    }
+  }
+  return jstar;
+}
+
+// One chain: the ministep loop and the chain's outputs.
+static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, int c) {
+  const int n = P.n, k = P.k;
   const uint32_t chain = P.chain_offset + (uint32_t)c;
   chain_init(T, P, S, c);
 
@@ -348,128 +482,7 @@ __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, in
       continue;
     }
 
-    step_helpers(T, P, S, i);
-    StepCtx X;
-    X.i = i;
-    X.od_i = S.outdeg[i];
-    X.id_i = S.indeg[i];
-    X.rdeg_i = 0;
-    if (P.flags & F_NEED_RDEG)
-      for (int w = 0; w < W; ++w) X.rdeg_i += __popc(S.rowsT[w * n + i] & S.colsT[w * n + i]);
-    X.zvi = (P.flags & F_HAS_Z) ? __dsub_rn((double)S.z[i], P.zbar) : 0.0;
-    if (P.flags & F_HAS_STEP) {
-      step_values(T, P, S, X);
-      T.sync();
-    }
-
-    // ---- one pass over the alters ------------------------------------------
-    // Lane by lane, alters in ascending j: integer change statistics, the
-    // float32 predictor f32_j (change_stats32) and the float32 Gumbel key
-    // g_j = f32_j - loglog_est(u_j) with u_j from the reference's counters
-    // (msteps, chain, 1, j). The key is within
-    //   E_j = (k + 10) 2^-24 absf_j + 6e-6
-    // of the float64 key f_j - log(-log u_j): (k + 8) u absf_j for f32_j, 4e-6
-    // for loglog_est and u (absf_j + 23) for the subtraction (|f32_j| <= absf_j,
-    // |log(-log u)| < 23). gbuf[j] keeps the upper bound g_j + E_j.
-    // The log-sum-exp sums are formed per block of 32 alters (alter j on lane
-    // j mod 32, whatever the team size): the block maximum and the block's
-    // sums of exp(f - max) and exp(f - max) d_e with a fixed warp reduction,
-    // stored per block and combined in block order after the pass, so the
-    // scores do not depend on the launch shape.
-    KeyTop best{-INFINITY, 0.f, -INFINITY, 0x7FFFFFFF};
-    const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
-    for (int jb = 32 * T.warp; jb < n; jb += L) {
-      const int j = jb + T.lane;
-      bool ok = false, stay = false;
-      float f = 0.f;
-      if (j < n) {
-        const int aij = bit_of(S.rowsT, n, i, j);
-        float ub = -INFINITY;
-        stay = j == i;
-        ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
-        if (ok) {
-          float absf = 0.f;
-          if (!stay) f = change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
-          uint32_t ph[4];
-          philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-          const float g = __fsub_rn(f, loglog_est(ph[0]));
-          const float E = __fadd_rn(__fmul_rn(ecoef, absf), 6e-6f);
-          ub = __fadd_rn(g, E);
-          keytop_add(best, g, E, j);
-        }
-        S.gbuf[j] = ub;
-      }
-      const uint32_t okb = __ballot_sync(kFull, ok);
-      if (T.lane == 0) S.okbits[jb >> 5] = okb;
-      // a NaN predictor turns the sums into NaN, as exp(NaN - lmax) does in
-      // the reference, and never wins the choice (its key compares false)
-      const float mb = warp_max_f(ok ? f : -INFINITY);
-      const float w = ok ? expf(__fsub_rn(f, mb)) : 0.f;
-      float *rec = S.blk + (size_t)(jb >> 5) * (k + 2);
-      if (T.lane == 0) rec[0] = mb;
-      if (k + 1 <= 8) block_lse<8>(rec + 1, w, d32, ok && !stay, k, T.lane);
-      else if (k + 1 <= 16) block_lse<16>(rec + 1, w, d32, ok && !stay, k, T.lane);
-      else block_lse<32>(rec + 1, w, d32, ok && !stay, k, T.lane);
-    }
-    T.sync();
-    // blocks combined in order: lane q <= k forms quantity q (0: sum of
-    // weights, 1+e: weighted sum of d_e) rescaled to the overall maximum
-    if (T.tl <= k) {
-      const int nb = (n + 31) >> 5, q = T.tl;
-      float M = -INFINITY;
-      for (int b = 0; b < nb; ++b) M = fmaxf(M, S.blk[(size_t)b * (k + 2)]);
-      double acc = 0.0;
-      for (int b = 0; b < nb; ++b) {
-        const float *rec = S.blk + (size_t)b * (k + 2);
-        const float r = rec[0] == M ? 1.f : expf(__fsub_rn(rec[0], M));
-        acc = __dadd_rn(acc, (double)__fmul_rn(rec[1 + q], r));
-      }
-      S.red[32 * T.G + q] = acc;   // past the warp slots the reductions below use
-    }
-    const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
-
-    // ---- the chosen alter ---------------------------------------------------
-    // The float32 keys decide when the best key's lower bound exceeds every
-    // other alter's upper bound. Otherwise every alter whose upper bound
-    // reaches that lower bound gets its exact float64 key (the reference's
-    // f_j - log(-log u_j)) and those decide, ties to the smaller j.
-    int jstar;
-    const float lb = __fsub_rn(top.b1, top.e1);
-    if (lb > top.ub2) {
-      jstar = top.j1;
-    } else {
-      long long bk = dkey(-1e300);
-      int bj = 0x7FFFFFFF;
-      for (int j = T.tl; j < n; j += L) {
-        if (S.gbuf[j] >= lb) {
-          double f = 0.0;
-          if (j != i) {
-            const int aij = bit_of(S.rowsT, n, i, j);
-            f = change_stats<true>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
-          }
-          uint32_t ph[4];
-          philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-          const double g = __dsub_rn(f, log(-log(unif01(ph[0]))));
-          if (is_nan64(g)) continue;
-          const long long kg = dkey(g);
-          if (kg > bk || (kg == bk && j < bj)) { bk = kg; bj = j; }
-        }
-      }
-      jstar = team_argmax(T, bk, bj, S.red + 29 * T.G);
-    }
-
-    // ---- score update (lane e updates effect e) and toggle ----------------
-    // the chosen alter's change statistics in float64, as the reference adds them
-    if (T.tl == jstar % L) {
-      if (jstar == i) {
-        for (int e = 0; e < k; ++e) S.dstar[e] = 0.0;
-      } else {
-        const int aij = bit_of(S.rowsT, n, i, jstar);
-        const int aji = bit_of(S.colsT, n, i, jstar);
-        change_stats<false>(P, S, X, jstar, aij, aji, d);
-        for (int e = 0; e < k; ++e) S.dstar[e] = d[e];
-      }
-    }
+    const int jstar = net_choice(T, P, S, i, ms, chain, d, d32);
     const int aij_star = bit_of(S.rowsT, n, i, jstar);
     T.sync();
     if (T.tl < k) {

@@ -41,6 +41,7 @@ enum : int {
                // alter covariate, dyadic covariate tables)
   K_STEP = 3,  // magnitude depends only on (i, a_ij, a_ji): formed per ministep
   K_ZERO = 4,  // the dyadic covariate X, which the CPU engine zero-fills
+  K_CROSS = 5, // multi-network cross effect (ecfn = type 33..37) reading network eoffd
 };
 
 // Canonical device form of one cusna_saom_problem. Every network is stored

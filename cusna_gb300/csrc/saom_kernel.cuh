@@ -58,6 +58,10 @@ struct Slice {
   int *rnet, *rfocal; //   network/behaviour flag, focal actor,
   uint32_t *rr3;     //   behaviour uniform
   int *ekind, *ecfn, *eoffd, *eofft;  // k  effect plan
+  // multi-network teams: network d's rows/columns are rows0/cols0 + d*net_stride
+  // words (single network: rows0 = rowsT, cols0 = colsT)
+  const uint32_t *rows0, *cols0;
+  size_t net_stride;
   double *stepd, *stept;  // 4k  per-ministep K_STEP magnitudes and terms
   float *stepd32, *stept32;  // 4k  their float32 images
 };
@@ -130,6 +134,9 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   Slice s;
   s.rowsT = rows_global ? rows_global : (uint32_t *)(base + L.o_rows);
   s.colsT = cols_global ? cols_global : (uint32_t *)(base + L.o_cols);
+  s.rows0 = s.rowsT;
+  s.cols0 = s.colsT;
+  s.net_stride = 0;
   s.indeg = (short *)(base + L.o_indeg);
   s.outdeg = (short *)(base + L.o_outdeg);
   s.z = (int *)(base + L.o_z);
@@ -435,6 +442,30 @@ __device__ __forceinline__ void step_values(const Team &T, const DevProblem &P, 
 // sign flip, table entries are the reference's expressions evaluated once, and
 // f adds the terms in e-order (terms of zeroed effects are +-0 and change
 // nothing, so they are skipped).
+// Cross-network change statistic magnitude (before the sign of the toggle) of
+// toggling i -> j in the own network for cross effect type t, reading network
+// w's current rows (src/libcusna_saom_cpu.cpp:431-444): 33 a_w[i][j], 34
+// a_w[j][i], 35 both, 36 |out_w(i) & out_w(j)|, 37 |out_w(i) & in_own(j)|.
+__device__ __forceinline__ int cross_count(const Slice &S, int n, int W, int t, int w, int i,
+                                           int j) {
+  const uint32_t *Rw = S.rows0 + (size_t)w * S.net_stride;
+  switch (t) {
+    case 33: return bit_of(Rw, n, i, j);
+    case 34: return bit_of(Rw, n, j, i);
+    case 35: return bit_of(Rw, n, i, j) & bit_of(Rw, n, j, i);
+    case 36: {
+      int c = 0;
+      for (int x = 0; x < W; ++x) c += __popc(Rw[x * n + i] & Rw[x * n + j]);
+      return c;
+    }
+    default: {  // 37
+      int c = 0;
+      for (int x = 0; x < W; ++x) c += __popc(Rw[x * n + i] & S.colsT[x * n + j]);
+      return c;
+    }
+  }
+}
+
 template <bool TERMS>
 __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice &S,
                                                const StepCtx &X, int j, int aij, int aji,
@@ -507,6 +538,10 @@ __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice 
     } else if (kind == K_ZERO) {
       v = 0.0;
       has_term = false;
+    } else if (kind == K_CROSS) {
+      const int c = cross_count(S, n, W, cfn, S.eoffd[e], i, j);
+      v = flip((cfn == 36 && S.p1[e] >= 2.0) ? sqrt(i2d(c)) : i2d(c), sg);
+      if (TERMS) term = __dmul_rn(S.th[e], v);
     } else {
       v = gen_stat(P, S, X, e, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, d);
       if (TERMS) term = __dmul_rn(S.th[e], v);
@@ -600,6 +635,11 @@ __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice
     } else if (kind == K_ZERO) {
       v = 0.f;
       has_term = false;
+    } else if (kind == K_CROSS) {
+      const int c = cross_count(S, n, W, cfn, S.eoffd[e], i, j);
+      const float m = (cfn == 36 && S.p1[e] >= 2.0) ? sqrtf((float)c) : (float)c;
+      v = __uint_as_float(__float_as_uint(m) ^ sg);
+      term = __fmul_rn(S.th32[e], v);
     } else if (S.tid[e] == 32) {
       const int c2 = S.i2[e];
       v = __fmul_rn(d32[S.i0[e]], d32[S.i1[e]]);

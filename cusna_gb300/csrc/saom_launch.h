@@ -5,6 +5,7 @@
 #include <cstdint>
 #include "saom_common.cuh"
 #include "saom_kernel.cuh"
+#include "libcusna.h"
 
 namespace cusna {
 
@@ -25,6 +26,31 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
                           uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
                           cudaStream_t st);
 int period_blocks_per_sm(int threads, size_t dyn_smem);
+
+// Multi-network problem: what the kernel needs beyond the per-network problems
+// (one DevProblem per network, holding that network's effects).
+struct MultiDev {
+  int D, n, W, nact, k;
+  const int *act;                 // nact active actors first
+  const float *lam;               // M*D rates
+  uint32_t k0, k1;                // Philox key
+  int goff[CUSNA_MAXNET + 1];     // network d's effects: gidx[goff[d] .. goff[d+1])
+  const int *gidx;                // their indices in the caller's effect order
+  float *rscores, *scores;        // device outputs (any may be null)
+  double *ntim;
+  int *steps;
+  uint8_t *a_ends;
+};
+int multi_blocks_per_sm(int threads, size_t dyn_smem);
+cudaError_t launch_multi(const LaunchShape &sh, const DevProblem *nets, const MultiDev &md, int M,
+                         unsigned long long *counter, uint32_t *cols_scratch,
+                         uint32_t *rows_scratch, size_t cols_words, cudaStream_t st);
+// Cross-network statistic of M dense own networks a against the dense source
+// predictor wp; ar (M*n*W words, type 37) and wr (n*W words, type 36) are
+// scratch for packed rows.
+cudaError_t launch_cross_stats(const uint8_t *a, const uint8_t *wp, int n, int M, int t,
+                               double parm, uint32_t *ar, uint32_t *wr, double *out,
+                               cudaStream_t st);
 
 // One theta-premultiplied term table of a plan's problem q, effect e (pool
 // offsets of the table and, for lookup tables, of its values).

@@ -1,0 +1,275 @@
+// saom_multi.cu -- the multi-network period simulator (cusna_saom_simulate_multi).
+//
+// Restates the reference's multi-network chain (src/libcusna_saom_cpu.cpp:
+// 463-552, simulate_one_multi) on the GB300 team design. D networks share the
+// actors; a team keeps one shared-memory slice per network (bit rows and
+// columns, degrees, the network's effect plan and parameters), laid out one
+// after another, so a cross-network effect reads network w's rows at a fixed
+// stride from network 0's. Each ministep draws the waiting time from the total
+// rate, the network in proportion to its rate and the focal actor (32
+// ministeps at a time, the reference's counters (msteps, chain, 0, 0)), then
+// runs the single-network choice (net_choice) on the chosen network's slice.
+#include "saom_chain.cuh"
+#include "saom_launch.h"
+
+namespace cusna {
+
+__device__ __forceinline__ Slice multi_slice(unsigned char *base, const SliceLayout &lay, int d,
+                                             uint32_t *cols_g, uint32_t *rows_g,
+                                             size_t cols_words) {
+  Slice s = carve(base + (size_t)d * lay.bytes, lay, cols_g ? cols_g + (size_t)d * cols_words : nullptr,
+                  rows_g ? rows_g + (size_t)d * cols_words : nullptr);
+  s.rows0 = rows_g ? rows_g : (uint32_t *)(base + lay.o_rows);
+  s.cols0 = cols_g ? cols_g : (uint32_t *)(base + lay.o_cols);
+  s.net_stride = rows_g ? cols_words : lay.bytes / 4;
+  return s;
+}
+
+__device__ void run_chain_multi(const Team &T, const DevProblem *nets, const MultiDev &md,
+                                unsigned char *base, const SliceLayout &lay, uint32_t *cols_g,
+                                uint32_t *rows_g, size_t cols_words, int c) {
+  const int D = md.D, n = md.n, L = T.L;
+  const uint32_t chain = (uint32_t)c;
+  for (int d = 0; d < D; ++d)
+    chain_init(T, nets[d], multi_slice(base, lay, d, cols_g, rows_g, cols_words), c);
+  double lam_d[CUSNA_MAXNET];
+  double lam_tot = 0.0;
+  for (int d = 0; d < D; ++d) {
+    lam_d[d] = (double)md.lam[(size_t)c * D + d];
+    lam_tot = __dadd_rn(lam_tot, lam_d[d]);
+  }
+  const double den = __dmul_rn((double)md.nact, lam_tot);
+  long long ms = 0, msd[CUSNA_MAXNET] = {};
+  double t = 0.0;
+  double dbuf[24];
+  float d32[24];
+  const Slice S0 = multi_slice(base, lay, 0, cols_g, rows_g, cols_words);
+  for (;;) {
+    const int slot = (int)(ms & 31);
+    if (slot == 0) {
+      if (T.warp == 0) {
+        uint32_t rr[4];
+        philox10((uint32_t)(ms + T.lane), chain, 0u, 0u, md.k0, md.k1, rr);
+        S0.rtau[T.lane] = __ddiv_rn(-log(unif01(rr[0])), den);
+        const double uv = __dmul_rn(unif01(rr[1]), lam_tot);
+        int d = 0;
+        double acc = lam_d[0];
+        while (d < D - 1 && uv >= acc) {
+          d += 1;
+          acc = __dadd_rn(acc, lam_d[d]);
+        }
+        S0.rnet[T.lane] = d;
+        long long idx = (long long)__dmul_rn(unif01(rr[2]), (double)md.nact);
+        if (idx >= md.nact) idx = md.nact - 1;
+        S0.rfocal[T.lane] = md.act[idx];
+      }
+      T.sync();
+    }
+    t = __dadd_rn(t, S0.rtau[slot]);
+    if (t > 1.0) break;
+    const int d = S0.rnet[slot], i = S0.rfocal[slot];
+    const DevProblem &P = nets[d];
+    const Slice S = multi_slice(base, lay, d, cols_g, rows_g, cols_words);
+    const int jstar = net_choice(T, P, S, i, ms, chain, dbuf, d32);
+    const int aij_star = bit_of(S.rowsT, n, i, jstar);
+    T.sync();
+    if (T.tl < P.k) {
+      const int e = T.tl;
+      const double s0 = S.red[32 * T.G], se = S.red[32 * T.G + 1 + e];
+      S.sc[e] = __dadd_rn(S.sc[e], __dsub_rn(S.dstar[e], __ddiv_rn(se, s0)));
+    }
+    ++ms;
+    ++msd[d];
+    if (jstar != i && T.tl == 0) {
+      const int j = jstar, dl = 1 - 2 * aij_star;
+      S.rowsT[(j >> 5) * n + i] ^= 1u << (j & 31);
+      S.colsT[(i >> 5) * n + j] ^= 1u << (i & 31);
+      S.indeg[j] += dl;
+      S.outdeg[i] += dl;
+      if (P.symflag) {
+        S.rowsT[(i >> 5) * n + j] ^= 1u << (i & 31);
+        S.colsT[(j >> 5) * n + i] ^= 1u << (j & 31);
+        S.indeg[i] += dl;
+        S.outdeg[j] += dl;
+      }
+    }
+    T.sync();
+    if (ms >= kMaxSteps) break;
+  }
+  // outputs (src/libcusna_saom_cpu.cpp:549-551, :594-600)
+  if (T.tl == 0) {
+    if (md.ntim) md.ntim[c] = t;
+    if (md.steps) md.steps[c] = (int)ms;
+    if (md.rscores)
+      for (int d = 0; d < D; ++d)
+        md.rscores[(size_t)c * D + d] =
+            (float)__dsub_rn(__ddiv_rn((double)msd[d], lam_d[d]), (double)md.nact);
+  }
+  for (int d = 0; d < D; ++d) {
+    const Slice S = multi_slice(base, lay, d, cols_g, rows_g, cols_words);
+    if (md.scores)
+      for (int q = T.tl; q < md.goff[d + 1] - md.goff[d]; q += L)
+        md.scores[(size_t)c * md.k + md.gidx[md.goff[d] + q]] = (float)S.sc[q];
+    if (md.a_ends) {
+      uint8_t *out = md.a_ends + ((size_t)c * D + d) * n * n;
+      for (size_t x = T.tl; x < (size_t)n * n; x += L) {
+        const int r = (int)(x / n), col = (int)(x % n);
+        out[x] = (uint8_t)bit_of(S.rowsT, n, r, col);
+      }
+    }
+  }
+  T.sync();
+}
+
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
+multi_kernel(const DevProblem *__restrict__ nets, MultiDev md, int M,
+             unsigned long long *counter, SliceLayout lay, int G, uint32_t *cols_scratch,
+             uint32_t *rows_scratch, size_t cols_words) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Team T;
+  T.G = G;
+  T.L = 32 * G;
+  const int tw = threadIdx.x / T.L;
+  T.tl = threadIdx.x % T.L;
+  T.warp = T.tl >> 5;
+  T.lane = T.tl & 31;
+  T.bar = 1 + tw;
+  const int teams_per_cta = blockDim.x / T.L;
+  const size_t slot = (size_t)blockIdx.x * teams_per_cta + tw;
+  unsigned char *base = smem + (size_t)tw * lay.bytes * md.D;
+  uint32_t *cg = cols_scratch ? cols_scratch + slot * md.D * cols_words : nullptr;
+  uint32_t *rg = rows_scratch ? rows_scratch + slot * md.D * cols_words : nullptr;
+  const Slice S0 = multi_slice(base, lay, 0, cg, rg, cols_words);
+  for (;;) {
+    long long u = 0;
+    if (T.tl == 0) u = (long long)atomicAdd(counter, 1ull);
+    if (G == 1) {
+      u = __shfl_sync(kFull, u, 0);
+    } else {
+      if (T.tl == 0) ((long long *)(S0.misc + 8))[0] = u;
+      T.sync();
+      u = ((long long *)(S0.misc + 8))[0];
+      T.sync();
+    }
+    if (u >= M) break;
+    run_chain_multi(T, nets, md, base, lay, cg, rg, cols_words, (int)u);
+  }
+}
+
+int multi_blocks_per_sm(int threads, size_t dyn_smem) {
+  int blocks = 0;
+  auto kern = threads <= 256 ? multi_kernel<256> : multi_kernel<512>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, threads, dyn_smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return blocks;
+}
+
+cudaError_t launch_multi(const LaunchShape &sh, const DevProblem *nets, const MultiDev &md, int M,
+                         unsigned long long *counter, uint32_t *cols_scratch,
+                         uint32_t *rows_scratch, size_t cols_words, cudaStream_t st) {
+  const int threads = 32 * sh.G * sh.teams_per_cta;
+  const size_t dyn = sh.lay.bytes * md.D * sh.teams_per_cta;
+  auto kern = threads <= 256 ? multi_kernel<256> : multi_kernel<512>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  if (e != cudaSuccess) return e;
+  kern<<<sh.ctas, threads, dyn, st>>>(nets, md, M, counter, sh.lay, sh.G, cols_scratch,
+                                      rows_scratch, cols_words);
+  return cudaGetLastError();
+}
+
+// ---- cross-network statistics (src/libcusna_saom_cpu.cpp:819-857) ----------
+// Rows of dense uint8 matrices packed into W words each (word w of row r holds
+// columns 32w .. 32w+31), one thread per word.
+__global__ void pack_rows_kernel(const uint8_t *__restrict__ a, long long rows, int n, int W,
+                                 uint32_t *__restrict__ out) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= rows * W) return;
+  const long long r = x / W;
+  const int w = (int)(x % W);
+  const uint8_t *src = a + r * n;
+  uint32_t v = 0;
+  for (int b = 0; b < 32; ++b) {
+    const int col = 32 * w + b;
+    if (col < n && src[col]) v |= 1u << b;
+  }
+  out[x] = v;
+}
+
+// One CTA per chain: the cross statistic of own network a (dense rows a, packed
+// rows ar) against the source predictor wp (dense, packed rows wr).
+//   33 sum a_ij wp_ij      34 sum a_ij wp_ji      35 sum a_ij wp_ij wp_ji
+//   36 sum a_ij s_ij, s_ij = |wp row i & wp row j| (sqrt when parm >= 2)
+//   37 sum a_ij (wp a)_ij = sum over wp_ih = 1 of |a row i & a row h|
+// Integer sums are exact in any order; the square-root sum of 36 adds in a
+// fixed order for a given launch.
+__global__ void __launch_bounds__(256) cross_stats_kernel(const uint8_t *__restrict__ a,
+                                                          const uint8_t *__restrict__ wp,
+                                                          const uint32_t *__restrict__ ar,
+                                                          const uint32_t *__restrict__ wr, int n,
+                                                          int W, int t, double parm,
+                                                          double *__restrict__ out) {
+  __shared__ double part[8];
+  const int c = blockIdx.x;
+  const size_t nn = (size_t)n * n;
+  const uint8_t *A = a + (size_t)c * nn;
+  const uint32_t *AR = ar ? ar + (size_t)c * n * W : nullptr;
+  double acc = 0.0;
+  for (size_t q = threadIdx.x; q < nn; q += blockDim.x) {
+    const int i = (int)(q / n), j = (int)(q % n);
+    switch (t) {
+      case 33: acc += (double)(A[q] & wp[q]); break;
+      case 34: acc += (double)(A[q] & wp[(size_t)j * n + i]); break;
+      case 35: acc += (double)(A[q] & wp[q] & wp[(size_t)j * n + i]); break;
+      case 36:
+        if (A[q]) {
+          int s = 0;
+          for (int w = 0; w < W; ++w) s += __popc(wr[(size_t)i * W + w] & wr[(size_t)j * W + w]);
+          acc += parm >= 2.0 ? sqrt((double)s) : (double)s;
+        }
+        break;
+      default:  // 37: q = (i, h) over the predictor
+        if (wp[q]) {
+          int s = 0;
+          for (int w = 0; w < W; ++w) s += __popc(AR[(size_t)i * W + w] & AR[(size_t)j * W + w]);
+          acc += (double)s;
+        }
+        break;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int x = 0; x < (int)(blockDim.x >> 5); ++x) s += part[x];
+    out[c] = s;
+  }
+}
+
+cudaError_t launch_cross_stats(const uint8_t *a, const uint8_t *wp, int n, int M, int t,
+                               double parm, uint32_t *ar, uint32_t *wr, double *out,
+                               cudaStream_t st) {
+  const int W = (n + 31) / 32;
+  if (t == 36) {
+    const long long words = (long long)n * W;
+    pack_rows_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(wp, n, n, W, wr);
+  }
+  if (t == 37) {
+    const long long words = (long long)M * n * W;
+    pack_rows_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a, (long long)M * n, n, W, ar);
+  }
+  cross_stats_kernel<<<M, 256, 0, st>>>(a, wp, t == 37 ? ar : nullptr, t == 36 ? wr : nullptr, n,
+                                        W, t, parm, out);
+  return cudaGetLastError();
+}
+
+}  // namespace cusna

@@ -213,3 +213,97 @@ def marshal_period(inp: PeriodInputs, M: int, seed: int, lam, theta, lamb=0.0, t
 
 def result_dict(m: Marshalled) -> dict:
     return {k[4:]: v for k, v in m.keep.items() if k.startswith("out_")}
+
+
+@dataclass
+class MultiInputs:
+    """One multi-network period (the arguments of the reference glue's
+    cusna_simulate_multi_cpu_, src/cusna_saom_glue.cpp:230-290): D start
+    networks on n shared actors and the effects of all networks."""
+    x0s: list                     # D dense n*n start networks
+    type_ids: np.ndarray          # k
+    netof: np.ndarray             # k, 0..D-1
+    netref: np.ndarray            # k, source network of cross effects (else -1)
+    etypes: np.ndarray            # k
+    wtab: np.ndarray              # k*(n+1)
+    p1: np.ndarray                # k
+    p2: np.ndarray                # k
+    vmat: np.ndarray              # k*n
+    perm: list | None = None      # D dense n*n permitted dyads (None: all i != j)
+    symf: np.ndarray | None = None  # D
+    dyc: np.ndarray | None = None   # n*n dyadic covariate (read by type 22)
+    dyc_idx: np.ndarray | None = None  # k: 0 reads dyc, -1 none (None: all -1)
+
+    @property
+    def n(self):
+        return int(np.asarray(self.x0s[0]).shape[0])
+
+    @property
+    def D(self):
+        return len(self.x0s)
+
+    @property
+    def k(self):
+        return len(self.type_ids)
+
+
+def marshal_multi(inp: MultiInputs, M: int, seed: int, lam, theta,
+                  want_ends: bool = True) -> Marshalled:
+    """cusna_saom_multi_problem/result for M chains, marshalled as the glue does
+    (float32 descriptors and parameters, every actor active).
+    lam: (D,) broadcast or (M, D); theta: (k,) broadcast or (M, k)."""
+    from .abi import MultiProblem, MultiResult
+    n, D, k = inp.n, inp.D, inp.k
+    W = (n + 31) // 32
+    keep = {}
+
+    def hold(name, arr):
+        keep[name] = arr
+        return ptr(arr)
+
+    p = MultiProblem()
+    C.memset(C.addressof(p), 0, C.sizeof(p))
+    p.struct_version = ABI_VERSION
+    p.n, p.W, p.k, p.M, p.D, p.threads = n, W, k, int(M), D, 0
+    outs, ins, perms = [], [], []
+    for d in range(D):
+        o, i_ = pack_rows(np.asarray(inp.x0s[d]) != 0)
+        outs.append(o)
+        ins.append(i_)
+        pm = (np.asarray(inp.perm[d]) != 0) if inp.perm is not None else ~np.eye(n, dtype=bool)
+        perms.append(pack_rows(pm)[0])
+    p.x0_out = hold("x0_out", np.concatenate(outs))
+    p.x0_in = hold("x0_in", np.concatenate(ins))
+    p.perm = hold("perm", np.concatenate(perms))
+    lv = np.asarray(lam, dtype=np.float64)
+    lv = np.broadcast_to(lv, (M, D)) if lv.ndim == 1 else lv.reshape(M, D)
+    p.lam = hold("lam", _c(lv.astype(np.float32), np.float32))
+    th = np.asarray(theta, dtype=np.float64)
+    th = np.broadcast_to(th, (M, k)) if th.ndim == 1 else th.reshape(M, k)
+    p.theta = hold("theta", _c(th.astype(np.float32), np.float32))
+    p.type_ids = hold("type_ids", _c(inp.type_ids, np.int32))
+    p.etypes = hold("etypes", _c(inp.etypes, np.int32))
+    p.netof = hold("netof", _c(inp.netof, np.int32))
+    p.netref = hold("netref", _c(inp.netref, np.int32))
+    p.wtab = hold("wtab", _c(inp.wtab, np.float32))
+    p.p1 = hold("p1", _c(inp.p1, np.float32))
+    p.p2 = hold("p2", _c(inp.p2, np.float32))
+    p.vmat = hold("vmat", _c(inp.vmat, np.float32))
+    p.dyc_idx = hold("dyc_idx", _c(inp.dyc_idx if inp.dyc_idx is not None
+                                   else -np.ones(k), np.int32))
+    if inp.dyc is not None:
+        p.dyc = hold("dyc", _c(inp.dyc, np.float32))
+    p.symf = hold("symf", _c(inp.symf if inp.symf is not None else np.zeros(D), np.int32))
+    p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    p.act = hold("act", np.arange(n, dtype=np.int32))
+    p.nact = n
+    r = MultiResult()
+    C.memset(C.addressof(r), 0, C.sizeof(r))
+    r.struct_version = ABI_VERSION
+    r.rscores = hold("out_rscores", np.zeros((M, D), np.float32))
+    r.scores = hold("out_scores", np.zeros((M, k), np.float32))
+    r.ntim = hold("out_ntim", np.zeros(M, np.float64))
+    r.steps = hold("out_steps", np.zeros(M, np.int32))
+    if want_ends:
+        r.a_ends = hold("out_a_ends", np.zeros((M, D, n, n), np.uint8))
+    return Marshalled(p, r, keep)

@@ -204,6 +204,31 @@ def network_stats(a, n, k, type_ids, p1, p2, vmat, vmiss, dyn_flags, vb, od0, id
     return out[0] if single else out
 
 
+def simulate_multi(m) -> dict:
+    """One marshalled multi-network period (cusna_gb300.glue.marshal_multi)
+    through cusna_saom_simulate_multi."""
+    lib = load_library()
+    st = lib.cusna_saom_simulate_multi(C.byref(m.problem), C.byref(m.result))
+    check(st, "cusna_saom_simulate_multi", lib)
+    return result_dict(m)
+
+
+def cross_stats(a_batch, wp, t, parm=0.0) -> np.ndarray:
+    """Cross-network statistic of type t (33..37) of own networks a_batch
+    ((n,n) or (M,n,n)) against the source predictor wp, on the GPU."""
+    lib = load_library()
+    a = np.ascontiguousarray(np.asarray(a_batch) != 0, dtype=np.uint8)
+    if a.ndim == 2:
+        a = a[None]
+    M, n = a.shape[0], a.shape[1]
+    w = np.ascontiguousarray(np.asarray(wp) != 0, dtype=np.uint8)
+    out = np.zeros(M)
+    st = lib.cusna_cross_stats(a.ctypes.data, w.ctypes.data, n, M, int(t), float(parm),
+                               out.ctypes.data)
+    check(st, "cusna_cross_stats", lib)
+    return out
+
+
 def behavior_stats(z_batch, bty, xnet, bkdist, zbar, brange, bsimmean) -> np.ndarray:
     lib = load_library()
     z = np.ascontiguousarray(np.atleast_2d(np.asarray(z_batch, dtype=np.int32)))

@@ -292,3 +292,81 @@ def c3_groups(engine, n_groups: int = 512, seed: int = 4, lam: float = 6.0):
         for g in range(n_groups):
             waves[g].append(outs[g]["a_ends"][0].astype(np.int64))
     return [(waves[g], covs[g]) for g in range(n_groups)]
+
+
+# ---- multi-network parity cases ------------------------------------------------
+MULTI_KINDS = ["cross", "typed_cov", "symmetric", "dyadic", "empty_net"]
+
+
+def multi_case(kind: str, seed: int = 0, n: int = 40, M: int = 4, D: int = 2):
+    """Small multi-network periods for exact GPU-vs-CPU comparisons: D start
+    networks on n actors, per-network effects with cross-network effects of
+    every type (33..37) reading the other networks. "dyadic" adds a dyadic
+    covariate effect (type 22) and reciAct (19, which the multi-network engine
+    evaluates with a reciprocated degree of 0); "empty_net" leaves the last
+    network without effects (its ministeps choose uniformly). Returns
+    (MultiInputs, seed, lam (D,), theta (k,))."""
+    from .glue import MultiInputs
+    r = _rng(2000 + seed)
+    x0s = [bernoulli_net(n, 0.06 + 0.02 * d, seed=seed * 31 + d) for d in range(D)]
+    cov = np.round(r.standard_normal(n), 3)
+    effs, netof, th, dyadic = [], [], [], []
+    for d in range(D):
+        src = (d + 1) % D
+        if kind == "empty_net" and d == D - 1:
+            continue
+        if kind == "cross":
+            spec = [("density", None, None, -2.0), ("recip", None, None, 0.9),
+                    ("transTrip", None, None, 0.15), ("crprod", None, src, 0.6),
+                    ("crprodRecip", None, src, 0.3), ("crprodMutual", None, src, -0.2),
+                    ("from", None, src, 0.1), ("to", None, src, 0.05)]
+        elif kind == "typed_cov":
+            spec = [("density", None, None, -2.1), ("recip", None, None, 1.0),
+                    ("inPop", None, None, 0.05), ("altX", cov, None, 0.2),
+                    ("simX", cov, None, 0.5), ("egoPlusAltX", cov, None, 0.3),
+                    ("crprod", None, src, 0.7)]
+        elif kind == "symmetric":
+            spec = [("density", None, None, -1.6), ("transTriads", None, None, 0.2),
+                    ("crprod", None, src, 0.5)]
+        elif kind == "dyadic":
+            spec = [("density", None, None, -2.0), ("recip", None, None, 0.8),
+                    ("X", None, None, 0.9), ("reciAct", None, None, 0.1),
+                    ("to", None, src, 0.2)]
+        elif kind == "empty_net":
+            spec = [("density", None, None, -1.9), ("recip", None, None, 0.7),
+                    ("crprod", None, D - 1, 0.8), ("from", None, D - 1, 0.1)]
+        else:
+            raise ValueError(kind)
+        for name, cv, ref, t in spec:
+            # the dyadic covariate effect reads the multi problem's dyc; its
+            # descriptor row is a density row with the type id set afterwards
+            dyadic.append(name == "X")
+            e = E.make_effect_spec("density" if name == "X" else name, cv, net_ref=ref)
+            if name == "egoPlusAltX":
+                e = E.make_effect_spec(name, cv, etype="creation" if d == 0 else "endow")
+            effs.append(e)
+            netof.append(d)
+            th.append(t)
+    pe = E.prepare_effects_v2(effs, n, 1, None, None)
+    symf = np.ones(D, np.int32) if kind == "symmetric" else np.zeros(D, np.int32)
+    if kind == "symmetric":
+        x0s = [((np.triu(x, 1) | np.triu(x, 1).T) != 0).astype(np.uint8) for x in x0s]
+    p1 = np.asarray(pe.p1, dtype=np.float64).copy()
+    for q, e in enumerate(effs):
+        if e.name == "from":
+            p1[q] = 2.0 if seed % 2 else 1.0   # square-root variant on odd seeds
+    tids = np.asarray(pe.type_ids, np.int32).copy()
+    dyc_idx = -np.ones(len(effs), np.int32)
+    dyc = None
+    if any(dyadic):
+        tids[np.asarray(dyadic)] = E.EFF_X
+        dyc_idx[np.asarray(dyadic)] = 0
+        dyc = np.round(r.standard_normal((n, n)), 3)
+        np.fill_diagonal(dyc, 0.0)
+    inp = MultiInputs(x0s=x0s, type_ids=tids,
+                      netof=np.asarray(netof, np.int32), netref=E.effect_netrefs(effs),
+                      etypes=E.effect_etypes(effs), wtab=E.effect_wtabs(effs, n), p1=p1,
+                      p2=np.asarray(pe.p2), vmat=np.asarray(pe.vmat), symf=symf, dyc=dyc,
+                      dyc_idx=dyc_idx)
+    lam = np.array([3.0 + 1.5 * d + r.uniform(0, 1) for d in range(D)])
+    return inp, int(r.integers(1, 2 ** 62)), lam, np.array(th)

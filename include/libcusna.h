@@ -304,6 +304,73 @@ CUSNA_API cusna_status cusna_saom_plan_shape(const cusna_saom_plan *plan,
 /* Waits for the device, then frees the plan and its device memory. */
 CUSNA_API void cusna_saom_plan_destroy(cusna_saom_plan *plan);
 
+/* ---- multi-network co-evolution (src/libcusna.h:219-291) --------------------
+ * D one-mode networks (2..CUSNA_MAXNET) on one actor set. Each ministep picks a
+ * network with probability proportional to its rate, then one actor of it
+ * toggles (or keeps) one tie. netof[e] is the network effect e belongs to;
+ * cross-network effects (type ids 33 crprod, 34 crprodRecip, 35 crprodMutual,
+ * 36 from, 37 to) read the current state of network netref[e]. The simulator
+ * returns scores, rate scores, times, steps and the end networks; statistics
+ * are computed from the end networks (cusna_network_stats_gpu,
+ * cusna_cross_stats). Structs as the reference lays them out. As in the
+ * reference engine, interactions (type 32) change nothing, reciAct (19) sees a
+ * reciprocated degree of 0, and dyc is one n*n dyadic covariate (dyc_idx -1 or
+ * 0, read by type 22). */
+typedef struct cusna_saom_multi_problem {
+    int32_t struct_version;   /* CUSNA_ABI_VERSION                              */
+    int32_t n;                /* actors, shared by the D networks               */
+    int32_t W;                /* (n + 31) / 32                                  */
+    int32_t k;                /* network effects over all networks, <= MAXEFF   */
+    int32_t M;                /* chains                                         */
+    int32_t D;                /* networks, 2..CUSNA_MAXNET                      */
+    int32_t threads;          /* unused by this build                           */
+
+    const uint32_t *x0_out;   /* D*n*W packed out-ties of the start networks    */
+    const uint32_t *x0_in;    /* D*n*W packed in-ties                           */
+    const float   *lam;       /* M*D per-chain, per-network basic rates         */
+    const float   *theta;     /* M*k per-chain parameters                       */
+
+    const int32_t *type_ids;  /* k effect type ids                              */
+    const int32_t *etypes;    /* k: 0 evaluation, 1 creation, 2 endowment       */
+    const int32_t *netof;     /* k: network of each effect, 0..D-1              */
+    const int32_t *netref;    /* k: source network of a cross effect, else 0    */
+    const float   *wtab;      /* k*(n+1) weight tables                          */
+    const float   *p1;        /* k                                              */
+    const float   *p2;        /* k                                              */
+    const float   *vmat;      /* k*n covariate values                           */
+    const float   *dyc;       /* [opt] dyadic covariates                        */
+    const int32_t *dyc_idx;   /* k: index into dyc, or -1                       */
+    const uint32_t *perm;     /* [opt] D*n*W permitted dyads (NULL: all i != j) */
+    const int32_t *symf;      /* D per-network symmetric flags                  */
+    uint64_t seed;            /* Philox key                                     */
+    const int32_t *act;       /* [opt] active actors first                      */
+    int32_t nact;             /* active actor count                             */
+} cusna_saom_multi_problem;
+
+typedef struct cusna_saom_multi_result {
+    int32_t struct_version;
+    float   *rscores;         /* [opt] M*D per-network basic-rate scores        */
+    float   *scores;          /* [opt] M*k effect scores                        */
+    double  *ntim;            /* [opt] M elapsed simulated time                 */
+    int32_t *steps;           /* [opt] M ministeps                              */
+    uint8_t *a_ends;          /* [opt] M*D*n*n dense end networks (row-major)   */
+} cusna_saom_multi_result;
+
+/* M chains of one multi-network period on the GPU (replaces the declaration at
+ * src/libcusna.h:280-285 and the CPU mirror cusna_saom_simulate_multi_cpu,
+ * src/libcusna_saom_cpu.cpp:427-604). Trajectories equal the CPU mirror's. */
+CUSNA_API cusna_status cusna_saom_simulate_multi(
+    const cusna_saom_multi_problem *problem, cusna_saom_multi_result *result);
+
+/* Cross-network statistic of M own end networks a_batch (M*n*n dense uint8)
+ * against the source network's period-start predictor wp (n*n dense uint8)
+ * for cross effect type t (33..37; parm: 36 takes square roots when >= 2),
+ * into out[M] (src/libcusna.h:366-374; CPU src/libcusna_saom_cpu.cpp:819-857).
+ * Computed on the GPU. */
+CUSNA_API cusna_status cusna_cross_stats(
+    const uint8_t *a_batch, const uint8_t *wp, int32_t n, int32_t M,
+    int32_t t, double parm, double *out);
+
 /* Measured float64 FMA throughput of the current device in TFLOP/s (an FMA
  * counts 2 flops): the peak against which the simulator's float64 work is
  * reported. Runs a short synthetic kernel. */

@@ -61,6 +61,14 @@ class Oracle:
         self._bs.argtypes = [vp, i32, i32, i32, vp, vp, vp, C.c_double, C.c_double,
                              C.c_double, vp]
         self._bs.restype = i32
+        from cusna_gb300.abi import MultiProblem, MultiResult
+        self._multi = getattr(self.lib, "oracle_simulate_multi" if kind == "port"
+                              else "cusna_saom_simulate_multi_cpu")
+        self._multi.argtypes = [C.POINTER(MultiProblem), C.POINTER(MultiResult)]
+        self._multi.restype = i32
+        self._cross = getattr(self.lib, "oracle_cross_stats" if kind == "port" else "cusna_cross_stats")
+        self._cross.argtypes = [vp, vp, i32, i32, i32, C.c_double, vp]
+        self._cross.restype = i32
         if kind == "port":
             self._ph = self.lib.oracle_philox4x32
             self._ph.argtypes = [vp, vp, vp]
@@ -81,6 +89,26 @@ class Oracle:
         if st != 0:
             raise RuntimeError(f"{self.kind} simulate_period status {st}")
         return result_dict(m)
+
+    def simulate_multi(self, m) -> dict:
+        """A marshalled multi-network period (cusna_gb300.glue.marshal_multi)."""
+        from cusna_gb300.glue import result_dict
+        st = self._multi(C.byref(m.problem), C.byref(m.result))
+        if st != 0:
+            raise RuntimeError(f"{self.kind} simulate_multi status {st}")
+        return result_dict(m)
+
+    def cross_stats(self, a_batch, wp, t, parm=0.0) -> np.ndarray:
+        a = np.ascontiguousarray(np.asarray(a_batch) != 0, dtype=np.uint8)
+        if a.ndim == 2:
+            a = a[None]
+        M, n = a.shape[0], a.shape[1]
+        w = np.ascontiguousarray(np.asarray(wp) != 0, dtype=np.uint8)
+        out = np.zeros(M)
+        st = self._cross(a.ctypes.data, w.ctypes.data, n, M, int(t), float(parm), out.ctypes.data)
+        if st != 0:
+            raise RuntimeError(f"{self.kind} cross_stats status {st}")
+        return out
 
     def simulate_batch(self, ms, threads: int = 0) -> list:
         """The engine interface of cusna_gb300.mom: one call per period."""

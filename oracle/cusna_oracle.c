@@ -780,3 +780,260 @@ int32_t oracle_max_threads(void) {
     return 1;
 #endif
 }
+
+/* ==== multi-network co-evolution: src/libcusna_saom_cpu.cpp:427-604 ======= */
+
+/* Cross-network change statistic of toggling i->j in the own network, reading
+ * the CURRENT dense state aw of the source network (ax: the own network, for
+ * type 37). src/libcusna_saom_cpu.cpp:431-444. */
+static double cross_change(int t, const uint8_t *aw, const uint8_t *ax, int n, int i, int j,
+                           double dl, double parm) {
+    switch (t) {
+        case 33: return dl * (double)aw[(size_t)i * n + j];
+        case 34: return dl * (double)aw[(size_t)j * n + i];
+        case 35: return dl * (double)(aw[(size_t)i * n + j] & aw[(size_t)j * n + i]);
+        case 36: {
+            long c = 0;
+            for (int h = 0; h < n; ++h)
+                if (aw[(size_t)i * n + h] && aw[(size_t)j * n + h]) ++c;
+            return dl * (parm >= 2.0 ? sqrt((double)c) : (double)c);
+        }
+        case 37: {
+            long c = 0;
+            for (int h = 0; h < n; ++h)
+                if (aw[(size_t)i * n + h] && ax[(size_t)h * n + j]) ++c;
+            return dl * (double)c;
+        }
+    }
+    return 0.0;
+}
+
+typedef struct {
+    int n, k, D, nact, need_tp;
+    const uint8_t *a0, *perm;                 /* D*n*n                          */
+    const double *lam, *th;                   /* M*D, M*k                       */
+    const int32_t *tid, *netof, *netref, *ety, *dyi, *symf, *act;
+    const double *wt, *p1, *p2, *vm, *dy;     /* dy: n*n or NULL                */
+    uint32_t k0, k1;
+} mctx;
+
+/* One unconditional multi-network chain. src/libcusna_saom_cpu.cpp:463-552. */
+static void run_chain_multi(const mctx *C, uint32_t chain, uint8_t *a, double *scores,
+                            double *rscores, double *ntim, long *steps) {
+    const int n = C->n, k = C->k, D = C->D;
+    const double *lam_d = C->lam + (size_t)chain * D;
+    const double *th = C->th + (size_t)chain * k;
+    long *indeg = calloc((size_t)D * n, sizeof(long)), *outdeg = calloc((size_t)D * n, sizeof(long));
+    long *msd = calloc((size_t)D, sizeof(long));
+    double *df = malloc((size_t)n * sizeof(double)), *wsum = malloc((size_t)k * sizeof(double));
+    double *dsb = calloc((size_t)n * k, sizeof(double));
+    uint8_t *okb = malloc((size_t)n);
+    int *tp = calloc((size_t)n, sizeof(int));
+    for (int d = 0; d < D; ++d)
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                uint8_t v = C->a0[((size_t)d * n + i) * n + j];
+                a[((size_t)d * n + i) * n + j] = v;
+                if (v) { indeg[(size_t)d * n + j]++; outdeg[(size_t)d * n + i]++; }
+            }
+    double lam_tot = 0.0;
+    for (int d = 0; d < D; ++d) lam_tot += lam_d[d];
+    for (int e = 0; e < k; ++e) scores[e] = 0.0;
+    long ms = 0;
+    double t = 0.0;
+    uint32_t rr[4];
+    for (;;) {
+        ph4((uint32_t)ms, chain, 0u, 0u, C->k0, C->k1, rr);
+        t += -log(unif(rr[0])) / ((double)C->nact * lam_tot);
+        if (t > 1.0) break;
+        double uv = unif(rr[1]) * lam_tot;
+        int d = 0;
+        double acc = lam_d[0];
+        while (d < D - 1 && uv >= acc) { d += 1; acc += lam_d[d]; }
+        long idx = (long)(unif(rr[2]) * C->nact);
+        if (idx >= C->nact) idx = C->nact - 1;
+        const int i = C->act[idx];
+        uint8_t *ad = a + (size_t)d * n * n;
+        const long *ind = indeg + (size_t)d * n, *outd = outdeg + (size_t)d * n;
+        if (C->need_tp) {
+            for (int h = 0; h < n; ++h) tp[h] = 0;
+            for (int x = 0; x < n; ++x)
+                if (ad[(size_t)i * n + x])
+                    for (int h = 0; h < n; ++h) tp[h] += ad[(size_t)x * n + h];
+        }
+        double gbest = -1e30, lmax = -1e30;
+        int jstar = i;
+        for (int j = 0; j < n; ++j) {
+            double f = 0.0;
+            int ok = 1;
+            if (j == i) {
+                for (int e = 0; e < k; ++e) dsb[(size_t)j * k + e] = 0.0;
+            } else if (!C->perm[((size_t)d * n + i) * n + j]) {
+                ok = 0;
+            } else {
+                const double dl = 1.0 - 2.0 * ad[(size_t)i * n + j];
+                for (int e = 0; e < k; ++e) {
+                    if (C->netof[e] != d) { dsb[(size_t)j * k + e] = 0.0; continue; }
+                    double dd;
+                    if (C->tid[e] >= 33) {
+                        dd = cross_change(C->tid[e], a + (size_t)C->netref[e] * n * n, ad, n, i, j,
+                                          dl, C->p1[e]);
+                    } else {
+                        const double dyw = (C->dy && C->dyi[e] >= 0)
+                                               ? C->dy[((size_t)C->dyi[e] * n + i) * n + j] : 0.0;
+                        dd = change_stat(C->tid[e], ad, n, ind, outd, 0, tp,
+                                         C->vm[(size_t)e * n + i], C->vm[(size_t)e * n + j], dyw,
+                                         C->p1[e], C->p2[e], i, j, dl, C->wt + (size_t)e * (n + 1));
+                    }
+                    if ((C->ety[e] == 1 && ad[(size_t)i * n + j] == 1) ||
+                        (C->ety[e] == 2 && ad[(size_t)i * n + j] == 0)) dd = 0.0;
+                    dsb[(size_t)j * k + e] = dd;
+                    f += th[e] * dd;
+                }
+            }
+            okb[j] = (uint8_t)ok;
+            df[j] = f;
+            if (ok && f > lmax) lmax = f;
+            ph4((uint32_t)ms, chain, 1u, (uint32_t)j, C->k0, C->k1, rr);
+            if (ok) {
+                const double g = f - log(-log(unif(rr[0])));
+                if (g > gbest || (g == gbest && j < jstar)) { gbest = g; jstar = j; }
+            }
+        }
+        double sume = 0.0;
+        for (int e = 0; e < k; ++e) wsum[e] = 0.0;
+        for (int j = 0; j < n; ++j)
+            if (okb[j]) {
+                const double w = exp(df[j] - lmax);
+                sume += w;
+                for (int e = 0; e < k; ++e) wsum[e] += w * dsb[(size_t)j * k + e];
+            }
+        for (int e = 0; e < k; ++e)
+            if (C->netof[e] == d) scores[e] += dsb[(size_t)jstar * k + e] - wsum[e] / sume;
+        ms++;
+        msd[d]++;
+        if (jstar != i) {
+            const int j = jstar;
+            const long dl = 1 - 2 * ad[(size_t)i * n + j];
+            indeg[(size_t)d * n + j] += dl;
+            outdeg[(size_t)d * n + i] += dl;
+            ad[(size_t)i * n + j] = (uint8_t)(1 - ad[(size_t)i * n + j]);
+            if (C->symf[d]) {
+                indeg[(size_t)d * n + i] += dl;
+                outdeg[(size_t)d * n + j] += dl;
+                ad[(size_t)j * n + i] = (uint8_t)(1 - ad[(size_t)j * n + i]);
+            }
+        }
+        if (ms >= ORACLE_MAX_STEPS) break;
+    }
+    for (int d = 0; d < D; ++d) rscores[d] = (double)msd[d] / lam_d[d] - (double)C->nact;
+    *ntim = t;
+    *steps = ms;
+    free(indeg); free(outdeg); free(msd); free(df); free(wsum); free(dsb); free(okb); free(tp);
+}
+
+/* Entry point. src/libcusna_saom_cpu.cpp:555-604 (composition restore is off
+ * there, as here). */
+cusna_status oracle_simulate_multi(const cusna_saom_multi_problem *pb,
+                                   cusna_saom_multi_result *r) {
+    if (!pb || !r) return CUSNA_ERR_NULL_ARG;
+    if (pb->struct_version != CUSNA_ABI_VERSION) return CUSNA_ERR_SHAPE;
+    const int n = pb->n, W = pb->W, k = pb->k, M = pb->M, D = pb->D;
+    if (n < 1 || n > CUSNA_MAX_N || W != (n + 31) / 32 || k < 1 || k > CUSNA_MAXEFF || M < 1 ||
+        D < 2 || D > CUSNA_MAXNET)
+        return CUSNA_ERR_SHAPE;
+    const size_t nn = (size_t)n * n;
+    uint8_t *a0 = malloc((size_t)D * nn), *perm = malloc((size_t)D * nn);
+    for (int d = 0; d < D; ++d) {
+        bits_to_dense(pb->x0_out + (size_t)d * n * W, n, W, a0 + (size_t)d * nn);
+        if (pb->perm) bits_to_dense(pb->perm + (size_t)d * n * W, n, W, perm + (size_t)d * nn);
+        else { memset(perm + (size_t)d * nn, 1, nn); offdiag(perm + (size_t)d * nn, n, 1); }
+    }
+    double *lam = malloc((size_t)M * D * sizeof(double)), *th = malloc((size_t)M * k * sizeof(double));
+    double *wt = calloc((size_t)k * (n + 1), sizeof(double)), *p1 = calloc((size_t)k, sizeof(double));
+    double *p2 = calloc((size_t)k, sizeof(double)), *vm = calloc((size_t)k * n, sizeof(double));
+    for (size_t q = 0; q < (size_t)M * D; ++q) lam[q] = pb->lam[q];
+    for (size_t q = 0; q < (size_t)M * k; ++q) th[q] = pb->theta[q];
+    if (pb->wtab) for (size_t q = 0; q < (size_t)k * (n + 1); ++q) wt[q] = pb->wtab[q];
+    for (int e = 0; e < k; ++e) { p1[e] = pb->p1 ? pb->p1[e] : 0.0; p2[e] = pb->p2 ? pb->p2[e] : 0.0; }
+    if (pb->vmat) for (size_t q = 0; q < (size_t)k * n; ++q) vm[q] = pb->vmat[q];
+    double *dy = NULL;
+    if (pb->dyc) { dy = malloc(nn * sizeof(double)); for (size_t q = 0; q < nn; ++q) dy[q] = pb->dyc[q]; }
+    int32_t *dyi = malloc((size_t)k * sizeof(int32_t)), *act = malloc((size_t)n * sizeof(int32_t));
+    for (int e = 0; e < k; ++e) dyi[e] = pb->dyc_idx ? pb->dyc_idx[e] : -1;
+    for (int i = 0; i < n; ++i) act[i] = pb->act ? pb->act[i] : i;
+    mctx C;
+    C.n = n; C.k = k; C.D = D; C.nact = pb->act ? pb->nact : n;
+    C.need_tp = 0;
+    for (int e = 0; e < k; ++e) if (pb->type_ids[e] == 5) C.need_tp = 1;
+    C.a0 = a0; C.perm = perm; C.lam = lam; C.th = th;
+    C.tid = pb->type_ids; C.netof = pb->netof; C.netref = pb->netref; C.ety = pb->etypes;
+    C.dyi = dyi; C.symf = pb->symf; C.act = act;
+    C.wt = wt; C.p1 = p1; C.p2 = p2; C.vm = vm; C.dy = dy;
+    C.k0 = (uint32_t)(pb->seed & 0xFFFFFFFFu); C.k1 = (uint32_t)(pb->seed >> 32);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < M; ++c) {
+        uint8_t *a = malloc((size_t)D * nn);
+        double *sc = malloc((size_t)k * sizeof(double)), *rs = malloc((size_t)D * sizeof(double));
+        double nt;
+        long st;
+        run_chain_multi(&C, (uint32_t)c, a, sc, rs, &nt, &st);
+        if (r->ntim) r->ntim[c] = nt;
+        if (r->steps) r->steps[c] = (int32_t)st;
+        if (r->rscores) for (int d = 0; d < D; ++d) r->rscores[(size_t)c * D + d] = (float)rs[d];
+        if (r->scores) for (int e = 0; e < k; ++e) r->scores[(size_t)c * k + e] = (float)sc[e];
+        if (r->a_ends) memcpy(r->a_ends + (size_t)c * D * nn, a, (size_t)D * nn);
+        free(a); free(sc); free(rs);
+    }
+    free(a0); free(perm); free(lam); free(th); free(wt); free(p1); free(p2); free(vm); free(dy);
+    free(dyi); free(act);
+    return CUSNA_OK;
+}
+
+/* Cross-network statistic of M own networks against the source predictor.
+ * src/libcusna_saom_cpu.cpp:819-857. */
+cusna_status oracle_cross_stats(const uint8_t *a_batch, const uint8_t *wp, int32_t n, int32_t M,
+                                int32_t t, double parm, double *out) {
+    if (!a_batch || !wp || !out || n < 1 || n > CUSNA_MAX_N || M < 1) return CUSNA_ERR_NULL_ARG;
+    const size_t nn = (size_t)n * n;
+    double *star = NULL;
+    if (t == 36) {
+        star = malloc(nn * sizeof(double));
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                long s = 0;
+                for (int h = 0; h < n; ++h) s += wp[(size_t)i * n + h] & wp[(size_t)j * n + h];
+                star[(size_t)i * n + j] = (parm >= 2.0) ? sqrt((double)s) : (double)s;
+            }
+    }
+    for (int c = 0; c < M; ++c) {
+        const uint8_t *a = a_batch + (size_t)c * nn;
+        double acc = 0.0;
+        switch (t) {
+            case 33: for (size_t q = 0; q < nn; ++q) acc += (a[q] & wp[q]); break;
+            case 34:
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < n; ++j) acc += (a[(size_t)i * n + j] & wp[(size_t)j * n + i]);
+                break;
+            case 35:
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < n; ++j)
+                        acc += (a[(size_t)i * n + j] & wp[(size_t)i * n + j] & wp[(size_t)j * n + i]);
+                break;
+            case 36: for (size_t q = 0; q < nn; ++q) if (a[q]) acc += star[q]; break;
+            case 37:
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < n; ++j) {
+                        if (!a[(size_t)i * n + j]) continue;
+                        long s = 0;
+                        for (int h = 0; h < n; ++h) s += wp[(size_t)i * n + h] & a[(size_t)h * n + j];
+                        acc += (double)s;
+                    }
+                break;
+            default: free(star); return CUSNA_ERR_UNSUPPORTED;
+        }
+        out[c] = acc;
+    }
+    free(star);
+    return CUSNA_OK;
+}

@@ -10,7 +10,10 @@ to the generator is detected instead of silently compared.
 
 Output: tests/golden/parity_<kind>_<seed>.npz with every output array of the
 reference call (stats, scores, ntim, dist, dist_stat, steps, behaviour and
-rate outputs, a_ends).
+rate outputs, a_ends); tests/golden/multi_<kind>_<seed>.npz, the same for the
+multi-network simulator (cusna_saom_simulate_multi_cpu) on the seeded cases of
+cusna_gb300.workloads.multi_case; tests/golden/cross_stats.npz, the reference's
+cusna_cross_stats on seeded networks.
 """
 from __future__ import annotations
 
@@ -54,6 +57,48 @@ def run_case(engine, c) -> dict:
     return engine.simulate(m)
 
 
+def multi_digest(case) -> str:
+    """Digest of a multi-network case's inputs (MultiInputs, seed, lam, theta)."""
+    inp, seed, lam, theta = case
+    h = hashlib.sha256()
+    for name in sorted(vars(inp)):
+        v = getattr(inp, name)
+        h.update(name.encode())
+        if v is None:
+            h.update(b"none")
+        else:
+            h.update(np.ascontiguousarray(np.asarray(v, dtype=np.float64)).tobytes())
+    h.update(repr(seed).encode())
+    for v in (lam, theta):
+        h.update(np.asarray(v, dtype=np.float64).tobytes())
+    return h.hexdigest()
+
+
+MULTI_M = 4
+
+
+def run_multi(engine, case) -> dict:
+    """One multi-network period on an engine with simulate_multi (the oracle's
+    two CPU engines or the GPU adapter of the tests)."""
+    from cusna_gb300.glue import marshal_multi
+    inp, seed, lam, theta = case
+    return engine.simulate_multi(marshal_multi(inp, MULTI_M, seed, lam, theta))
+
+
+def cross_case(seed: int, n: int = 37, M: int = 3):
+    """Own networks (M, n, n) and a source predictor (n, n) for the cross
+    statistics."""
+    r = np.random.Generator(np.random.PCG64(500 + seed))
+    a = (r.random((M, n, n)) < 0.12).astype(np.uint8)
+    w = (r.random((n, n)) < 0.15).astype(np.uint8)
+    for x in list(a) + [w]:
+        np.fill_diagonal(x, 0)
+    return a, w
+
+
+CROSS_TYPES = ((33, 0.0), (34, 0.0), (35, 0.0), (36, 1.0), (36, 2.0), (37, 0.0))
+
+
 def main() -> None:
     from oracle import Oracle, reference_available
     if not reference_available():
@@ -66,6 +111,21 @@ def main() -> None:
             path = os.path.join(HERE, f"parity_{kind}_{seed}.npz")
             np.savez_compressed(path, digest=np.array(case_digest(c)), **out)
             print(path, os.path.getsize(path))
+    for kind in WL.MULTI_KINDS:
+        for seed in SEEDS:
+            case = WL.multi_case(kind, seed=seed, M=MULTI_M)
+            out = run_multi(ref, case)
+            path = os.path.join(HERE, f"multi_{kind}_{seed}.npz")
+            np.savez_compressed(path, digest=np.array(multi_digest(case)), **out)
+            print(path, os.path.getsize(path))
+    cross = {}
+    for seed in SEEDS:
+        a, w = cross_case(seed)
+        for t, parm in CROSS_TYPES:
+            cross[f"s{seed}_t{t}_p{int(parm)}"] = ref.cross_stats(a, w, t, parm)
+    path = os.path.join(HERE, "cross_stats.npz")
+    np.savez_compressed(path, **cross)
+    print(path, os.path.getsize(path))
 
 
 if __name__ == "__main__":

@@ -14,19 +14,18 @@ from cusna_gb300 import workloads as WL
 from cusna_gb300.glue import marshal_period
 from tests.conftest import REFERENCE, ROOT
 
-PROBLEM_FIELDS = [f for f, _ in abi.SaomProblem._fields_]
-RESULT_FIELDS = [f for f, _ in abi.SaomResult._fields_]
+STRUCTS = [("cusna_saom_problem", abi.SaomProblem), ("cusna_saom_result", abi.SaomResult),
+           ("cusna_saom_multi_problem", abi.MultiProblem),
+           ("cusna_saom_multi_result", abi.MultiResult)]
 
 
 def c_offsets(include_dir: str) -> dict:
-    """sizeof/offsetof of both structs as a C compiler lays them out."""
+    """sizeof/offsetof of every ABI struct as a C compiler lays them out."""
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "libcusna.h"', "int main(void){"]
-    lines.append('printf("problem.size %zu\\n", sizeof(cusna_saom_problem));')
-    lines.append('printf("result.size %zu\\n", sizeof(cusna_saom_result));')
-    for f in PROBLEM_FIELDS:
-        lines.append(f'printf("problem.{f} %zu\\n", offsetof(cusna_saom_problem, {f}));')
-    for f in RESULT_FIELDS:
-        lines.append(f'printf("result.{f} %zu\\n", offsetof(cusna_saom_result, {f}));')
+    for cname, cls in STRUCTS:
+        lines.append(f'printf("{cname}.size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
     lines.append("return 0;}")
     with tempfile.TemporaryDirectory() as td:
         src = os.path.join(td, "off.c")
@@ -38,11 +37,11 @@ def c_offsets(include_dir: str) -> dict:
 
 
 def ctypes_offsets() -> dict:
-    d = {"problem.size": C.sizeof(abi.SaomProblem), "result.size": C.sizeof(abi.SaomResult)}
-    for f in PROBLEM_FIELDS:
-        d["problem." + f] = getattr(abi.SaomProblem, f).offset
-    for f in RESULT_FIELDS:
-        d["result." + f] = getattr(abi.SaomResult, f).offset
+    d = {}
+    for cname, cls in STRUCTS:
+        d[cname + ".size"] = C.sizeof(cls)
+        for f, _ in cls._fields_:
+            d[f"{cname}.{f}"] = getattr(cls, f).offset
     return d
 
 
