@@ -349,6 +349,88 @@ def batching_comparison(full_fit=False):
     return out
 
 
+def multi_comparison(args):
+    """The multi-network simulator (cusna_saom_simulate_multi) and estimator.
+    Throughput: M chains of a 2-network period with every cross-effect type,
+    through the C ABI with host buffers (median of 3 calls after 2 warm-up
+    calls), beside the reference CPU engine (cusna_saom_simulate_multi_cpu) on a
+    bounded sample of the chains. Fit: mom_estimate_multinet on a synthetic
+    2-network panel with the reference test's control settings, over the GPU
+    engine and over the CPU engine (the oracle's restatement of the simulator
+    and statistics), host wall clock, one fit each."""
+    from cusna_gb300 import sim
+    from cusna_gb300 import multinet as MN
+    from cusna_gb300 import effects as E
+    from cusna_gb300.glue import marshal_multi
+    M = 4096
+    inp, seed, lam, theta = WL.multi_case("cross", seed=1, n=200, M=M, D=2)
+    m = marshal_multi(inp, M, seed, lam, theta, want_ends=False)
+    for _ in range(2):
+        sim.simulate_multi(m)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        out = sim.simulate_multi(m)
+        ts.append(time.perf_counter() - t0)
+    steps = int(out["steps"].sum())
+    res = {"workload": "multi: D=2 networks, n=200 actors, wave-1 densities 0.06 and 0.08; per "
+                       "network density, recip, transTrip and the cross effects crprod, "
+                       "crprodRecip, crprodMutual, from, to of the other network (k=16); "
+                       f"rates {np.round(lam, 2).tolist()}; M={M} chains",
+           "metric": "ministeps/s", "unit": "ministeps/s",
+           "e2e": steps / float(np.median(ts)), "ministeps_per_call": steps,
+           "call_ms": 1e3 * float(np.median(ts))}
+    if not args.no_cpu_baseline:
+        import oracle
+        kind = "reference" if oracle.reference_available() else "port"
+        eng = oracle.Oracle(kind)
+        sample = 48
+        ms = marshal_multi(inp, sample, seed, lam, theta, want_ends=False)
+        t0 = time.perf_counter()
+        o = eng.simulate_multi(ms)
+        dt = time.perf_counter() - t0
+        st = int(o["steps"].sum())
+        res["cpu_baseline"] = {"value": st / dt, "unit": "ministeps/s",
+                               "cores": os.cpu_count() or 1, "kind": kind,
+                               "sample": f"{sample} of the {M} chains ({st} ministeps, {dt:.1f} s)"}
+    # the estimator
+    waves = WL.multinet_panel(sim.simulate_multi)
+    ctl = dict(firstg=0.4, nsub=2, n2=(15, 20), batch2=128, n1=300, n3=600, nD=300,
+               diagonalize=0.2, seed=11)
+    effs = [[E.cusna_effect("density"), E.cusna_effect("recip")] for _ in range(2)]
+    data = MN.saom_multinet_data(waves)
+    fit = MN.mom_estimate_multinet(data, effs, control=ctl)
+    res["fit"] = {"workload": "2 networks, n=50, 2 waves (wave 1 Bernoulli(0.045), wave 2 "
+                              "simulated at rates 5.3/7.5 and density/recip -2.15/2.3, "
+                              "-2.4/2.9); density and recip per network; unconditional",
+                  "gpu_s": fit.wall_time, "theta": np.round(fit.theta, 4).tolist(),
+                  "se": np.round(fit.se, 4).tolist(),
+                  "max_abs_tconv": float(np.abs(fit.tconv).max()),
+                  "control": {k: (list(v) if isinstance(v, tuple) else v) for k, v in ctl.items()}}
+    if not args.no_cpu_baseline:
+        import oracle
+
+        class CpuEngine:
+            def __init__(self):
+                self.o = oracle.Oracle("port")
+
+            def simulate_multi(self, mm):
+                return self.o.simulate_multi(mm)
+
+            def network_stats_batch(self, A, n, k, *desc):
+                return np.stack([self.o.network_stats(a, n, k, *desc) for a in A])
+
+            def cross_stats(self, A, wp, t, parm):
+                return self.o.cross_stats(A, wp, t, parm)
+
+        cf = MN.mom_estimate_multinet(data, effs, control=ctl, engine=CpuEngine())
+        res["fit"]["cpu_s"] = cf.wall_time
+        res["fit"]["cpu_engine"] = "oracle port (C restatement), all host threads"
+        res["fit"]["max_abs_theta_diff_over_se"] = float(np.max(np.abs(cf.theta - fit.theta)
+                                                                 / fit.se))
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -362,6 +444,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mom", action="store_true",
                     help="skip the MoM fit comparison (plain vs surrogate) on the n=300 panel")
+    ap.add_argument("--no-multi", action="store_true",
+                    help="skip the multi-network simulator and estimator measurement")
     ap.add_argument("--no-batching", action="store_true",
                     help="skip the multi-group round timing (batch calls vs replayed plans)")
     ap.add_argument("--c3-fit", action="store_true",
@@ -485,6 +569,12 @@ def main():
         except Exception as exc:   # the simulator line is reported regardless
             batching = {"error": f"{type(exc).__name__}: {exc}"}
 
+    multi = None
+    if not args.no_multi and ws == 1:
+        try:
+            multi = multi_comparison(args)
+        except Exception as exc:  # reported, never fatal to the headline line
+            multi = {"error": f"{type(exc).__name__}: {exc}"}
     mom_fit = None
     if not args.no_mom and ws == 1:
         try:
@@ -494,7 +584,8 @@ def main():
 
     clk = clocks.summary(local)
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
-    roofline = period_roofline(args.workload, n, inp.W, k, net_steps, kern_avg_ms, sm_count, clk)
+    roofline = period_roofline(args.workload, n, (n + 31) // 32, k, net_steps, kern_avg_ms, sm_count,
+                               clk)
     line = {
         "metric": "ministeps/s", "value": value, "unit": "ministeps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -510,6 +601,7 @@ def main():
         "wall_s_timed_region": t_wall,
         "mom_fit": mom_fit,
         "batching": batching,
+        "multi": multi,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

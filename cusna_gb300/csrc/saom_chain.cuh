@@ -291,9 +291,13 @@ __device__ __forceinline__ void block_lse(float *rec, float w, const float *d32,
 // exact float64 choice, and the chosen alter's float64 change statistics in
 // S.dstar. Returns j*. The log-sum-exp sums are left in S.red[32G + q] for the
 // score update. d (float64) and d32 are per-thread scratch of k values.
+// MULTI: the network is one of a multi-network problem's, whose network w has
+// its rows at rows0 + w*net_stride words (cross effects read them).
+template <bool MULTI>
 __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, const Slice &S,
                                           int i, long long ms, uint32_t chain, double *d,
-                                          float *d32) {
+                                          float *d32, const uint32_t *rows0 = nullptr,
+                                          size_t net_stride = 0) {
   const int n = P.n, W = P.W, k = P.k, L = T.L;
   step_helpers(T, P, S, i);
   StepCtx X;
@@ -304,6 +308,8 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   if (P.flags & F_NEED_RDEG)
     for (int w = 0; w < W; ++w) X.rdeg_i += __popc(S.rowsT[w * n + i] & S.colsT[w * n + i]);
   X.zvi = (P.flags & F_HAS_Z) ? __dsub_rn((double)S.z[i], P.zbar) : 0.0;
+  X.rows0 = rows0;
+  X.net_stride = net_stride;
   if (P.flags & F_HAS_STEP) {
     step_values(T, P, S, X);
     T.sync();
@@ -336,7 +342,7 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
       ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
       if (ok) {
         float absf = 0.f;
-        if (!stay) f = change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+        if (!stay) f = change_stats32<MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
         uint32_t ph[4];
         philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
         const float g = __fsub_rn(f, loglog_est(ph[0]));
@@ -392,7 +398,7 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
         double f = 0.0;
         if (j != i) {
           const int aij = bit_of(S.rowsT, n, i, j);
-          f = change_stats<true>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
+          f = change_stats<true, MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
         }
         uint32_t ph[4];
         philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
@@ -413,7 +419,7 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     } else {
       const int aij = bit_of(S.rowsT, n, i, jstar);
       const int aji = bit_of(S.colsT, n, i, jstar);
-      change_stats<false>(P, S, X, jstar, aij, aji, d);
+      change_stats<false, MULTI>(P, S, X, jstar, aij, aji, d);
       for (int e = 0; e < k; ++e) S.dstar[e] = d[e];
     }
   }
@@ -482,7 +488,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
       continue;
     }
 
-    const int jstar = net_choice(T, P, S, i, ms, chain, d, d32);
+    const int jstar = net_choice<false>(T, P, S, i, ms, chain, d, d32);
     const int aij_star = bit_of(S.rowsT, n, i, jstar);
     T.sync();
     if (T.tl < k) {

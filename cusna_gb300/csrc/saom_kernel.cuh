@@ -58,10 +58,6 @@ struct Slice {
   int *rnet, *rfocal; //   network/behaviour flag, focal actor,
   uint32_t *rr3;     //   behaviour uniform
   int *ekind, *ecfn, *eoffd, *eofft;  // k  effect plan
-  // multi-network teams: network d's rows/columns are rows0/cols0 + d*net_stride
-  // words (single network: rows0 = rowsT, cols0 = colsT)
-  const uint32_t *rows0, *cols0;
-  size_t net_stride;
   double *stepd, *stept;  // 4k  per-ministep K_STEP magnitudes and terms
   float *stepd32, *stept32;  // 4k  their float32 images
 };
@@ -134,9 +130,6 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   Slice s;
   s.rowsT = rows_global ? rows_global : (uint32_t *)(base + L.o_rows);
   s.colsT = cols_global ? cols_global : (uint32_t *)(base + L.o_cols);
-  s.rows0 = s.rowsT;
-  s.cols0 = s.colsT;
-  s.net_stride = 0;
   s.indeg = (short *)(base + L.o_indeg);
   s.outdeg = (short *)(base + L.o_outdeg);
   s.z = (int *)(base + L.o_z);
@@ -306,6 +299,9 @@ __device__ __forceinline__ int team_argmax(const Team &T, long long key, int j, 
 struct StepCtx {
   int i, od_i, id_i, rdeg_i;
   double zvi;
+  // multi-network teams: network w's rows are rows0 + w*net_stride words
+  const uint32_t *rows0;
+  size_t net_stride;
 };
 
 // Popcount of (A_word(a) & B_word(b)) summed over the W words.
@@ -446,9 +442,9 @@ __device__ __forceinline__ void step_values(const Team &T, const DevProblem &P, 
 // toggling i -> j in the own network for cross effect type t, reading network
 // w's current rows (src/libcusna_saom_cpu.cpp:431-444): 33 a_w[i][j], 34
 // a_w[j][i], 35 both, 36 |out_w(i) & out_w(j)|, 37 |out_w(i) & in_own(j)|.
-__device__ __forceinline__ int cross_count(const Slice &S, int n, int W, int t, int w, int i,
-                                           int j) {
-  const uint32_t *Rw = S.rows0 + (size_t)w * S.net_stride;
+__device__ __forceinline__ int cross_count(const Slice &S, const StepCtx &X, int n, int W, int t,
+                                           int w, int i, int j) {
+  const uint32_t *Rw = X.rows0 + (size_t)w * X.net_stride;
   switch (t) {
     case 33: return bit_of(Rw, n, i, j);
     case 34: return bit_of(Rw, n, j, i);
@@ -466,7 +462,9 @@ __device__ __forceinline__ int cross_count(const Slice &S, int n, int W, int t, 
   }
 }
 
-template <bool TERMS>
+// MULTI: the kernel serves multi-network problems (cross effects K_CROSS);
+// the single-network kernel compiles without that branch.
+template <bool TERMS, bool MULTI>
 __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice &S,
                                                const StepCtx &X, int j, int aij, int aji,
                                                double *d) {
@@ -538,8 +536,8 @@ __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice 
     } else if (kind == K_ZERO) {
       v = 0.0;
       has_term = false;
-    } else if (kind == K_CROSS) {
-      const int c = cross_count(S, n, W, cfn, S.eoffd[e], i, j);
+    } else if (MULTI && kind == K_CROSS) {
+      const int c = cross_count(S, X, n, W, cfn, S.eoffd[e], i, j);
       v = flip((cfn == 36 && S.p1[e] >= 2.0) ? sqrt(i2d(c)) : i2d(c), sg);
       if (TERMS) term = __dmul_rn(S.th[e], v);
     } else {
@@ -565,6 +563,7 @@ __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice 
 // interaction product, one in the product with theta) and the k additions add
 // at most (k-1)u absf, so |f32 - f| <= (k + 8) u absf for the float64 predictor
 // f of change_stats<true> (itself within 2^-50 absf of the exact sum).
+template <bool MULTI>
 __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice &S,
                                                 const StepCtx &X, int j, int aij, int aji,
                                                 float *d32, float *absf) {
@@ -635,8 +634,8 @@ __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice
     } else if (kind == K_ZERO) {
       v = 0.f;
       has_term = false;
-    } else if (kind == K_CROSS) {
-      const int c = cross_count(S, n, W, cfn, S.eoffd[e], i, j);
+    } else if (MULTI && kind == K_CROSS) {
+      const int c = cross_count(S, X, n, W, cfn, S.eoffd[e], i, j);
       const float m = (cfn == 36 && S.p1[e] >= 2.0) ? sqrtf((float)c) : (float)c;
       v = __uint_as_float(__float_as_uint(m) ^ sg);
       term = __fmul_rn(S.th32[e], v);

@@ -17,12 +17,8 @@ namespace cusna {
 __device__ __forceinline__ Slice multi_slice(unsigned char *base, const SliceLayout &lay, int d,
                                              uint32_t *cols_g, uint32_t *rows_g,
                                              size_t cols_words) {
-  Slice s = carve(base + (size_t)d * lay.bytes, lay, cols_g ? cols_g + (size_t)d * cols_words : nullptr,
-                  rows_g ? rows_g + (size_t)d * cols_words : nullptr);
-  s.rows0 = rows_g ? rows_g : (uint32_t *)(base + lay.o_rows);
-  s.cols0 = cols_g ? cols_g : (uint32_t *)(base + lay.o_cols);
-  s.net_stride = rows_g ? cols_words : lay.bytes / 4;
-  return s;
+  return carve(base + (size_t)d * lay.bytes, lay, cols_g ? cols_g + (size_t)d * cols_words : nullptr,
+               rows_g ? rows_g + (size_t)d * cols_words : nullptr);
 }
 
 __device__ void run_chain_multi(const Team &T, const DevProblem *nets, const MultiDev &md,
@@ -44,6 +40,10 @@ __device__ void run_chain_multi(const Team &T, const DevProblem *nets, const Mul
   double dbuf[24];
   float d32[24];
   const Slice S0 = multi_slice(base, lay, 0, cols_g, rows_g, cols_words);
+  // network w's rows: rows0 + w*net_stride words (in shared memory the slices
+  // follow one another; in global scratch each network has cols_words)
+  const uint32_t *rows0 = S0.rowsT;
+  const size_t net_stride = rows_g ? cols_words : lay.bytes / 4;
   for (;;) {
     const int slot = (int)(ms & 31);
     if (slot == 0) {
@@ -70,7 +70,7 @@ __device__ void run_chain_multi(const Team &T, const DevProblem *nets, const Mul
     const int d = S0.rnet[slot], i = S0.rfocal[slot];
     const DevProblem &P = nets[d];
     const Slice S = multi_slice(base, lay, d, cols_g, rows_g, cols_words);
-    const int jstar = net_choice(T, P, S, i, ms, chain, dbuf, d32);
+    const int jstar = net_choice<true>(T, P, S, i, ms, chain, dbuf, d32, rows0, net_stride);
     const int aij_star = bit_of(S.rowsT, n, i, jstar);
     T.sync();
     if (T.tl < P.k) {

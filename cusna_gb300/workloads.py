@@ -370,3 +370,28 @@ def multi_case(kind: str, seed: int = 0, n: int = 40, M: int = 4, D: int = 2):
                       dyc_idx=dyc_idx)
     lam = np.array([3.0 + 1.5 * d + r.uniform(0, 1) for d in range(D)])
     return inp, int(r.integers(1, 2 ** 62)), lam, np.array(th)
+
+
+# ---- multi-network panels ------------------------------------------------------
+# Two co-evolving networks on 50 actors with density and recip each, the shape
+# of the reference's multi-network estimation test; parameters near its fit.
+MN_LAMBDA = np.array([5.3, 7.5])
+MN_THETA = np.array([-2.15, 2.3, -2.4, 2.9])   # net0 density, recip, net1 density, recip
+
+
+def multinet_panel(simulate_multi, n: int = 50, seed: int = 12):
+    """Wave 1 of each network Bernoulli(0.045) (seeds 12, 13); wave 2 of both
+    simulated jointly at MN_LAMBDA, MN_THETA (Philox seed 31) through
+    simulate_multi (a marshalled multi-network period -> outputs). Returns the
+    waves of each network."""
+    from .glue import MultiInputs, marshal_multi
+    x0s = [bernoulli_net(n, 0.045, seed=seed + d) for d in range(2)]
+    specs = [E.make_effect_spec(nm) for nm in ("density", "recip")] * 2
+    pe = E.prepare_effects_v2(specs, n, 1, None, None)
+    inp = MultiInputs(x0s=x0s, type_ids=np.asarray(pe.type_ids, np.int32),
+                      netof=np.array([0, 0, 1, 1], np.int32), netref=E.effect_netrefs(specs),
+                      etypes=E.effect_etypes(specs), wtab=E.effect_wtabs(specs, n), p1=pe.p1,
+                      p2=pe.p2, vmat=pe.vmat, symf=np.zeros(2, np.int32))
+    out = simulate_multi(marshal_multi(inp, 1, 31, MN_LAMBDA, MN_THETA))
+    ends = np.asarray(out["a_ends"]).reshape(2, n, n)
+    return [[x0s[d].astype(np.int64), ends[d].astype(np.int64)] for d in range(2)]
