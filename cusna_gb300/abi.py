@@ -173,6 +173,10 @@ def load_library(path: str | None = None):
     lib.cusna_saom_simulate_multi.restype = i32
     lib.cusna_cross_stats.argtypes = [_p, _p, i32, i32, i32, C.c_double, _p]
     lib.cusna_cross_stats.restype = i32
+    lib.cusna_typed_stats.argtypes = [_p, i32, i32, i32, _p, _p, _p, _p, _p, _p, _p, _p, _p]
+    lib.cusna_typed_stats.restype = i32
+    lib.cusna_gof_distribution.argtypes = [_p, i32, i32, i32, _p, i32, _p]
+    lib.cusna_gof_distribution.restype = i32
     if path is None:
         _lib = lib
     return lib
@@ -189,7 +193,8 @@ EXPORTED_SYMBOLS = [
     "cusna_saom_plan_shape", "cusna_saom_plan_destroy",
     "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",
     "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_train_steps", "cusna_mlp_jacobian",
-    "cusna_saom_simulate_multi", "cusna_cross_stats",
+    "cusna_saom_simulate_multi", "cusna_cross_stats", "cusna_typed_stats",
+    "cusna_gof_distribution",
 ]
 
 # cusna_adam_hyper: int32 step, float lr, beta1, beta2, eps, c1, c2

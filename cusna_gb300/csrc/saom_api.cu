@@ -1582,6 +1582,85 @@ CUSNA_API cusna_status cusna_cross_stats(const uint8_t *a_batch, const uint8_t *
   return CUSNA_OK;
 }
 
+CUSNA_API cusna_status cusna_typed_stats(const uint8_t *a_batch, int32_t n, int32_t M,
+                                         int32_t etype, const double *F, const uint8_t *x0,
+                                         const uint8_t *keep, const uint8_t *force,
+                                         const uint8_t *keepS, const uint8_t *forceS,
+                                         const uint8_t *miss_m, const uint8_t *miss_m1,
+                                         double *out) {
+  g_err.clear();
+  // argument errors as the reference reports them (src/libcusna_saom_cpu.cpp:697)
+  if (!a_batch || !F || !x0 || !out || n < 1 || M < 1) {
+    set_err("a_batch, F, x0 and out are required; n >= 1, M >= 1");
+    return CUSNA_ERR_NULL_ARG;
+  }
+  cusna_status s = ensure_ctx();
+  if (s != CUSNA_OK) return s;
+  cudaStream_t st = g_ctx.stream;
+  const size_t nn = (size_t)n * n;
+  Planner pl;
+  const size_t oa = pl.take(nn * M), oF = pl.take(nn * 8), ox = pl.take(nn), oout = pl.take((size_t)M * 8);
+  const uint8_t *masks[6] = {keep, force, keepS, forceS, miss_m, miss_m1};
+  size_t om[6];
+  for (int q = 0; q < 6; ++q) om[q] = masks[q] ? pl.take(nn) : NONE;
+  if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
+  CU(cudaMemcpyAsync(at<char>(oa), a_batch, nn * M, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(oF), F, nn * 8, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(ox), x0, nn, cudaMemcpyHostToDevice, st));
+  const uint8_t *dm[6];
+  for (int q = 0; q < 6; ++q) {
+    dm[q] = nullptr;
+    if (om[q] == NONE) continue;
+    CU(cudaMemcpyAsync(at<char>(om[q]), masks[q], nn, cudaMemcpyHostToDevice, st));
+    dm[q] = at<uint8_t>(om[q]);
+  }
+  CU(launch_typed_stats(at<uint8_t>(oa), n, M, etype, at<double>(oF), at<uint8_t>(ox), dm[0],
+                        dm[1], dm[2], dm[3], dm[4], dm[5], at<double>(oout), st));
+  CU(cudaMemcpyAsync(out, at<char>(oout), (size_t)M * 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_gof_distribution(const uint8_t *a_batch, int32_t n, int32_t M,
+                                              int32_t kind, const int32_t *levls, int32_t nlev,
+                                              double *out) {
+  g_err.clear();
+  // argument errors as the reference reports them (src/libcusna_saom_cpu.cpp:719)
+  if (!a_batch || !levls || !out || n < 1 || M < 1 || nlev < 1) {
+    set_err("a_batch, levls and out are required; n >= 1, M >= 1, nlev >= 1");
+    return CUSNA_ERR_NULL_ARG;
+  }
+  if (kind < 0 || kind > 2) { set_err("gof kind %d", kind); return CUSNA_ERR_UNSUPPORTED; }
+  int maxlev = 0;
+  for (int L = 0; L < nlev; ++L) {
+    // a negative geodesic level indexes before the reference's count table
+    if (kind == 2 && levls[L] < 0) { set_err("geodesic level %d < 0", levls[L]); return CUSNA_ERR_SHAPE; }
+    maxlev = std::max(maxlev, (int)levls[L]);
+  }
+  // nothing changes beyond distance n - 1
+  const int K = kind == 2 ? std::min(maxlev, n - 1) : 0;
+  cusna_status s = ensure_ctx();
+  if (s != CUSNA_OK) return s;
+  cudaStream_t st = g_ctx.stream;
+  const size_t nn = (size_t)n * n;
+  const size_t cols = kind == 2 ? (size_t)nlev + 1 : (size_t)nlev;
+  Planner pl;
+  const size_t oa = pl.take(nn * M), ol = pl.take((size_t)nlev * 4), oout = pl.take((size_t)M * cols * 8);
+  const size_t words = gof_scratch_words(n, M, kind, K);
+  const size_t orow = words ? pl.take(words * 4) : NONE;
+  const size_t oadd = kind == 2 ? pl.take((size_t)M * (K + 1) * 8) : NONE;
+  if ((s = ensure_arena(pl.off)) != CUSNA_OK) return s;
+  CU(cudaMemcpyAsync(at<char>(oa), a_batch, nn * M, cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(at<char>(ol), levls, (size_t)nlev * 4, cudaMemcpyHostToDevice, st));
+  CU(launch_gof(at<uint8_t>(oa), n, M, kind, at<int>(ol), nlev, K,
+                orow == NONE ? nullptr : at<uint32_t>(orow),
+                oadd == NONE ? nullptr : at<unsigned long long>(oadd), at<double>(oout),
+                g_ctx.smem_optin, st));
+  CU(cudaMemcpyAsync(out, at<char>(oout), (size_t)M * cols * 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  return CUSNA_OK;
+}
+
 CUSNA_API cusna_status cusna_behavior_stats_gpu(const int32_t *z_batch, int32_t n, int32_t M,
                                                 int32_t kb, const int32_t *bty,
                                                 const uint8_t *xnet, const int32_t *bkdist,

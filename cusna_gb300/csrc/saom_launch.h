@@ -51,6 +51,22 @@ cudaError_t launch_multi(const LaunchShape &sh, const DevProblem *nets, const Mu
 cudaError_t launch_cross_stats(const uint8_t *a, const uint8_t *wp, int n, int M, int t,
                                double parm, uint32_t *ar, uint32_t *wr, double *out,
                                cudaStream_t st);
+// Rows of dense uint8 matrices (rows x n) packed into W words per row.
+cudaError_t launch_pack_rows(const uint8_t *a, long long rows, int n, int W, uint32_t *out,
+                             cudaStream_t st);
+// Typed (creation / endowment) statistic of M dense end networks.
+cudaError_t launch_typed_stats(const uint8_t *a, int n, int M, int etype, const double *F,
+                               const uint8_t *x0, const uint8_t *keep, const uint8_t *force,
+                               const uint8_t *keepS, const uint8_t *forceS,
+                               const uint8_t *miss_m, const uint8_t *miss_m1, double *out,
+                               cudaStream_t st);
+// sienaGOF distributions of M dense end networks (kind 0 in-degree, 1
+// out-degree, 2 geodesic with K = min(largest level, n - 1)); rows (M*n*W
+// words) and added (M*(K+1)) are scratch of the geodesic kind.
+size_t gof_scratch_words(int n, int M, int kind, int K);
+cudaError_t launch_gof(const uint8_t *a, int n, int M, int kind, const int *levls, int nlev,
+                       int K, uint32_t *rows, unsigned long long *added, double *out,
+                       int smem_optin, cudaStream_t st);
 
 // One theta-premultiplied term table of a plan's problem q, effect e (pool
 // offsets of the table and, for lookup tables, of its values).

@@ -255,6 +255,13 @@ __global__ void __launch_bounds__(256) cross_stats_kernel(const uint8_t *__restr
   }
 }
 
+cudaError_t launch_pack_rows(const uint8_t *a, long long rows, int n, int W, uint32_t *out,
+                             cudaStream_t st) {
+  const long long words = rows * W;
+  pack_rows_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a, rows, n, W, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cross_stats(const uint8_t *a, const uint8_t *wp, int n, int M, int t,
                                double parm, uint32_t *ar, uint32_t *wr, double *out,
                                cudaStream_t st) {

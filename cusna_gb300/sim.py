@@ -229,6 +229,48 @@ def cross_stats(a_batch, wp, t, parm=0.0) -> np.ndarray:
     return out
 
 
+def _u8(x):
+    return None if x is None else np.ascontiguousarray(np.asarray(x) != 0, dtype=np.uint8)
+
+
+def typed_stats(a_batch, etype, F, x0, keep=None, force=None, keepS=None, forceS=None,
+                miss_m=None, miss_m1=None) -> np.ndarray:
+    """Creation (etype 1) or endowment (2, negated) statistic of one typed
+    effect over end networks a_batch ((n,n) or (M,n,n)), on the GPU."""
+    lib = load_library()
+    a = _u8(a_batch)
+    if a.ndim == 2:
+        a = a[None]
+    M, n = a.shape[0], a.shape[1]
+    Fm = np.ascontiguousarray(np.asarray(F, dtype=np.float64))
+    arrs = [_u8(x0), _u8(keep), _u8(force), _u8(keepS), _u8(forceS), _u8(miss_m), _u8(miss_m1)]
+    P = [None if x is None else x.ctypes.data for x in arrs]
+    out = np.zeros(M)
+    st = lib.cusna_typed_stats(a.ctypes.data, n, M, int(etype), Fm.ctypes.data, *P,
+                               out.ctypes.data)
+    check(st, "cusna_typed_stats", lib)
+    return out
+
+
+def gof_distribution(a_batch, kind, levls) -> np.ndarray:
+    """sienaGOF auxiliary distribution of end networks a_batch ((n,n) or
+    (M,n,n)) on the GPU: kind 0 in-degree / 1 out-degree cumulative counts per
+    level, (M, len(levls)); kind 2 ordered pairs within each geodesic level and
+    the unreachable pairs, (M, len(levls) + 1)."""
+    lib = load_library()
+    a = _u8(a_batch)
+    if a.ndim == 2:
+        a = a[None]
+    M, n = a.shape[0], a.shape[1]
+    lv = np.ascontiguousarray(np.asarray(levls, dtype=np.int32))
+    cols = len(lv) + 1 if kind == 2 else len(lv)
+    out = np.zeros((M, cols))
+    st = lib.cusna_gof_distribution(a.ctypes.data, n, M, int(kind), lv.ctypes.data, len(lv),
+                                    out.ctypes.data)
+    check(st, "cusna_gof_distribution", lib)
+    return out
+
+
 def behavior_stats(z_batch, bty, xnet, bkdist, zbar, brange, bsimmean) -> np.ndarray:
     lib = load_library()
     z = np.ascontiguousarray(np.atleast_2d(np.asarray(z_batch, dtype=np.int32)))

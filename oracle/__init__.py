@@ -69,6 +69,13 @@ class Oracle:
         self._cross = getattr(self.lib, "oracle_cross_stats" if kind == "port" else "cusna_cross_stats")
         self._cross.argtypes = [vp, vp, i32, i32, i32, C.c_double, vp]
         self._cross.restype = i32
+        self._typed = getattr(self.lib, "oracle_typed_stats" if kind == "port" else "cusna_typed_stats")
+        self._typed.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        self._typed.restype = i32
+        self._gof = getattr(self.lib, "oracle_gof_distribution" if kind == "port"
+                            else "cusna_gof_distribution")
+        self._gof.argtypes = [vp, i32, i32, i32, vp, i32, vp]
+        self._gof.restype = i32
         if kind == "port":
             self._ph = self.lib.oracle_philox4x32
             self._ph.argtypes = [vp, vp, vp]
@@ -108,6 +115,35 @@ class Oracle:
         st = self._cross(a.ctypes.data, w.ctypes.data, n, M, int(t), float(parm), out.ctypes.data)
         if st != 0:
             raise RuntimeError(f"{self.kind} cross_stats status {st}")
+        return out
+
+    def typed_stats(self, a_batch, etype, F, x0, keep=None, force=None, keepS=None,
+                    forceS=None, miss_m=None, miss_m1=None) -> np.ndarray:
+        def u8(x):
+            return None if x is None else np.ascontiguousarray(np.asarray(x) != 0, dtype=np.uint8)
+        a = u8(a_batch)
+        if a.ndim == 2:
+            a = a[None]
+        M, n = a.shape[0], a.shape[1]
+        Fm = np.ascontiguousarray(np.asarray(F, dtype=np.float64))
+        arrs = [u8(x0), u8(keep), u8(force), u8(keepS), u8(forceS), u8(miss_m), u8(miss_m1)]
+        P = [None if x is None else x.ctypes.data for x in arrs]
+        out = np.zeros(M)
+        st = self._typed(a.ctypes.data, n, M, int(etype), Fm.ctypes.data, *P, out.ctypes.data)
+        if st != 0:
+            raise RuntimeError(f"{self.kind} typed_stats status {st}")
+        return out
+
+    def gof_distribution(self, a_batch, kind, levls) -> np.ndarray:
+        a = np.ascontiguousarray(np.asarray(a_batch) != 0, dtype=np.uint8)
+        if a.ndim == 2:
+            a = a[None]
+        M, n = a.shape[0], a.shape[1]
+        lv = np.ascontiguousarray(np.asarray(levls, dtype=np.int32))
+        out = np.zeros((M, len(lv) + 1 if kind == 2 else len(lv)))
+        st = self._gof(a.ctypes.data, n, M, int(kind), lv.ctypes.data, len(lv), out.ctypes.data)
+        if st != 0:
+            raise RuntimeError(f"{self.kind} gof_distribution status {st}")
         return out
 
     def simulate_batch(self, ms, threads: int = 0) -> list:

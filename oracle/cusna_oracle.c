@@ -8,7 +8,10 @@
  *   src/libcusna_saom_cpu.cpp:30-425  period simulator (Philox, change
  *                                     statistics, ministep loop, entry point)
  *   src/libcusna_saom_cpu.cpp:606-689 evaluation statistics of one network
+ *   src/libcusna_saom_cpu.cpp:691-765 typed statistics, GoF distributions
  *   src/libcusna_saom_cpu.cpp:767-817 behaviour statistics
+ *   src/libcusna_saom_cpu.cpp:427-604 multi-network simulator
+ *   src/libcusna_saom_cpu.cpp:819-857 cross-network statistics
  * Each function names the lines it follows. The restatement keeps the
  * reference's dense n*n uint8 layout, loop orders and float64 operation order
  * (so it reproduces the reference bit for bit), and therefore also its
@@ -1035,5 +1038,93 @@ cusna_status oracle_cross_stats(const uint8_t *a_batch, const uint8_t *wp, int32
         out[c] = acc;
     }
     free(star);
+    return CUSNA_OK;
+}
+
+/* Creation / endowment statistic of one typed effect over M end networks.
+ * src/libcusna_saom_cpu.cpp:691-714: creation sums F over gained ties of the
+ * statistic network ((a & keep) | force, not in x0, not missing at the start);
+ * endowment sums F over lost ties of the structural-only statistic network
+ * (in x0, not in (a & keepS) | forceS, not missing at the end) and is reported
+ * negated. NULL masks: keep/keepS all 1, force/forceS and the missing masks
+ * all 0. */
+cusna_status oracle_typed_stats(const uint8_t *a_batch, int32_t n, int32_t M, int32_t etype,
+                                const double *F, const uint8_t *x0, const uint8_t *keep,
+                                const uint8_t *force, const uint8_t *keepS,
+                                const uint8_t *forceS, const uint8_t *miss_m,
+                                const uint8_t *miss_m1, double *out) {
+    if (!a_batch || !F || !x0 || !out || n < 1 || M < 1) return CUSNA_ERR_NULL_ARG;
+    const size_t nn = (size_t)n * n;
+    for (int c = 0; c < M; ++c) {
+        const uint8_t *a = a_batch + (size_t)c * nn;
+        double s = 0.0;
+        for (size_t q = 0; q < nn; ++q) {
+            if (etype == 1) {
+                const int st = (a[q] & (keep ? keep[q] : 1)) | (force ? force[q] : 0);
+                if (st && !x0[q] && !(miss_m && miss_m[q])) s += F[q];
+            } else {
+                const int st = (a[q] & (keepS ? keepS[q] : 1)) | (forceS ? forceS[q] : 0);
+                if (x0[q] && !st && !(miss_m1 && miss_m1[q])) s += F[q];
+            }
+        }
+        out[c] = etype == 1 ? s : -s;
+    }
+    return CUSNA_OK;
+}
+
+/* sienaGOF auxiliary distributions. src/libcusna_saom_cpu.cpp:716-765.
+ * kind 0 / 1: per level L the number of actors whose in- / out-degree is at
+ * most levls[L]. kind 2: per level the number of ordered pairs i != j within
+ * geodesic distance levls[L] (reachability grown one step at a time from the
+ * network, the diagonal cleared after each step), then the unreachable pairs
+ * n(n-1) - (pairs within the largest level). */
+cusna_status oracle_gof_distribution(const uint8_t *a_batch, int32_t n, int32_t M, int32_t kind,
+                                     const int32_t *levls, int32_t nlev, double *out) {
+    if (!a_batch || !levls || !out || n < 1 || M < 1 || nlev < 1) return CUSNA_ERR_NULL_ARG;
+    const size_t nn = (size_t)n * n;
+    if (kind == 0 || kind == 1) {
+        int *deg = malloc((size_t)n * sizeof(int));
+        for (int c = 0; c < M; ++c) {
+            const uint8_t *a = a_batch + (size_t)c * nn;
+            memset(deg, 0, (size_t)n * sizeof(int));
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j)
+                    if (a[(size_t)i * n + j]) deg[kind == 0 ? j : i]++;
+            for (int L = 0; L < nlev; ++L) {
+                long cnt = 0;
+                for (int v = 0; v < n; ++v) cnt += deg[v] <= levls[L];
+                out[(size_t)c * nlev + L] = (double)cnt;
+            }
+        }
+        free(deg);
+        return CUSNA_OK;
+    }
+    if (kind != 2) return CUSNA_ERR_UNSUPPORTED;
+    int maxk = 0;
+    for (int L = 0; L < nlev; ++L) if (levls[L] > maxk) maxk = levls[L];
+    uint8_t *cur = malloc(nn), *nxt = malloc(nn);
+    long *within = calloc((size_t)maxk + 1, sizeof(long));
+    for (int c = 0; c < M; ++c) {
+        const uint8_t *a = a_batch + (size_t)c * nn;
+        for (size_t q = 0; q < nn; ++q) cur[q] = a[q] != 0;
+        for (int k = 1; k <= maxk; ++k) {
+            long cnt = 0;
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) cnt += i != j && cur[(size_t)i * n + j];
+            within[k] = cnt;
+            if (k == maxk) break;
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    uint8_t r = cur[(size_t)i * n + j];
+                    for (int m = 0; !r && m < n; ++m) r = cur[(size_t)i * n + m] && a[(size_t)m * n + j];
+                    nxt[(size_t)i * n + j] = r;
+                }
+            for (int i = 0; i < n; ++i) nxt[(size_t)i * n + i] = 0;
+            uint8_t *t = cur; cur = nxt; nxt = t;
+        }
+        for (int L = 0; L < nlev; ++L) out[(size_t)c * (nlev + 1) + L] = (double)within[levls[L]];
+        out[(size_t)c * (nlev + 1) + nlev] = (double)((long)n * (n - 1) - within[maxk]);
+    }
+    free(cur); free(nxt); free(within);
     return CUSNA_OK;
 }

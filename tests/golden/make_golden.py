@@ -13,7 +13,8 @@ reference call (stats, scores, ntim, dist, dist_stat, steps, behaviour and
 rate outputs, a_ends); tests/golden/multi_<kind>_<seed>.npz, the same for the
 multi-network simulator (cusna_saom_simulate_multi_cpu) on the seeded cases of
 cusna_gb300.workloads.multi_case; tests/golden/cross_stats.npz, the reference's
-cusna_cross_stats on seeded networks.
+cusna_cross_stats on seeded networks; tests/golden/gof_typed.npz, its
+cusna_gof_distribution and cusna_typed_stats on seeded networks.
 """
 from __future__ import annotations
 
@@ -99,6 +100,28 @@ def cross_case(seed: int, n: int = 37, M: int = 3):
 CROSS_TYPES = ((33, 0.0), (34, 0.0), (35, 0.0), (36, 1.0), (36, 2.0), (37, 0.0))
 
 
+def gof_case(seed: int, n: int, M: int = 3, p: float = 0.08):
+    """End networks (M, n, n) with a few self-ties, the start network x0, a
+    per-pair effect matrix F with a zero diagonal and six masks, for the typed
+    statistics and the GoF distributions."""
+    r = np.random.Generator(np.random.PCG64(900 + seed))
+    a = (r.random((M, n, n)) < p).astype(np.uint8)
+    for x in a:
+        x[np.arange(n), np.arange(n)] = r.random(n) < 0.05
+    x0 = (r.random((n, n)) < p).astype(np.uint8)
+    np.fill_diagonal(x0, 0)
+    F = np.round(r.standard_normal((n, n)), 4)
+    np.fill_diagonal(F, 0.0)
+    masks = {nm: (r.random((n, n)) < q).astype(np.uint8)
+             for nm, q in (("keep", 0.9), ("force", 0.05), ("keepS", 0.95), ("forceS", 0.03),
+                           ("miss_m", 0.05), ("miss_m1", 0.05))}
+    return a, x0, F, masks
+
+
+GOF_SIZES = (1, 2, 31, 33, 65)
+GOF_LEVELS = {0: [0, 1, 2, 3, 5, 8], 1: [0, 1, 2, 4, 6], 2: [1, 2, 3, 4, 6, 100]}
+
+
 def main() -> None:
     from oracle import Oracle, reference_available
     if not reference_available():
@@ -125,6 +148,17 @@ def main() -> None:
             cross[f"s{seed}_t{t}_p{int(parm)}"] = ref.cross_stats(a, w, t, parm)
     path = os.path.join(HERE, "cross_stats.npz")
     np.savez_compressed(path, **cross)
+    print(path, os.path.getsize(path))
+    gof = {}
+    for seed, n in enumerate(GOF_SIZES):
+        a, x0, F, masks = gof_case(seed, n)
+        for kind, lv in GOF_LEVELS.items():
+            gof[f"n{n}_gof{kind}"] = ref.gof_distribution(a, kind, lv)
+        for et in (1, 2):
+            gof[f"n{n}_typed{et}"] = ref.typed_stats(a, et, F, x0, **masks)
+            gof[f"n{n}_typed{et}_nomask"] = ref.typed_stats(a, et, F, x0)
+    path = os.path.join(HERE, "gof_typed.npz")
+    np.savez_compressed(path, **gof)
     print(path, os.path.getsize(path))
 
 
