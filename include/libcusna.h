@@ -371,6 +371,34 @@ CUSNA_API cusna_status cusna_cross_stats(
     const uint8_t *a_batch, const uint8_t *wp, int32_t n, int32_t M,
     int32_t t, double parm, double *out);
 
+/* Creation / endowment statistic of one typed effect over M end networks
+ * a_batch (M*n*n dense uint8), computed on the GPU (replaces
+ * src/libcusna.h:319-331; CPU src/libcusna_saom_cpu.cpp:691-714). etype 1
+ * (creation) sums F (n*n float64) over ties of (a & keep) | force absent from
+ * the start network x0 and not missing at the period start (miss_m); any other
+ * etype (endowment) sums F over ties of x0 absent from (a & keepS) | forceS and
+ * not missing at the end (miss_m1), and reports the sum negated. Masks are
+ * dense n*n uint8 and optional (NULL: keep/keepS all 1, the others all 0).
+ * out[M]. The sum is added in another order than the CPU engine's: equal
+ * within float64 rounding of the sum of |F|. */
+CUSNA_API cusna_status cusna_typed_stats(
+    const uint8_t *a_batch, int32_t n, int32_t M, int32_t etype,
+    const double *F, const uint8_t *x0,
+    const uint8_t *keep, const uint8_t *force,
+    const uint8_t *keepS, const uint8_t *forceS,
+    const uint8_t *miss_m, const uint8_t *miss_m1, double *out);
+
+/* sienaGOF auxiliary distributions of M end networks a_batch (M*n*n dense
+ * uint8), computed on the GPU (replaces src/libcusna.h:333-343; CPU
+ * src/libcusna_saom_cpu.cpp:716-765). kind 0 / 1: per level the number of
+ * actors with in- / out-degree at most levls[L], out is M*nlev. kind 2: per
+ * level the ordered pairs i != j within geodesic distance levls[L], then the
+ * unreachable pairs, out is M*(nlev+1); a negative geodesic level is
+ * CUSNA_ERR_SHAPE. Counts equal the CPU engine's. */
+CUSNA_API cusna_status cusna_gof_distribution(
+    const uint8_t *a_batch, int32_t n, int32_t M, int32_t kind,
+    const int32_t *levls, int32_t nlev, double *out);
+
 /* Measured float64 FMA throughput of the current device in TFLOP/s (an FMA
  * counts 2 flops): the peak against which the simulator's float64 work is
  * reported. Runs a short synthetic kernel. */
