@@ -270,7 +270,10 @@ def mom_fit_comparison(n3_check=True):
                             dict(mom.DEFAULT_CONTROL), engine=eng)
     centre = WL.c5_theta_true()
     # warm-up: one small simulation round and a tiny network fit
-    mom.mom_simulate(est, centre, 256, np.random.default_rng(0), eng)
+    for _ in range(3):
+        mom.mom_simulate(est, centre, 256, np.random.default_rng(0), eng)
+    from cusna_gb300 import sim as G
+    G.specialise_wait(900.0)   # the specialised period kernel of this model
     r = np.random.default_rng(0)
     S.MlpSurrogate(S.N_IN, est.k + 1, S.HIDDEN).fit(r.standard_normal((2048, S.N_IN)),
                                                       r.standard_normal((2048, est.k + 1)),
@@ -318,6 +321,10 @@ def batching_comparison(full_fit=False):
     est = mom.mom_estimator_groups(datas, effs, ctl, engine=eng)
     theta = np.array([-2.4, 1.9, 0.35, 0.45])
     rng = np.random.default_rng(1)
+    from cusna_gb300 import sim as G
+    for _ in range(3):
+        mom.mom_simulate(est, theta, 1, rng, mom.GpuEngine())
+    G.specialise_wait(900.0)   # the specialised period kernel of this model
     rounds = {}
     shape = None
     for name, engine in (("batch_calls", mom.GpuEngine()),
@@ -489,6 +496,14 @@ def main():
 
     # the library's autotuner times one candidate launch shape per call until it
     # settles (results do not depend on the shape); these calls are untimed
+    # the first calls also have the library compile the period kernel for this
+    # effect plan (NVRTC, in the background); it is waited for, then the tuner
+    # explores shapes again with the specialised kernel. Results are identical.
+    t_spec = time.perf_counter()
+    for _ in range(3):
+        step(G.options(device_ptrs=True, chain_offset=off, stream=stream.cuda_stream))
+    G.specialise_wait(900.0)
+    t_spec = time.perf_counter() - t_spec
     for _ in range(10):
         step(G.options(device_ptrs=True, chain_offset=off, stream=stream.cuda_stream))
     for _ in range(args.warmup):
@@ -496,7 +511,7 @@ def main():
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    kernel_ms, launches = [], []
+    kernel_ms, launches, specialised = [], [], []
     clk_path = os.path.join(tempfile.gettempdir(), f"cusna_clocks_{os.getpid()}.csv")
     barrier()
     torch.cuda.synchronize()
@@ -510,6 +525,7 @@ def main():
             ev[s][1].record(stream)
             kernel_ms.append(o.elapsed_ms)
             launches.append(o.launches)
+            specialised.append(o.specialised)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall0
     barrier()
@@ -595,7 +611,10 @@ def main():
                    "chains_per_gpu": M, "n": n, "effects": k,
                    "ministeps_per_step": all_ministeps,
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
-                   "parallelism": f"replicas x{ws}, chains sharded by chain offset"},
+                   "parallelism": f"replicas x{ws}, chains sharded by chain offset",
+                   "period_kernel": ("specialised to the effect plan (NVRTC, compiled before "
+                                     f"the timed steps in {t_spec:.1f} s)"
+                                     if all(specialised) else "library kernel")},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(sum(launches)), "clocks": clk,
         "wall_s_timed_region": t_wall,

@@ -90,6 +90,7 @@ class GpuOptions(C.Structure):
         ("chain_offset", C.c_uint32), ("warps_per_chain", C.c_int32),
         ("chains_per_cta", C.c_int32), ("launches", C.c_int32),
         ("stream", _p), ("elapsed_ms", C.c_double), ("ministeps", C.c_int64),
+        ("specialise", C.c_int32), ("specialised", C.c_int32),
     ]
 
 
@@ -177,6 +178,10 @@ def load_library(path: str | None = None):
     lib.cusna_typed_stats.restype = i32
     lib.cusna_gof_distribution.argtypes = [_p, i32, i32, i32, _p, i32, _p]
     lib.cusna_gof_distribution.restype = i32
+    lib.cusna_saom_specialise_check.argtypes = [P(SaomProblem), C.c_char_p, sz, P(C.c_double)]
+    lib.cusna_saom_specialise_check.restype = i32
+    lib.cusna_saom_specialise_wait.argtypes = [C.c_double, P(i32)]
+    lib.cusna_saom_specialise_wait.restype = i32
     if path is None:
         _lib = lib
     return lib
@@ -194,7 +199,7 @@ EXPORTED_SYMBOLS = [
     "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",
     "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_train_steps", "cusna_mlp_jacobian",
     "cusna_saom_simulate_multi", "cusna_cross_stats", "cusna_typed_stats",
-    "cusna_gof_distribution",
+    "cusna_gof_distribution", "cusna_saom_specialise_check", "cusna_saom_specialise_wait",
 ]
 
 # cusna_adam_hyper: int32 step, float lr, beta1, beta2, eps, c1, c2

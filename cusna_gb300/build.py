@@ -36,6 +36,35 @@ def nvcc() -> str:
     return path
 
 
+# device headers the run-time specialisation (csrc/saom_jit.cu) compiles with
+# NVRTC; they are embedded into the library as strings
+JIT_HEADERS = ["saom_common.cuh", "saom_kernel.cuh", "saom_stats.cuh", "saom_chain.cuh",
+               "saom_period.cuh"]
+
+
+def write_jit_sources(build_dir: str) -> None:
+    """Write build_dir/jit_sources.inc: the JIT headers as raw string literals
+    (rewritten only when their text changes)."""
+    delim = "cusnajit"
+    parts = ["// generated by cusna_gb300/build.py from csrc/: do not edit\n"]
+    for name in JIT_HEADERS:
+        text = open(os.path.join(CSRC, name)).read()
+        if ")" + delim + '"' in text:
+            raise RuntimeError(f"{name} contains the raw-string delimiter")
+        parts.append(f'static const char kJitSrc_{name.replace(".", "_")}[] = R"{delim}(' + text +
+                     f')' + delim + '";\n')
+    parts.append("static const int kJitHeaderCount = %d;\n" % len(JIT_HEADERS))
+    parts.append("static const char *const kJitHeaderNames[] = {" +
+                 ", ".join(f'"{n}"' for n in JIT_HEADERS) + "};\n")
+    parts.append("static const char *const kJitHeaderSources[] = {" +
+                 ", ".join(f'kJitSrc_{n.replace(".", "_")}' for n in JIT_HEADERS) + "};\n")
+    text = "".join(parts)
+    path = os.path.join(build_dir, "jit_sources.inc")
+    if not os.path.exists(path) or open(path).read() != text:
+        with open(path, "w") as f:
+            f.write(text)
+
+
 def sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
@@ -56,7 +85,8 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False,
                                                            os.path.basename(out).replace(".so", ""))
     os.makedirs(os.path.dirname(lib_path), exist_ok=True)
     os.makedirs(build_dir, exist_ok=True)
-    extra = list(extra_flags or [])
+    extra = list(extra_flags or []) + ["-I" + build_dir]
+    write_jit_sources(build_dir)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "libcusna.h"))
     srcs = sources()
@@ -79,7 +109,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False,
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _stale(lib_path, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib_path] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib_path] + objs + ["-lcudart", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "libcusna.h"
+#include "saom_jit.h"
 #include "saom_launch.h"
 #include "saom_stats.cuh"
 
@@ -111,7 +112,8 @@ T *at(size_t off) {
 
 // Per-problem host-side facts read during validation, and the effect plan.
 struct Facts {
-  std::vector<int> tid, i0, i1, i2, rk;
+  std::vector<int> tid, i0, i1, i2, rk, ety;
+  std::string spec;                        // effect plan of the specialised kernel (saom_jit.h)
   int flags = 0;
   std::vector<int> kind, cfn, offd, offt;  // effect plan, k each
   std::vector<int> tsize;                  // theta-table length per effect (0: none)
@@ -335,6 +337,7 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
   if ((s = fetch(p->int1, k, F.i1, -1)) != CUSNA_OK) return s;
   if ((s = fetch(p->int2, k, F.i2, -1)) != CUSNA_OK) return s;
   if ((s = fetch(p->rkind, p->nrate, F.rk, 0)) != CUSNA_OK) return s;
+  if ((s = fetch(p->etypes, k, F.ety, 0)) != CUSNA_OK) return s;
   if (p->act) {
     std::vector<int> act;
     if ((s = fetch(p->act, p->nact, act, 0)) != CUSNA_OK) return s;
@@ -373,6 +376,14 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
   }
   F.flags = fl;
   if ((s = build_plan(p, dev, F, one_row)) != CUSNA_OK) return s;
+  if (!F.multi) {
+    JitPlan J;
+    J.pc_flags = F.flags & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ |
+                            F_PC_RICIRJ);
+    J.kind = F.kind; J.cfn = F.cfn; J.tid = F.tid; J.ety = F.ety;
+    J.i0 = F.i0; J.i1 = F.i1; J.i2 = F.i2;
+    F.spec = jit_spec_source(J);
+  }
   // gwdsp change statistics index the weight table at p+1 with p <= n-2 on a
   // network without self-ties; a self-tie in the start network could push p to
   // n and read past the table, so such problems are rejected
@@ -706,7 +717,8 @@ cusna_status fetch_outputs(Job &J) {
 // smaller teams (fewer barriers) and to in-rows in shared memory.
 std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp,
                                      bool gw, bool tq, long long total_units, int force_G,
-                                     int force_tpc, int nets = 1) {
+                                     int force_tpc, int nets = 1,
+                                     const JitKernel *jk = nullptr) {
   const Ctx &c = g_ctx;
   std::vector<std::pair<double, LaunchShape>> all;
   const int Gs[5] = {1, 2, 4, 8, 16};
@@ -730,7 +742,8 @@ std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, in
         const size_t dyn = sh.lay.bytes * nets * tpc;
         if (dyn > (size_t)c.smem_optin) continue;
         const int per_sm = nets > 1 ? multi_blocks_per_sm(threads, dyn)
-                                    : period_blocks_per_sm(threads, dyn);
+                           : (jk ? jit_blocks_per_sm(*jk, threads, dyn)
+                                 : period_blocks_per_sm(threads, dyn));
         if (per_sm < 1) continue;
         const double teams_sm = (double)per_sm * tpc;
         const double chains_sm = (double)total_units / c.sms;
@@ -789,12 +802,24 @@ bool tuning_enabled() {
 }
 
 TuneKey tune_key(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bool gw, bool tq,
-                 long long units) {
+                 long long units, bool jit = false) {
   TuneKey k;
   std::memset(&k, 0, sizeof k);
   k.dev = g_ctx.device; k.nmax = nmax; k.Wmax = Wmax; k.kmax = kmax; k.kbmax = kbmax;
-  k.nrmax = nrmax; k.flags = (tp ? 1 : 0) | (gw ? 2 : 0) | (tq ? 4 : 0); k.units = units;
+  k.nrmax = nrmax; k.flags = (tp ? 1 : 0) | (gw ? 2 : 0) | (tq ? 4 : 0) | (jit ? 8 : 0);
+  k.units = units;
   return k;
+}
+
+// The specialised kernel of a launch: every problem must have the same effect
+// plan. spec_mode: 0 as CUSNA_JIT says, -1 never, 1 compile now if needed.
+bool jit_for(const std::vector<Job> &jobs, int spec_mode, JitKernel *jk) {
+  if (spec_mode < 0 || jobs.empty() || jobs[0].F.spec.empty()) return false;
+  for (const Job &J : jobs)
+    if (J.F.spec != jobs[0].F.spec) return false;
+  // spec_mode 1: compile and load now (tests, and callers that know the
+  // effect plan will run long enough)
+  return jit_get(jobs[0].F.spec, jk, spec_mode > 0);
 }
 
 // the model's two best shapes of each team size, in the model's order
@@ -872,8 +897,11 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
     total += J.p->M;
   }
   const int fG = opts ? opts->warps_per_chain : 0, fT = opts ? opts->chains_per_cta : 0;
+  JitKernel jk;
+  const bool use_jit = jit_for(jobs, opts ? opts->specialise : 0, &jk);
   const std::vector<LaunchShape> ranked =
-      rank_shapes(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, fG, fT);
+      rank_shapes(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, fG, fT, 1,
+                  use_jit ? &jk : nullptr);
   if (ranked.empty()) {
     set_err("no launch shape fits n=%d in shared memory", nmax);
     return CUSNA_ERR_UNSUPPORTED;
@@ -881,7 +909,7 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
   // a forced shape is used as given; otherwise the autotuner picks (and may be
   // timing one of its candidates in this call)
   int trial = -1;
-  const TuneKey tkey = tune_key(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total);
+  const TuneKey tkey = tune_key(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, use_jit);
   const LaunchShape sh = (fG || fT) ? ranked[0] : tuner_pick(tkey, tuning_candidates(ranked), &trial);
   Planner pl;
   for (auto &J : jobs) plan_problem(pl, J, dev);
@@ -906,10 +934,16 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
                      cudaMemcpyHostToDevice, st));
   CU(cudaMemsetAsync(at<char>(o_counter), 0, sizeof(unsigned long long), st));
   CU(cudaEventRecord(g_ctx.ev0, st));
-  CU(launch_period(sh, at<DevProblem>(o_probs), at<long long>(o_units), (int)jobs.size(), total,
-                   at<unsigned long long>(o_counter),
-                   o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
-                   o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
+  if (use_jit)
+    CU(launch_period_jit(jk, sh, at<DevProblem>(o_probs), at<long long>(o_units), (int)jobs.size(),
+                         total, at<unsigned long long>(o_counter),
+                         o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
+                         o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
+  else
+    CU(launch_period(sh, at<DevProblem>(o_probs), at<long long>(o_units), (int)jobs.size(), total,
+                     at<unsigned long long>(o_counter),
+                     o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
+                     o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
   CU(cudaEventRecord(g_ctx.ev1, st));
   if (!dev)
     for (auto &J : jobs)
@@ -923,6 +957,7 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
     opts->warps_per_chain = sh.G;
     opts->chains_per_cta = sh.teams_per_cta;
     opts->launches = (int32_t)(kernel_launches() - launches0);
+    opts->specialised = use_jit ? 1 : 0;
   }
   return CUSNA_OK;
 }
@@ -1177,6 +1212,10 @@ struct cusna_saom_plan {
   size_t trial = 0;
   bool pending = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the specialised kernel of the plan's effect plan, once it is available
+  std::string spec;
+  bool jit = false;
+  cusna::JitKernel jk;
 };
 
 namespace cusna {
@@ -1322,6 +1361,9 @@ cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *
   P->cols = o_cols == NONE ? nullptr : at<uint32_t>(o_cols);
   P->rows = o_rows == NONE ? nullptr : at<uint32_t>(o_rows);
   P->cols_words = cols_words;
+  bool same = true;
+  for (auto &J : jobs) same = same && J.F.spec == jobs[0].F.spec;
+  if (same) P->spec = jobs[0].F.spec;
   *out = P;
   return CUSNA_OK;
 }
@@ -1331,9 +1373,14 @@ cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *
 cusna_status plan_enqueue(cusna_saom_plan *P, const LaunchShape &sh, cudaStream_t st) {
   CU(launch_plan_prologue(P->probs, P->seeds, P->count, P->epoch, P->tabs, P->n_tabs, st));
   CU(cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), st));
-  CU(launch_period(sh, P->probs, P->units, P->count, P->total, P->counter,
-                   sh.cols_in_smem ? nullptr : P->cols, sh.rows_in_smem ? nullptr : P->rows,
-                   P->cols_words, st));
+  if (P->jit)
+    CU(launch_period_jit(P->jk, sh, P->probs, P->units, P->count, P->total, P->counter,
+                         sh.cols_in_smem ? nullptr : P->cols, sh.rows_in_smem ? nullptr : P->rows,
+                         P->cols_words, st));
+  else
+    CU(launch_period(sh, P->probs, P->units, P->count, P->total, P->counter,
+                     sh.cols_in_smem ? nullptr : P->cols, sh.rows_in_smem ? nullptr : P->rows,
+                     P->cols_words, st));
   return CUSNA_OK;
 }
 
@@ -1357,6 +1404,21 @@ cusna_status plan_launch(cusna_saom_plan *P, cudaStream_t st, bool graph) {
   }
   cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
   CU(cudaStreamIsCapturing(st, &cap_status));
+  if (!P->jit && !P->pending && !P->spec.empty() && cap_status == cudaStreamCaptureStatusNone &&
+      jit_get(P->spec, &P->jk)) {
+    // the specialised kernel is ready: time the candidate shapes again with it
+    // and capture a new graph (same smem layout, so every candidate fits the
+    // plan's scratch)
+    P->jit = true;
+    if (P->cand.size() > 1) {
+      P->trial = 0;
+      P->cand_ms.assign(P->cand.size(), INFINITY);
+    }
+    if (P->graph) {
+      cudaGraphExecDestroy(P->graph);
+      P->graph = nullptr;
+    }
+  }
   if (P->trial < P->cand.size() && cap_status == cudaStreamCaptureStatusNone) {
     const LaunchShape sh = P->cand[P->trial];
     CU(cudaEventRecord(P->ev0, st));
@@ -1428,6 +1490,38 @@ CUSNA_API cusna_status cusna_saom_simulate_batch(const cusna_saom_problem *probl
                                                  cusna_gpu_options *opts) {
   g_err.clear();
   return simulate(problems, results, count, opts);
+}
+
+CUSNA_API cusna_status cusna_saom_specialise_check(const cusna_saom_problem *problem, char *log,
+                                                   size_t log_len, double *seconds) {
+  g_err.clear();
+  if (!problem) { set_err("problem is NULL"); return CUSNA_ERR_NULL_ARG; }
+  cusna_saom_result dummy;
+  std::memset(&dummy, 0, sizeof dummy);
+  dummy.struct_version = CUSNA_ABI_VERSION;
+  Facts F;
+  cusna_status s = validate(problem, &dummy, false, F);
+  if (s != CUSNA_OK) return s;
+  std::string text;
+  double sec = 0.0;
+  const int st = jit_compile_only(F.spec, &text, &sec);
+  if (seconds) *seconds = sec;
+  if (log && log_len) {
+    const size_t m = std::min(log_len - 1, text.size());
+    std::memcpy(log, text.data(), m);
+    log[m] = 0;
+  }
+  if (st != 0) {
+    set_err("specialised kernel did not compile: %.400s", text.c_str());
+    return CUSNA_ERR_UNSUPPORTED;
+  }
+  return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_saom_specialise_wait(double seconds, int32_t *compiled) {
+  const int c = jit_wait(seconds);
+  if (compiled) *compiled = c;
+  return CUSNA_OK;
 }
 
 CUSNA_API cusna_status cusna_saom_simulate_multi(const cusna_saom_multi_problem *problem,

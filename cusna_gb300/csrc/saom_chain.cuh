@@ -342,7 +342,12 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
       ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
       if (ok) {
         float absf = 0.f;
+#ifdef CUSNA_JIT_SPEC
+        // the effect plan compiled in (saom_jit.cu): the same float32 values
+        if (!stay) f = jit_change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+#else
         if (!stay) f = change_stats32<MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+#endif
         uint32_t ph[4];
         philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
         const float g = __fsub_rn(f, loglog_est(ph[0]));
@@ -360,9 +365,14 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     const float w = ok ? expf(__fsub_rn(f, mb)) : 0.f;
     float *rec = S.blk + (size_t)(jb >> 5) * (k + 2);
     if (T.lane == 0) rec[0] = mb;
+#ifdef CUSNA_JIT_SPEC
+    block_lse<(CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))>(
+        rec + 1, w, d32, ok && !stay, CUSNA_JIT_K, T.lane);
+#else
     if (k + 1 <= 8) block_lse<8>(rec + 1, w, d32, ok && !stay, k, T.lane);
     else if (k + 1 <= 16) block_lse<16>(rec + 1, w, d32, ok && !stay, k, T.lane);
     else block_lse<32>(rec + 1, w, d32, ok && !stay, k, T.lane);
+#endif
   }
   T.sync();
   // blocks combined in order: lane q <= k forms quantity q (0: sum of

@@ -1,8 +1,20 @@
 // saom_common.cuh -- device-side problem descriptor and small helpers of the
 // GB300 SAOM period simulator.
 #pragma once
+#ifdef __CUDACC_RTC__
+// compiled at run time by NVRTC (saom_jit.cu): device code only, no host headers
+typedef unsigned int uint32_t;
+typedef int int32_t;
+typedef unsigned long long uint64_t;
+typedef long long int64_t;
+typedef unsigned char uint8_t;
+typedef unsigned short uint16_t;
+typedef unsigned long long uintptr_t;
+#define INFINITY __int_as_float(0x7f800000)
+#else
 #include <cstdint>
 #include <cuda_runtime.h>
+#endif
 
 namespace cusna {
 

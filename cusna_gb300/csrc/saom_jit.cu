@@ -1,0 +1,450 @@
+// saom_jit.cu -- run-time specialisation of the period kernel to one effect
+// plan: source generation, NVRTC compilation in a background thread, module
+// loading and launch through driver entry points. See saom_jit.h.
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "saom_jit.h"
+#include "jit_sources.inc"   // kJitHeaderNames / kJitHeaderSources (build.py)
+
+namespace cusna {
+
+// ---- generated source --------------------------------------------------------
+// Each effect becomes the branch of change_stats32 (saom_kernel.cuh) that its
+// kind selects, with the kind, count function, type, creation/endowment type
+// and interaction components as constants. Offsets, theta and every table stay
+// run-time values, so one compiled plan serves every problem with that plan.
+std::string jit_spec_source(const JitPlan &J) {
+  const int k = (int)J.kind.size();
+  const int fl = J.pc_flags;
+  std::string s;
+  char buf[512];
+  auto put = [&](const char *fmt, auto... a) {
+    std::snprintf(buf, sizeof buf, fmt, a...);
+    s += buf;
+  };
+  put("#define CUSNA_JIT_SPEC 1\n#define CUSNA_JIT_K %d\nnamespace cusna {\n", k);
+  s += "__device__ __forceinline__ float jit_change_stats32(const DevProblem &P, const Slice &S,\n"
+       "    const StepCtx &X, int j, int aij, int aji, float *d32, float *absf) {\n"
+       "  const int n = P.n, W = P.W, i = X.i;\n"
+       "  (void)n; (void)W; (void)i; (void)aji;\n"
+       "  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;\n"
+       "  (void)ri_cj; (void)ri_rj; (void)rj_ci; (void)ci_cj; (void)ci_rj; (void)ricirj;\n";
+  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
+    s += "  for (int w = 0; w < W; ++w) {\n"
+         "    const uint32_t ri = S.rowsT[w * n + i], rj = S.rowsT[w * n + j];\n"
+         "    const uint32_t ci = S.colsT[w * n + i], cj = S.colsT[w * n + j];\n"
+         "    (void)ri; (void)rj; (void)ci; (void)cj;\n";
+    if (fl & F_PC_RI_CJ) s += "    ri_cj += __popc(ri & cj);\n";
+    if (fl & F_PC_RI_RJ) s += "    ri_rj += __popc(ri & rj);\n";
+    if (fl & F_PC_RJ_CI) s += "    rj_ci += __popc(rj & ci);\n";
+    if (fl & F_PC_CI_CJ) s += "    ci_cj += __popc(ci & cj);\n";
+    if (fl & F_PC_CI_RJ) s += "    ci_rj += __popc(ci & rj);\n";
+    if (fl & F_PC_RICIRJ) s += "    ricirj += __popc(ri & ci & rj);\n";
+    s += "  }\n";
+  }
+  s += "  const uint32_t sg = aij ? 0x80000000u : 0u;\n"
+       "  float f = 0.f, a = 0.f;\n";
+  for (int e = 0; e < k; ++e) {
+    const int kind = J.kind[e], cfn = J.cfn[e], t = J.tid[e];
+    put("  {  // effect %d: type %d, kind %d, function %d\n", e, t, kind, cfn);
+    s += "    float v, term = 0.f;\n    bool has_term = true;\n";
+    if (kind == K_CNT) {
+      switch (cfn) {
+        case 0: s += "    const int c = 1;\n"; break;
+        case 1: s += "    const int c = aji;\n"; break;
+        case 2: s += "    const int c = ri_cj + ri_rj;\n"; break;
+        case 3: s += "    const int c = rj_ci;\n"; break;
+        case 4: s += "    const int c = S.indeg[j] + 1 - aij;\n"; break;
+        case 5:
+          s += "    int c = 0;\n"
+               "    const uint32_t *eq = S.tpeq + (aij ? W : 0);\n"
+               "    for (int w = 0; w < W; ++w)\n"
+               "      c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);\n"
+               "    if (S.tp[j] > 0) ++c;\n";
+          break;
+        case 6: s += "    const int c = (aji ? ri_cj : 0) + ricirj;\n"; break;
+        default: s += "    const int c = S.outdeg[j];\n"; break;
+      }
+      put("    v = __uint_as_float(__float_as_uint((float)c) ^ sg);\n"
+          "    term = __fmul_rn(S.th32[%d], v);\n", e);
+    } else if (kind == K_LOOK) {
+      switch (cfn) {
+        case 4: s += "    const int idx = S.indeg[j] + 1 - aij;\n"; break;
+        case 7: s += "    const int idx = S.outdeg[j];\n"; break;
+        case 8: s += "    const int idx = ri_cj;\n"; break;
+        case 9: s += "    const int idx = ri_rj;\n"; break;
+        case 10: s += "    const int idx = ci_cj;\n"; break;
+        case 11: s += "    const int idx = ci_rj;\n"; break;
+        case 12: s += "    const int idx = j;\n"; break;
+        case 13: s += "    const int idx = S.z[j] - P.zlo;\n"; break;
+        case 14: s += "    const int idx = i * n + j;\n"; break;
+        default: s += "    const int idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo);\n"; break;
+      }
+      put("    v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[%d] + idx]) ^ sg);\n"
+          "    term = __fmul_rn(S.th32[%d], v);\n", e, e);
+    } else if (kind == K_STEP) {
+      put("    const int q = 2 * aij + aji;\n"
+          "    v = S.stepd32[%d + q];\n    term = S.stept32[%d + q];\n", 4 * e, 4 * e);
+    } else if (kind == K_ZERO) {
+      s += "    v = 0.f;\n    has_term = false;\n";
+    } else if (t == 32) {
+      const int c2 = J.i2[e];
+      put("    v = __fmul_rn(d32[%d], d32[%d]);\n", J.i0[e], J.i1[e]);
+      if (c2 >= 0) put("    v = __fmul_rn(v, d32[%d]);\n", c2);
+      else s += "    if (aij) v = -v;\n";
+      put("    term = __fmul_rn(S.th32[%d], v);\n", e);
+    } else {
+      put("    v = (float)gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj,\n"
+          "                        nullptr);\n    term = __fmul_rn(S.th32[%d], v);\n", e, e);
+    }
+    if (J.ety[e] == 1) s += "    if (aij) { v = 0.f; has_term = false; }\n";
+    else if (J.ety[e] == 2) s += "    if (!aij) { v = 0.f; has_term = false; }\n";
+    put("    d32[%d] = v;\n", e);
+    s += "    if (has_term) {\n      f = __fadd_rn(f, term);\n      a = __fadd_rn(a, fabsf(term));\n"
+         "    }\n  }\n";
+  }
+  s += "  *absf = a;\n  return f;\n}\n}  // namespace cusna\n";
+  return s;
+}
+
+namespace {
+
+// ---- NVRTC, loaded at run time (the library has no link-time dependency) -----
+struct Nvrtc {
+  bool ok = false;
+  decltype(&nvrtcCreateProgram) create = nullptr;
+  decltype(&nvrtcAddNameExpression) add_name = nullptr;
+  decltype(&nvrtcCompileProgram) compile = nullptr;
+  decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+  decltype(&nvrtcGetProgramLog) get_log = nullptr;
+  decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+  decltype(&nvrtcGetCUBIN) get_cubin = nullptr;
+  decltype(&nvrtcGetLoweredName) lowered = nullptr;
+  decltype(&nvrtcDestroyProgram) destroy = nullptr;
+};
+
+Nvrtc load_nvrtc() {
+  Nvrtc N;
+  const char *names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
+                         "/usr/local/cuda/lib64/libnvrtc.so"};
+  void *h = nullptr;
+  for (const char *nm : names)
+    if ((h = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
+  if (!h) return N;
+  bool ok = true;
+  auto sym = [&](auto &fp, const char *name) {
+    fp = reinterpret_cast<std::remove_reference_t<decltype(fp)>>(dlsym(h, name));
+    ok = ok && fp != nullptr;
+  };
+  sym(N.create, "nvrtcCreateProgram");
+  sym(N.add_name, "nvrtcAddNameExpression");
+  sym(N.compile, "nvrtcCompileProgram");
+  sym(N.log_size, "nvrtcGetProgramLogSize");
+  sym(N.get_log, "nvrtcGetProgramLog");
+  sym(N.cubin_size, "nvrtcGetCUBINSize");
+  sym(N.get_cubin, "nvrtcGetCUBIN");
+  sym(N.lowered, "nvrtcGetLoweredName");
+  sym(N.destroy, "nvrtcDestroyProgram");
+  N.ok = ok;
+  return N;
+}
+
+const Nvrtc &nvrtc() {
+  static const Nvrtc N = load_nvrtc();
+  return N;
+}
+
+// ---- driver entry points (module loading and launch) --------------------------
+struct Driver {
+  bool ok = false;
+  decltype(&cuModuleLoadData) load = nullptr;
+  decltype(&cuModuleGetFunction) get_function = nullptr;
+  decltype(&cuFuncSetAttribute) set_attr = nullptr;
+  decltype(&cuLaunchKernel) launch = nullptr;
+  decltype(&cuOccupancyMaxActiveBlocksPerMultiprocessor) occupancy = nullptr;
+};
+
+Driver load_driver() {
+  Driver D;
+  bool ok = true;
+  auto sym = [&](auto &fp, const char *name) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    fp = reinterpret_cast<std::remove_reference_t<decltype(fp)>>(p);
+    ok = ok && p != nullptr;
+  };
+  sym(D.load, "cuModuleLoadData");
+  sym(D.get_function, "cuModuleGetFunction");
+  sym(D.set_attr, "cuFuncSetAttribute");
+  sym(D.launch, "cuLaunchKernel");
+  sym(D.occupancy, "cuOccupancyMaxActiveBlocksPerMultiprocessor");
+  cudaGetLastError();
+  D.ok = ok;
+  return D;
+}
+
+const Driver &driver() {
+  static const Driver D = load_driver();
+  return D;
+}
+
+// ---- compilation -------------------------------------------------------------
+const char *kNames[2] = {"cusna::period_kernel<256>", "cusna::period_kernel<512>"};
+
+struct Compiled {
+  int status = -1;             // 0 ok
+  std::vector<char> cubin;
+  std::string lowered[2];
+  std::string log;
+  double seconds = 0.0;
+};
+
+Compiled compile_spec(const std::string &spec) {
+  Compiled C;
+  const Nvrtc &N = nvrtc();
+  if (!N.ok) {
+    C.log = "NVRTC is not available";
+    return C;
+  }
+  const std::string src = std::string("#include \"saom_kernel.cuh\"\n") + spec +
+                          "#include \"saom_period.cuh\"\n";
+  const auto t0 = std::chrono::steady_clock::now();
+  nvrtcProgram prog = nullptr;
+  if (N.create(&prog, src.c_str(), "cusna_period_jit.cu", kJitHeaderCount, kJitHeaderSources,
+               kJitHeaderNames) != NVRTC_SUCCESS) {
+    C.log = "nvrtcCreateProgram failed";
+    return C;
+  }
+  for (const char *nm : kNames) N.add_name(prog, nm);
+  const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false",
+                        "-default-device", "-DLIBCUSNA_BUILD"};
+  const nvrtcResult r = N.compile(prog, (int)(sizeof opts / sizeof opts[0]), opts);
+  size_t ls = 0;
+  N.log_size(prog, &ls);
+  if (ls > 1) {
+    C.log.resize(ls);
+    N.get_log(prog, &C.log[0]);
+  }
+  if (r == NVRTC_SUCCESS) {
+    size_t cs = 0;
+    N.cubin_size(prog, &cs);
+    C.cubin.resize(cs);
+    N.get_cubin(prog, C.cubin.data());
+    bool names_ok = true;
+    for (int q = 0; q < 2; ++q) {
+      const char *lw = nullptr;
+      if (N.lowered(prog, kNames[q], &lw) != NVRTC_SUCCESS || !lw) names_ok = false;
+      else C.lowered[q] = lw;
+    }
+    C.status = names_ok && cs > 0 ? 0 : -1;
+  }
+  N.destroy(&prog);
+  C.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return C;
+}
+
+// ---- registry and the background compiler ----------------------------------------
+enum { S_IDLE = 0, S_QUEUED = 1, S_COMPILED = 2, S_LOADED = 3, S_FAILED = -1 };
+
+struct Entry {
+  int state = S_IDLE;
+  int uses = 0;
+  Compiled comp;
+  CUmodule mod = nullptr;
+  JitKernel k;
+};
+
+struct Registry {
+  std::mutex mu;
+  std::condition_variable cv;
+  std::unordered_map<std::string, std::unique_ptr<Entry>> map;
+  std::deque<std::pair<std::string, Entry *>> queue;
+  bool busy = false;
+  bool worker = false;
+  int compiled = 0;
+};
+
+// never destroyed: the background compiler may still run at process exit
+Registry &reg() {
+  static Registry *R = new Registry();
+  return *R;
+}
+
+void worker_loop() {
+  Registry &R = reg();
+  for (;;) {
+    std::pair<std::string, Entry *> job;
+    {
+      std::unique_lock<std::mutex> lk(R.mu);
+      R.cv.wait(lk, [&] { return !R.queue.empty(); });
+      job = R.queue.front();
+      R.queue.pop_front();
+      R.busy = true;
+    }
+    Compiled c = compile_spec(job.first);
+    {
+      std::lock_guard<std::mutex> lk(R.mu);
+      job.second->comp = std::move(c);
+      job.second->state = job.second->comp.status == 0 ? S_COMPILED : S_FAILED;
+      if (job.second->state == S_COMPILED) ++R.compiled;
+      R.busy = false;
+    }
+    R.cv.notify_all();
+  }
+}
+
+int uses_before_compile() {
+  const char *s = std::getenv("CUSNA_JIT_AFTER");
+  const int v = s ? std::atoi(s) : 3;
+  return v < 1 ? 1 : v;
+}
+
+// module load in the calling thread's context (the caller holds no capture)
+bool load_entry(Entry &E) {
+  const Driver &D = driver();
+  if (!D.ok) return false;
+  if (D.load(&E.mod, E.comp.cubin.data()) != CUDA_SUCCESS) return false;
+  CUfunction f[2];
+  for (int q = 0; q < 2; ++q)
+    if (D.get_function(&f[q], E.mod, E.comp.lowered[q].c_str()) != CUDA_SUCCESS) return false;
+  E.k.f256 = (void *)f[0];
+  E.k.f512 = (void *)f[1];
+  return true;
+}
+
+}  // namespace
+
+int jit_mode() {
+  static const int mode = [] {
+    const char *s = std::getenv("CUSNA_JIT");
+    if (!s) return 1;
+    if (!std::strcmp(s, "0") || !std::strcmp(s, "off")) return 0;
+    if (!std::strcmp(s, "sync")) return 2;
+    return 1;
+  }();
+  return mode;
+}
+
+bool jit_get(const std::string &spec, JitKernel *out, bool now) {
+  const int mode = jit_mode();
+  if (mode == 0) return false;
+  Registry &R = reg();
+  Entry *E = nullptr;
+  bool compile_now = false;
+  {
+    std::lock_guard<std::mutex> lk(R.mu);
+    auto &slot = R.map[spec];
+    if (!slot) slot.reset(new Entry());
+    E = slot.get();
+    if (E->state == S_LOADED) {
+      *out = E->k;
+      return true;
+    }
+    if (E->state == S_FAILED) return false;
+    ++E->uses;
+    if (E->state == S_IDLE && (now || mode == 2 || E->uses >= uses_before_compile())) {
+      if (now || mode == 2) {
+        E->state = S_QUEUED;
+        compile_now = true;
+      } else {
+        E->state = S_QUEUED;
+        R.queue.emplace_back(spec, E);
+        if (!R.worker) {
+          R.worker = true;
+          std::thread(worker_loop).detach();
+        }
+        R.cv.notify_all();
+      }
+    }
+  }
+  if (compile_now) {
+    Compiled c = compile_spec(spec);
+    std::lock_guard<std::mutex> lk(R.mu);
+    E->comp = std::move(c);
+    E->state = E->comp.status == 0 ? S_COMPILED : S_FAILED;
+    if (E->state == S_COMPILED) ++R.compiled;
+  }
+  std::unique_lock<std::mutex> lk(R.mu);
+  // asked for it now while the background compiler has it: wait for that
+  if (now && E->state == S_QUEUED) R.cv.wait(lk, [&] { return E->state != S_QUEUED; });
+  if (E->state == S_LOADED) {
+    *out = E->k;
+    return true;
+  }
+  if (E->state != S_COMPILED) return false;
+  if (!load_entry(*E)) {
+    E->state = S_FAILED;
+    return false;
+  }
+  E->state = S_LOADED;
+  *out = E->k;
+  return true;
+}
+
+int jit_blocks_per_sm(const JitKernel &K, int threads, size_t dyn_smem) {
+  const Driver &D = driver();
+  CUfunction f = (CUfunction)(threads <= 256 ? K.f256 : K.f512);
+  if (!D.ok || !f) return 0;
+  if (D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn_smem) != CUDA_SUCCESS)
+    return 0;
+  int blocks = 0;
+  if (D.occupancy(&blocks, f, threads, dyn_smem) != CUDA_SUCCESS) return 0;
+  return blocks;
+}
+
+cudaError_t launch_period_jit(const JitKernel &K, const LaunchShape &sh, const DevProblem *probs,
+                              const long long *unit_start, int nprob, long long total,
+                              unsigned long long *counter, uint32_t *cols_scratch,
+                              uint32_t *rows_scratch, size_t cols_words, cudaStream_t st) {
+  const Driver &D = driver();
+  const int threads = 32 * sh.G * sh.teams_per_cta;
+  const size_t dyn = sh.lay.bytes * sh.teams_per_cta;
+  CUfunction f = (CUfunction)(threads <= 256 ? K.f256 : K.f512);
+  if (!D.ok || !f) return cudaErrorInvalidDeviceFunction;
+  if (D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  SliceLayout lay = sh.lay;
+  int G = sh.G;
+  void *args[] = {&probs, &unit_start, &nprob, &total, &counter, &lay, &G, &cols_scratch,
+                  &rows_scratch, &cols_words};
+  const CUresult r = D.launch(f, (unsigned)sh.ctas, 1, 1, (unsigned)threads, 1, 1, (unsigned)dyn,
+                              (CUstream)st, args, nullptr);
+  if (r != CUDA_SUCCESS) return cudaErrorLaunchFailure;
+  note_launch();
+  return cudaSuccess;
+}
+
+int jit_compile_only(const std::string &spec, std::string *log, double *seconds) {
+  Compiled c = compile_spec(spec);
+  if (log) *log = c.log;
+  if (seconds) *seconds = c.seconds;
+  return c.status;
+}
+
+int jit_wait(double seconds) {
+  Registry &R = reg();
+  std::unique_lock<std::mutex> lk(R.mu);
+  R.cv.wait_for(lk, std::chrono::duration<double>(seconds),
+                [&] { return R.queue.empty() && !R.busy; });
+  return R.compiled;
+}
+
+}  // namespace cusna

@@ -79,6 +79,7 @@ cudaError_t launch_plan_prologue(DevProblem *probs, const unsigned long long *ba
                                  unsigned long long *epoch, const PlanTable *tabs, int n_tabs,
                                  cudaStream_t st);
 long long kernel_launches();  // kernels launched so far by the calling thread
+void note_launch();           // counts a launch made outside the wrappers here
 void set_last_error(const char *msg);  // text of cusna_last_error() for this thread
 cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
                             cudaStream_t st);

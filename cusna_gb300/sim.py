@@ -18,7 +18,9 @@ from .glue import Marshalled, result_dict
 
 
 def options(device_ptrs=False, chain_offset=0, warps_per_chain=0, chains_per_cta=0,
-            stream=None) -> GpuOptions:
+            stream=None, specialise=0) -> GpuOptions:
+    """specialise: 0 as CUSNA_JIT says, -1 never run the specialised kernel, 1
+    compile it now (cusna_gpu_options.specialise)."""
     o = GpuOptions()
     C.memset(C.addressof(o), 0, C.sizeof(o))
     o.struct_version = ABI_VERSION
@@ -27,7 +29,29 @@ def options(device_ptrs=False, chain_offset=0, warps_per_chain=0, chains_per_cta
     o.warps_per_chain = int(warps_per_chain)
     o.chains_per_cta = int(chains_per_cta)
     o.stream = stream
+    o.specialise = int(specialise)
     return o
+
+
+def specialise_check(m: Marshalled) -> float:
+    """Compile the period kernel specialised to m's effect plan (NVRTC, no
+    device needed); returns the compile time in seconds, raises on failure."""
+    lib = load_library()
+    buf = C.create_string_buffer(1 << 16)
+    sec = C.c_double(0.0)
+    st = lib.cusna_saom_specialise_check(C.byref(m.problem), buf, len(buf), C.byref(sec))
+    if st != 0:
+        raise RuntimeError(f"specialised kernel: status {st}: {buf.value.decode()[:2000]}")
+    return sec.value
+
+
+def specialise_wait(seconds: float = 120.0) -> int:
+    """Wait for background compilations of specialised kernels; returns how
+    many have completed."""
+    lib = load_library()
+    n = C.c_int32(0)
+    lib.cusna_saom_specialise_wait(float(seconds), C.byref(n))
+    return int(n.value)
 
 
 def simulate(m: Marshalled) -> dict:

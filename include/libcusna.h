@@ -213,6 +213,10 @@ typedef struct cusna_gpu_options {
                                   own per-thread stream)                       */
     double   elapsed_ms;       /* out: device time of the simulation kernels  */
     int64_t  ministeps;        /* out: ministeps summed over all chains       */
+    int32_t  specialise;       /* in: 0 as CUSNA_JIT says (compile the period
+                                  kernel for the effect plan in the background
+                                  after a few uses), -1 never, 1 compile now  */
+    int32_t  specialised;      /* out: 1 if the specialised kernel ran        */
 } cusna_gpu_options;
 
 /* cusna_saom_simulate_period with options (device-resident buffers, chain
@@ -403,6 +407,24 @@ CUSNA_API cusna_status cusna_gof_distribution(
  * counts 2 flops): the peak against which the simulator's float64 work is
  * reported. Runs a short synthetic kernel. */
 CUSNA_API cusna_status cusna_measure_fp64_tflops(double *tflops);
+
+/* ---- period kernel specialised to an effect plan (no counterpart) ----------
+ * The library's period kernel evaluates the model's effects through a per-
+ * effect dispatch. For a model used repeatedly, the library compiles (NVRTC,
+ * in a background thread, after CUSNA_JIT_AFTER uses of the same effect plan,
+ * default 3) a copy of the kernel with the effect plan written out, and runs it
+ * once it is ready; every output is bit-identical to the library kernel's.
+ * CUSNA_JIT=0 disables this, CUSNA_JIT=sync compiles on first use, and
+ * cusna_gpu_options.specialise overrides it per call.
+ * cusna_saom_specialise_check validates problem (host pointers) and compiles
+ * its specialised kernel without loading it (no device needed): CUSNA_OK, or
+ * CUSNA_ERR_UNSUPPORTED with the compiler log in log[0..log_len) and
+ * cusna_last_error(); *seconds (may be NULL) receives the compile time.
+ * cusna_saom_specialise_wait waits up to `seconds` for background compilations
+ * and writes how many have completed to *compiled (may be NULL). */
+CUSNA_API cusna_status cusna_saom_specialise_check(const cusna_saom_problem *problem, char *log,
+                                                   size_t log_len, double *seconds);
+CUSNA_API cusna_status cusna_saom_specialise_wait(double seconds, int32_t *compiled);
 
 /* ---- moment surrogate (no counterpart in the reference) --------------------
  * A multilayer perceptron n_in -> hidden -> hidden -> n_out with GELU
