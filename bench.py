@@ -86,13 +86,14 @@ def smem_bytes_per_network_ministep(n, W):
     return (n - 1) * (4 * 3 * W + 12)
 
 
-# Warp-instructions the period kernel executes per network ministep, from the
-# ncu capture of the kernel on each workload (smsp__inst_executed.sum over the
-# launch's network ministeps): n=200, k=8, 1024 chains.
-INST_PER_MINISTEP = {"c2": 11400.0}
+# Warp-instructions the period kernel executes per network ministep, from ncu
+# captures of the bench's own timed launch (smsp__inst_executed.sum over the
+# launch's 6,557,430 network ministeps; n=200, k=8, 4096 chains, autotuned
+# shape): the kernel specialised to the effect plan and the library kernel.
+INST_PER_MINISTEP = {("c2", True): 6600.0, ("c2", False): 10100.0}
 
 
-def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk):
+def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, specialised=True):
     """The period kernel is latency-bound: its state is on chip (DRAM moves only
     the problem and the outputs) and no pipe is busier than a quarter of its
     peak, so its ceiling is the SMs' instruction issue rate (4 warp-instructions
@@ -103,7 +104,7 @@ def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk):
     mhz = (clk or {}).get("sm_mhz") or 2070.0
     hz = mhz * 1e6
     rate = net_steps / (kernel_ms / 1e3)
-    ipm = INST_PER_MINISTEP.get(workload)
+    ipm = INST_PER_MINISTEP.get((workload, bool(specialised)))
     peak = 4.0 * sm_count * hz / 1e9
     achieved = rate * ipm / 1e9 if ipm else None
     smem_peak = 128.0 * sm_count * hz / 1e12          # TB/s, 128 B per cycle per SM
@@ -601,7 +602,7 @@ def main():
     clk = clocks.summary(local)
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     roofline = period_roofline(args.workload, n, (n + 31) // 32, k, net_steps, kern_avg_ms, sm_count,
-                               clk)
+                               clk, specialised=all(specialised))
     line = {
         "metric": "ministeps/s", "value": value, "unit": "ministeps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
