@@ -527,6 +527,7 @@ def main():
             kernel_ms.append(o.elapsed_ms)
             launches.append(o.launches)
             specialised.append(o.specialised)
+            shape = (o.warps_per_chain, o.chains_per_cta)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall0
     barrier()
@@ -613,6 +614,7 @@ def main():
                    "ministeps_per_step": all_ministeps,
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
                    "parallelism": f"replicas x{ws}, chains sharded by chain offset",
+                   "launch_shape": {"warps_per_chain": shape[0], "chains_per_cta": shape[1]},
                    "period_kernel": ("specialised to the effect plan (NVRTC, compiled before "
                                      f"the timed steps in {t_spec:.1f} s)"
                                      if all(specialised) else "library kernel")},

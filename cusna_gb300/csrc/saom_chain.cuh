@@ -408,7 +408,11 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
         double f = 0.0;
         if (j != i) {
           const int aij = bit_of(S.rowsT, n, i, j);
+#ifdef CUSNA_JIT_SPEC
+          f = jit_change_stats<true>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
+#else
           f = change_stats<true, MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
+#endif
         }
         uint32_t ph[4];
         philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
@@ -429,7 +433,11 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     } else {
       const int aij = bit_of(S.rowsT, n, i, jstar);
       const int aji = bit_of(S.colsT, n, i, jstar);
+#ifdef CUSNA_JIT_SPEC
+      jit_change_stats<false>(P, S, X, jstar, aij, aji, d);
+#else
       change_stats<false, MULTI>(P, S, X, jstar, aij, aji, d);
+#endif
       for (int e = 0; e < k; ++e) S.dstar[e] = d[e];
     }
   }

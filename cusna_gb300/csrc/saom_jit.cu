@@ -118,7 +118,88 @@ std::string jit_spec_source(const JitPlan &J) {
     s += "    if (has_term) {\n      f = __fadd_rn(f, term);\n      a = __fadd_rn(a, fabsf(term));\n"
          "    }\n  }\n";
   }
-  s += "  *absf = a;\n  return f;\n}\n}  // namespace cusna\n";
+  s += "  *absf = a;\n  return f;\n}\n";
+
+  // the float64 evaluation (the chosen alter and uncertified choices): the
+  // branches of change_stats (saom_kernel.cuh) in the same way
+  s += "template <bool TERMS>\n"
+       "__device__ __forceinline__ double jit_change_stats(const DevProblem &P, const Slice &S,\n"
+       "    const StepCtx &X, int j, int aij, int aji, double *d) {\n"
+       "  const int n = P.n, W = P.W, i = X.i;\n"
+       "  (void)n; (void)W; (void)i; (void)aji;\n"
+       "  const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;\n"
+       "  const bool ttab = (P.flags & F_THETA_TAB) != 0;\n  (void)ttab;\n"
+       "  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;\n"
+       "  (void)ri_cj; (void)ri_rj; (void)rj_ci; (void)ci_cj; (void)ci_rj; (void)ricirj;\n";
+  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
+    s += "  for (int w = 0; w < W; ++w) {\n"
+         "    const uint32_t ri = S.rowsT[w * n + i], rj = S.rowsT[w * n + j];\n"
+         "    const uint32_t ci = S.colsT[w * n + i], cj = S.colsT[w * n + j];\n"
+         "    (void)ri; (void)rj; (void)ci; (void)cj;\n";
+    if (fl & F_PC_RI_CJ) s += "    ri_cj += __popc(ri & cj);\n";
+    if (fl & F_PC_RI_RJ) s += "    ri_rj += __popc(ri & rj);\n";
+    if (fl & F_PC_RJ_CI) s += "    rj_ci += __popc(rj & ci);\n";
+    if (fl & F_PC_CI_CJ) s += "    ci_cj += __popc(ci & cj);\n";
+    if (fl & F_PC_CI_RJ) s += "    ci_rj += __popc(ci & rj);\n";
+    if (fl & F_PC_RICIRJ) s += "    ricirj += __popc(ri & ci & rj);\n";
+    s += "  }\n";
+  }
+  s += "  double f = 0.0;\n";
+  for (int e = 0; e < k; ++e) {
+    const int kind = J.kind[e], cfn = J.cfn[e];
+    put("  {  // effect %d\n", e);
+    s += "    double v, term = 0.0;\n    bool has_term = TERMS;\n";
+    if (kind == K_CNT) {
+      switch (cfn) {
+        case 0: s += "    const int c = 1;\n"; break;
+        case 1: s += "    const int c = aji;\n"; break;
+        case 2: s += "    const int c = ri_cj + ri_rj;\n"; break;
+        case 3: s += "    const int c = rj_ci;\n"; break;
+        case 4: s += "    const int c = S.indeg[j] + 1 - aij;\n"; break;
+        case 5:
+          s += "    int c = 0;\n"
+               "    const uint32_t *eq = S.tpeq + (aij ? W : 0);\n"
+               "    for (int w = 0; w < W; ++w)\n"
+               "      c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);\n"
+               "    if (S.tp[j] > 0) ++c;\n";
+          break;
+        case 6: s += "    const int c = (aji ? ri_cj : 0) + ricirj;\n"; break;
+        default: s += "    const int c = S.outdeg[j];\n"; break;
+      }
+      put("    v = flip(i2d(c), sg);\n"
+          "    if (TERMS) term = ttab ? flip(P.tab[S.eofft[%d] + c], sg) : __dmul_rn(S.th[%d], v);\n",
+          e, e);
+    } else if (kind == K_LOOK) {
+      switch (cfn) {
+        case 4: s += "    const int idx = S.indeg[j] + 1 - aij;\n"; break;
+        case 7: s += "    const int idx = S.outdeg[j];\n"; break;
+        case 8: s += "    const int idx = ri_cj;\n"; break;
+        case 9: s += "    const int idx = ri_rj;\n"; break;
+        case 10: s += "    const int idx = ci_cj;\n"; break;
+        case 11: s += "    const int idx = ci_rj;\n"; break;
+        case 12: s += "    const int idx = j;\n"; break;
+        case 13: s += "    const int idx = S.z[j] - P.zlo;\n"; break;
+        case 14: s += "    const int idx = i * n + j;\n"; break;
+        default: s += "    const int idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo);\n"; break;
+      }
+      put("    v = flip(P.tab[S.eoffd[%d] + idx], sg);\n"
+          "    if (TERMS) term = ttab ? flip(P.tab[S.eofft[%d] + idx], sg) : __dmul_rn(S.th[%d], v);\n",
+          e, e, e);
+    } else if (kind == K_STEP) {
+      put("    const int q = 2 * aij + aji;\n"
+          "    v = S.stepd[%d + q];\n    term = S.stept[%d + q];\n", 4 * e, 4 * e);
+    } else if (kind == K_ZERO) {
+      s += "    v = 0.0;\n    has_term = false;\n";
+    } else {
+      put("    v = gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, d);\n"
+          "    if (TERMS) term = __dmul_rn(S.th[%d], v);\n", e, e);
+    }
+    if (J.ety[e] == 1) s += "    if (aij) { v = 0.0; has_term = false; }\n";
+    else if (J.ety[e] == 2) s += "    if (!aij) { v = 0.0; has_term = false; }\n";
+    put("    d[%d] = v;\n", e);
+    s += "    if (has_term) f = __dadd_rn(f, term);\n  }\n";
+  }
+  s += "  return f;\n}\n}  // namespace cusna\n";
   return s;
 }
 
