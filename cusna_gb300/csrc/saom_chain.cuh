@@ -286,6 +286,34 @@ __device__ __forceinline__ void block_lse(float *rec, float w, const float *d32,
   if (writer && q <= k) rec[q] = v[0];
 }
 
+// The block records of one pass combined by the team's warp 0: lane l takes
+// blocks l, l+32, ... in order and adds each block's sums rescaled to the
+// overall maximum (float32), then a fixed butterfly adds the lanes' partial
+// sums (warp_multi_sum). Quantity q lands in S.red[32G + q], past the warp
+// slots the team reductions use. The order of every addition depends on the
+// block index only, so the result is the same for every team size.
+template <int V>
+__device__ __forceinline__ void combine_blocks(const Team &T, const Slice &S, int n, int k) {
+  if (T.warp != 0) return;
+  const int nb = (n + 31) >> 5;
+  float M = -INFINITY;
+  for (int b = T.lane; b < nb; b += 32) M = fmaxf(M, S.blk[(size_t)b * (k + 2)]);
+  M = warp_max_f(M);
+  float v[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) v[q] = 0.f;
+  for (int b = T.lane; b < nb; b += 32) {
+    const float *rec = S.blk + (size_t)b * (k + 2);
+    const float r = rec[0] == M ? 1.f : expf(__fsub_rn(rec[0], M));
+#pragma unroll
+    for (int q = 0; q < V; ++q)
+      if (q <= k) v[q] = __fadd_rn(v[q], __fmul_rn(rec[1 + q], r));
+  }
+  const int q = warp_multi_sum<V>(v, T.lane);
+  const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
+  if (writer && q <= k) S.red[32 * T.G + q] = (double)v[0];
+}
+
 // One network ministep of focal actor i on the network of slice S, up to the
 // choice: change statistics, float32 keys and log-sum-exp, the certified or
 // exact float64 choice, and the chosen alter's float64 change statistics in
@@ -375,20 +403,15 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
 #endif
   }
   T.sync();
-  // blocks combined in order: lane q <= k forms quantity q (0: sum of
-  // weights, 1+e: weighted sum of d_e) rescaled to the overall maximum
-  if (T.tl <= k) {
-    const int nb = (n + 31) >> 5, q = T.tl;
-    float M = -INFINITY;
-    for (int b = 0; b < nb; ++b) M = fmaxf(M, S.blk[(size_t)b * (k + 2)]);
-    double acc = 0.0;
-    for (int b = 0; b < nb; ++b) {
-      const float *rec = S.blk + (size_t)b * (k + 2);
-      const float r = rec[0] == M ? 1.f : expf(__fsub_rn(rec[0], M));
-      acc = __dadd_rn(acc, (double)__fmul_rn(rec[1 + q], r));
-    }
-    S.red[32 * T.G + q] = acc;   // past the warp slots the reductions below use
-  }
+  // the block records combined into quantity q (0: sum of weights, 1+e:
+  // weighted sum of d_e) rescaled to the overall maximum, in S.red[32G + q]
+#ifdef CUSNA_JIT_SPEC
+  combine_blocks<(CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))>(T, S, n, CUSNA_JIT_K);
+#else
+  if (k + 1 <= 8) combine_blocks<8>(T, S, n, k);
+  else if (k + 1 <= 16) combine_blocks<16>(T, S, n, k);
+  else combine_blocks<32>(T, S, n, k);
+#endif
   const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
 
   // ---- the chosen alter ---------------------------------------------------
