@@ -315,8 +315,13 @@ Compiled compile_spec(const std::string &spec) {
     return C;
   }
   for (const char *nm : kNames) N.add_name(prog, nm);
+  // CUSNA_JIT_MINB: resident 256-thread CTAs per SM the register budget of
+  // the 256-thread instantiation allows (default 3: 85 registers; measured
+  // faster than 2 on the C2 workload, 75 vs 79 ms, and equal on C4)
+  std::string minb = "-DCUSNA_MINB_256=3";
+  if (const char *m = std::getenv("CUSNA_JIT_MINB")) minb = std::string("-DCUSNA_MINB_256=") + m;
   const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false",
-                        "-default-device", "-DLIBCUSNA_BUILD"};
+                        "-default-device", "-DLIBCUSNA_BUILD", minb.c_str()};
   const nvrtcResult r = N.compile(prog, (int)(sizeof opts / sizeof opts[0]), opts);
   size_t ls = 0;
   N.log_size(prog, &ls);
