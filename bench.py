@@ -357,6 +357,51 @@ def batching_comparison(full_fit=False):
     return out
 
 
+def fran_latency(args):
+    """Per-call latency of the FRAN backend (one chain of every period per
+    call, as siena07() drives it): a 50-actor, 3-wave conditional panel with
+    density, recip and transTrip, through the GPU plan engine (graph replay)
+    and through the CPU engine (the oracle's restatement), host wall clock,
+    mean over 200 calls after warm-up (the specialised kernel compiled first)."""
+    from cusna_gb300 import effects as E
+    from cusna_gb300 import fran as FR
+    from cusna_gb300 import mom
+    from cusna_gb300 import sim as G
+    names = ["density", "recip", "transTrip"]
+    specs = [E.make_effect_spec(nm) for nm in names]
+    eng = mom.GpuEngine()
+    waves = [WL.bernoulli_net(50, 0.05, seed=1).astype(np.int64)]
+    for sd in (11, 12):
+        m = marshal_period(WL.period_inputs(waves[-1], specs), 1, sd, 6.0,
+                           np.array([-2.5, 2.0, 0.4]), want_ends=True)
+        waves.append(eng.simulate_batch([m])[0]["a_ends"][0].astype(np.int64))
+    th = np.array([-2.5, 2.0, 0.4])
+    out = {"workload": "n=50, 3 waves (wave 1 Bernoulli(0.05), waves 2-3 simulated at rate 6), "
+                       "density/recip/transTrip, conditional; one chain per period per call"}
+    f = FR.cusna_fran(waves, names, conditional=True, seed=1)
+    for _ in range(5):
+        f({"theta": th})
+    G.specialise_wait(900.0)
+    for _ in range(20):
+        f({"theta": th})
+    t0 = time.perf_counter()
+    for _ in range(200):
+        f({"theta": th})
+    out["gpu_ms_per_call"] = 1e3 * (time.perf_counter() - t0) / 200
+    f.engine.close()
+    if not args.no_cpu_baseline:
+        import oracle
+        cf = FR.cusna_fran(waves, names, conditional=True, seed=1, engine=oracle.Oracle("port"))
+        for _ in range(5):
+            cf({"theta": th})
+        t0 = time.perf_counter()
+        for _ in range(200):
+            cf({"theta": th})
+        out["cpu_ms_per_call"] = 1e3 * (time.perf_counter() - t0) / 200
+        out["cpu_engine"] = "oracle port (C restatement), one call at a time"
+    return out
+
+
 def multi_comparison(args):
     """The multi-network simulator (cusna_saom_simulate_multi) and estimator.
     Throughput: M chains of a 2-network period with every cross-effect type,
@@ -587,6 +632,12 @@ def main():
         except Exception as exc:   # the simulator line is reported regardless
             batching = {"error": f"{type(exc).__name__}: {exc}"}
 
+    fran = None
+    if not args.no_multi and ws == 1:
+        try:
+            fran = fran_latency(args)
+        except Exception as exc:  # reported, never fatal to the headline line
+            fran = {"error": f"{type(exc).__name__}: {exc}"}
     multi = None
     if not args.no_multi and ws == 1:
         try:
@@ -624,6 +675,7 @@ def main():
         "mom_fit": mom_fit,
         "batching": batching,
         "multi": multi,
+        "fran": fran,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
