@@ -7,6 +7,7 @@ the library is missing, `load_library()` raises.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
 
@@ -184,6 +185,10 @@ def load_library(path: str | None = None):
     lib.cusna_saom_specialise_wait.restype = i32
     if path is None:
         _lib = lib
+        # a specialised period kernel may still be compiling in the library's
+        # background thread: let it finish before the interpreter (and the
+        # compiler library it uses) is torn down
+        atexit.register(lambda: lib.cusna_saom_specialise_wait(600.0, None))
     return lib
 
 

@@ -365,6 +365,7 @@ struct Registry {
   std::deque<std::pair<std::string, Entry *>> queue;
   bool busy = false;
   bool worker = false;
+  bool stopping = false;
   int compiled = 0;
 };
 
@@ -380,7 +381,8 @@ void worker_loop() {
     std::pair<std::string, Entry *> job;
     {
       std::unique_lock<std::mutex> lk(R.mu);
-      R.cv.wait(lk, [&] { return !R.queue.empty(); });
+      R.cv.wait(lk, [&] { return !R.queue.empty() || R.stopping; });
+      if (R.stopping) return;
       job = R.queue.front();
       R.queue.pop_front();
       R.busy = true;
@@ -395,6 +397,18 @@ void worker_loop() {
     }
     R.cv.notify_all();
   }
+}
+
+// At process exit: drop queued compilations and wait for the one in flight,
+// so NVRTC is not inside a compilation while the process tears it down.
+void stop_worker_at_exit() {
+  Registry &R = reg();
+  std::unique_lock<std::mutex> lk(R.mu);
+  R.stopping = true;
+  for (auto &job : R.queue) job.second->state = S_IDLE;
+  R.queue.clear();
+  R.cv.notify_all();
+  R.cv.wait(lk, [&] { return !R.busy; });
 }
 
 int uses_before_compile() {
@@ -455,6 +469,10 @@ bool jit_get(const std::string &spec, JitKernel *out, bool now) {
         R.queue.emplace_back(spec, E);
         if (!R.worker) {
           R.worker = true;
+          // the compiler library is loaded first, so this handler runs before
+          // its static destructors at exit (handlers run in reverse order)
+          (void)nvrtc();
+          std::atexit(stop_worker_at_exit);
           std::thread(worker_loop).detach();
         }
         R.cv.notify_all();
