@@ -418,6 +418,11 @@ def multi_comparison(args):
     M = 4096
     inp, seed, lam, theta = WL.multi_case("cross", seed=1, n=200, M=M, D=2)
     m = marshal_multi(inp, M, seed, lam, theta, want_ends=False)
+    # the first calls have the library compile the kernel for these effect
+    # plans; it is waited for, so the timed calls run the specialised kernel
+    for _ in range(3):
+        sim.simulate_multi(m)
+    sim.specialise_wait(900.0)
     for _ in range(2):
         sim.simulate_multi(m)
     ts = []

@@ -183,6 +183,11 @@ def load_library(path: str | None = None):
     lib.cusna_saom_specialise_check.restype = i32
     lib.cusna_saom_specialise_wait.argtypes = [C.c_double, P(i32)]
     lib.cusna_saom_specialise_wait.restype = i32
+    lib.cusna_saom_specialise_check_multi.argtypes = [P(MultiProblem), C.c_char_p, sz,
+                                                      P(C.c_double)]
+    lib.cusna_saom_specialise_check_multi.restype = i32
+    lib.cusna_saom_specialise_mode.argtypes = [i32]
+    lib.cusna_saom_specialise_mode.restype = i32
     if path is None:
         _lib = lib
         # a specialised period kernel may still be compiling in the library's
@@ -205,6 +210,7 @@ EXPORTED_SYMBOLS = [
     "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_train_steps", "cusna_mlp_jacobian",
     "cusna_saom_simulate_multi", "cusna_cross_stats", "cusna_typed_stats",
     "cusna_gof_distribution", "cusna_saom_specialise_check", "cusna_saom_specialise_wait",
+    "cusna_saom_specialise_check_multi", "cusna_saom_specialise_mode",
 ]
 
 # cusna_adam_hyper: int32 step, float lr, beta1, beta2, eps, c1, c2

@@ -39,7 +39,7 @@ def nvcc() -> str:
 # device headers the run-time specialisation (csrc/saom_jit.cu) compiles with
 # NVRTC; they are embedded into the library as strings
 JIT_HEADERS = ["saom_common.cuh", "saom_kernel.cuh", "saom_stats.cuh", "saom_chain.cuh",
-               "saom_period.cuh"]
+               "saom_period.cuh", "saom_multi_kernel.cuh"]
 
 
 def write_jit_sources(build_dir: str) -> None:

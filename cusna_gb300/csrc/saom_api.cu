@@ -114,6 +114,7 @@ T *at(size_t off) {
 struct Facts {
   std::vector<int> tid, i0, i1, i2, rk, ety;
   std::string spec;                        // effect plan of the specialised kernel (saom_jit.h)
+  JitPlan jplan;
   int flags = 0;
   std::vector<int> kind, cfn, offd, offt;  // effect plan, k each
   std::vector<int> tsize;                  // theta-table length per effect (0: none)
@@ -376,13 +377,13 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
   }
   F.flags = fl;
   if ((s = build_plan(p, dev, F, one_row)) != CUSNA_OK) return s;
-  if (!F.multi) {
-    JitPlan J;
+  {
+    JitPlan &J = F.jplan;
     J.pc_flags = F.flags & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ |
                             F_PC_RICIRJ);
     J.kind = F.kind; J.cfn = F.cfn; J.tid = F.tid; J.ety = F.ety;
     J.i0 = F.i0; J.i1 = F.i1; J.i2 = F.i2;
-    F.spec = jit_spec_source(J);
+    if (!F.multi) F.spec = jit_spec_source(J);
   }
   // gwdsp change statistics index the weight table at p+1 with p <= n-2 on a
   // network without self-ties; a self-tie in the start network could push p to
@@ -741,9 +742,9 @@ std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, in
         if (threads > 512 || (G > 1 && tpc > 15)) continue;
         const size_t dyn = sh.lay.bytes * nets * tpc;
         if (dyn > (size_t)c.smem_optin) continue;
-        const int per_sm = nets > 1 ? multi_blocks_per_sm(threads, dyn)
-                           : (jk ? jit_blocks_per_sm(*jk, threads, dyn)
-                                 : period_blocks_per_sm(threads, dyn));
+        const int per_sm = jk ? jit_blocks_per_sm(*jk, threads, dyn)
+                              : (nets > 1 ? multi_blocks_per_sm(threads, dyn)
+                                          : period_blocks_per_sm(threads, dyn));
         if (per_sm < 1) continue;
         const double teams_sm = (double)per_sm * tpc;
         const double chains_sm = (double)total_units / c.sms;
@@ -1022,7 +1023,11 @@ struct MultiNet {
   std::vector<float> th, lam, p1, p2, vm, wt;
 };
 
-cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi_result *r) {
+// check_only: validate and compile the specialised kernel (no device), with
+// the compiler log in *log and the compile time in *seconds.
+cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi_result *r,
+                            bool check_only = false, std::string *log = nullptr,
+                            double *seconds = nullptr) {
   if (!pb || !r) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
   if (pb->struct_version != CUSNA_ABI_VERSION || r->struct_version != CUSNA_ABI_VERSION) {
     set_err("struct_version %d/%d != %d", pb->struct_version, r->struct_version, CUSNA_ABI_VERSION);
@@ -1122,10 +1127,24 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
     gw |= (F.flags & (F_NEED_GW29 | F_NEED_TP)) != 0;
     tq |= (F.flags & F_NEED_GW30) != 0;
   }
+  // the multi-network kernel specialised to the networks' effect plans
+  std::vector<JitPlan> jplans;
+  for (int d = 0; d < D; ++d) jplans.push_back(jobs[d].F.jplan);
+  const std::string mspec = jit_multi_spec_source(jplans);
+  if (check_only) {
+    if (jit_compile_only(mspec, log, seconds) != 0) {
+      set_err("specialised multi-network kernel did not compile");
+      return CUSNA_ERR_UNSUPPORTED;
+    }
+    return CUSNA_OK;
+  }
   cusna_status s;
   if ((s = ensure_ctx()) != CUSNA_OK) return s;
   cudaStream_t st = g_ctx.stream;
-  const std::vector<LaunchShape> ranked = rank_shapes(n, W, kmax, 0, 0, tp, gw, tq, M, 0, 0, D);
+  JitKernel jk;
+  const bool use_jit = jit_get(mspec, &jk);
+  const std::vector<LaunchShape> ranked =
+      rank_shapes(n, W, kmax, 0, 0, tp, gw, tq, M, 0, 0, D, use_jit ? &jk : nullptr);
   if (ranked.empty()) {
     set_err("no launch shape fits %d networks of n=%d", D, n);
     return CUSNA_ERR_UNSUPPORTED;
@@ -1168,9 +1187,14 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
   CU(cudaMemcpyAsync(at<char>(o_lam), pb->lam, (size_t)M * D * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<char>(o_gidx), gidx.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemsetAsync(at<char>(o_counter), 0, sizeof(unsigned long long), st));
-  CU(launch_multi(sh, at<DevProblem>(o_probs), md, M, at<unsigned long long>(o_counter),
-                  o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
-                  o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
+  if (use_jit)
+    CU(launch_multi_jit(jk, sh, at<DevProblem>(o_probs), md, M, at<unsigned long long>(o_counter),
+                        o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
+                        o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
+  else
+    CU(launch_multi(sh, at<DevProblem>(o_probs), md, M, at<unsigned long long>(o_counter),
+                    o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
+                    o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
   auto get = [&](void *dst, size_t off, size_t bytes) -> cusna_status {
     if (!dst || off == NONE) return CUSNA_OK;
     CU(cudaMemcpyAsync(dst, at<char>(off), bytes, cudaMemcpyDeviceToHost, st));
@@ -1515,6 +1539,30 @@ CUSNA_API cusna_status cusna_saom_specialise_check(const cusna_saom_problem *pro
     set_err("specialised kernel did not compile: %.400s", text.c_str());
     return CUSNA_ERR_UNSUPPORTED;
   }
+  return CUSNA_OK;
+}
+
+CUSNA_API cusna_status cusna_saom_specialise_check_multi(const cusna_saom_multi_problem *problem,
+                                                         char *log, size_t log_len,
+                                                         double *seconds) {
+  g_err.clear();
+  if (!problem) { set_err("problem is NULL"); return CUSNA_ERR_NULL_ARG; }
+  cusna_saom_multi_result dummy;
+  std::memset(&dummy, 0, sizeof dummy);
+  dummy.struct_version = CUSNA_ABI_VERSION;
+  std::string text;
+  const cusna_status st = simulate_multi(problem, &dummy, true, &text, seconds);
+  if (log && log_len) {
+    const size_t m = std::min(log_len - 1, text.size());
+    std::memcpy(log, text.data(), m);
+    log[m] = 0;
+  }
+  return st;
+}
+
+CUSNA_API cusna_status cusna_saom_specialise_mode(int32_t mode) {
+  if (mode < -1 || mode > 2) { set_err("specialise mode %d", mode); return CUSNA_ERR_SHAPE; }
+  jit_set_mode(mode);
   return CUSNA_OK;
 }
 

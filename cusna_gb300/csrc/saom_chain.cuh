@@ -325,8 +325,9 @@ template <bool MULTI>
 __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, const Slice &S,
                                           int i, long long ms, uint32_t chain, double *d,
                                           float *d32, const uint32_t *rows0 = nullptr,
-                                          size_t net_stride = 0) {
+                                          size_t net_stride = 0, int net = 0) {
   const int n = P.n, W = P.W, k = P.k, L = T.L;
+  (void)net;
   step_helpers(T, P, S, i);
   StepCtx X;
   X.i = i;
@@ -370,9 +371,12 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
       ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
       if (ok) {
         float absf = 0.f;
-#ifdef CUSNA_JIT_SPEC
+#if defined(CUSNA_JIT_SPEC)
         // the effect plan compiled in (saom_jit.cu): the same float32 values
         if (!stay) f = jit_change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+#elif defined(CUSNA_JIT_MULTI)
+        if (!stay)
+          f = jit_change_stats32(net, P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
 #else
         if (!stay) f = change_stats32<MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
 #endif
@@ -431,8 +435,10 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
         double f = 0.0;
         if (j != i) {
           const int aij = bit_of(S.rowsT, n, i, j);
-#ifdef CUSNA_JIT_SPEC
+#if defined(CUSNA_JIT_SPEC)
           f = jit_change_stats<true>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
+#elif defined(CUSNA_JIT_MULTI)
+          f = jit_change_stats<true>(net, P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
 #else
           f = change_stats<true, MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
 #endif
@@ -456,8 +462,10 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     } else {
       const int aij = bit_of(S.rowsT, n, i, jstar);
       const int aji = bit_of(S.colsT, n, i, jstar);
-#ifdef CUSNA_JIT_SPEC
+#if defined(CUSNA_JIT_SPEC)
       jit_change_stats<false>(P, S, X, jstar, aij, aji, d);
+#elif defined(CUSNA_JIT_MULTI)
+      jit_change_stats<false>(net, P, S, X, jstar, aij, aji, d);
 #else
       change_stats<false, MULTI>(P, S, X, jstar, aij, aji, d);
 #endif

@@ -56,6 +56,22 @@ enum : int {
   K_CROSS = 5, // multi-network cross effect (ecfn = type 33..37) reading network eoffd
 };
 
+// Multi-network problem: what the multi-network kernel needs beyond the
+// per-network problems (one DevProblem per network, holding its effects).
+constexpr int kMaxNet = 4;  // CUSNA_MAXNET
+struct MultiDev {
+  int D, n, W, nact, k;
+  const int *act;                 // nact active actors first
+  const float *lam;               // M*D rates
+  uint32_t k0, k1;                // Philox key
+  int goff[kMaxNet + 1];          // network d's effects: gidx[goff[d] .. goff[d+1])
+  const int *gidx;                // their indices in the caller's effect order
+  float *rscores, *scores;        // device outputs (any may be null)
+  double *ntim;
+  int *steps;
+  uint8_t *a_ends;
+};
+
 // Canonical device form of one cusna_saom_problem. Every network is stored
 // word-major: element (w, j) of an n-actor bit matrix is word w of actor j's
 // row, at index w*n + j. Word w of row i, bit b, is the tie i -> 32*w + b.

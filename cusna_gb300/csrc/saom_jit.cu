@@ -5,6 +5,7 @@
 #include <dlfcn.h>
 #include <nvrtc.h>
 
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
@@ -24,183 +25,203 @@
 namespace cusna {
 
 // ---- generated source --------------------------------------------------------
-// Each effect becomes the branch of change_stats32 (saom_kernel.cuh) that its
-// kind selects, with the kind, count function, type, creation/endowment type
-// and interaction components as constants. Offsets, theta and every table stay
-// run-time values, so one compiled plan serves every problem with that plan.
-std::string jit_spec_source(const JitPlan &J) {
-  const int k = (int)J.kind.size();
-  const int fl = J.pc_flags;
+// Each effect becomes the branch of change_stats32 / change_stats
+// (saom_kernel.cuh) that its kind selects, with the kind, count function,
+// type, creation/endowment type and interaction components as constants.
+// Offsets, theta and every table stay run-time values, so one compiled plan
+// serves every problem with that plan.
+namespace {
+
+struct Gen {
   std::string s;
-  char buf[512];
-  auto put = [&](const char *fmt, auto... a) {
+  char buf[640];
+  template <class... A>
+  void put(const char *fmt, A... a) {
     std::snprintf(buf, sizeof buf, fmt, a...);
     s += buf;
-  };
-  put("#define CUSNA_JIT_SPEC 1\n#define CUSNA_JIT_K %d\nnamespace cusna {\n", k);
-  s += "__device__ __forceinline__ float jit_change_stats32(const DevProblem &P, const Slice &S,\n"
-       "    const StepCtx &X, int j, int aij, int aji, float *d32, float *absf) {\n"
-       "  const int n = P.n, W = P.W, i = X.i;\n"
-       "  (void)n; (void)W; (void)i; (void)aji;\n"
-       "  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;\n"
-       "  (void)ri_cj; (void)ri_rj; (void)rj_ci; (void)ci_cj; (void)ci_rj; (void)ricirj;\n";
-  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
-    s += "  for (int w = 0; w < W; ++w) {\n"
+  }
+};
+
+const int kPcAll = F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ;
+
+void gen_pair_counts(Gen &g, int fl) {
+  g.s += "  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;\n"
+         "  (void)ri_cj; (void)ri_rj; (void)rj_ci; (void)ci_cj; (void)ci_rj; (void)ricirj;\n";
+  if (!(fl & kPcAll)) return;
+  g.s += "  for (int w = 0; w < W; ++w) {\n"
          "    const uint32_t ri = S.rowsT[w * n + i], rj = S.rowsT[w * n + j];\n"
          "    const uint32_t ci = S.colsT[w * n + i], cj = S.colsT[w * n + j];\n"
          "    (void)ri; (void)rj; (void)ci; (void)cj;\n";
-    if (fl & F_PC_RI_CJ) s += "    ri_cj += __popc(ri & cj);\n";
-    if (fl & F_PC_RI_RJ) s += "    ri_rj += __popc(ri & rj);\n";
-    if (fl & F_PC_RJ_CI) s += "    rj_ci += __popc(rj & ci);\n";
-    if (fl & F_PC_CI_CJ) s += "    ci_cj += __popc(ci & cj);\n";
-    if (fl & F_PC_CI_RJ) s += "    ci_rj += __popc(ci & rj);\n";
-    if (fl & F_PC_RICIRJ) s += "    ricirj += __popc(ri & ci & rj);\n";
-    s += "  }\n";
+  if (fl & F_PC_RI_CJ) g.s += "    ri_cj += __popc(ri & cj);\n";
+  if (fl & F_PC_RI_RJ) g.s += "    ri_rj += __popc(ri & rj);\n";
+  if (fl & F_PC_RJ_CI) g.s += "    rj_ci += __popc(rj & ci);\n";
+  if (fl & F_PC_CI_CJ) g.s += "    ci_cj += __popc(ci & cj);\n";
+  if (fl & F_PC_CI_RJ) g.s += "    ci_rj += __popc(ci & rj);\n";
+  if (fl & F_PC_RICIRJ) g.s += "    ricirj += __popc(ri & ci & rj);\n";
+  g.s += "  }\n";
+}
+
+// the integer magnitude c of a K_CNT effect, or the table index of a K_LOOK one
+void gen_count(Gen &g, int cfn) {
+  switch (cfn) {
+    case 0: g.s += "    const int c = 1;\n"; break;
+    case 1: g.s += "    const int c = aji;\n"; break;
+    case 2: g.s += "    const int c = ri_cj + ri_rj;\n"; break;
+    case 3: g.s += "    const int c = rj_ci;\n"; break;
+    case 4: g.s += "    const int c = S.indeg[j] + 1 - aij;\n"; break;
+    case 5:
+      g.s += "    int c = 0;\n"
+             "    const uint32_t *eq = S.tpeq + (aij ? W : 0);\n"
+             "    for (int w = 0; w < W; ++w)\n"
+             "      c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);\n"
+             "    if (S.tp[j] > 0) ++c;\n";
+      break;
+    case 6: g.s += "    const int c = (aji ? ri_cj : 0) + ricirj;\n"; break;
+    default: g.s += "    const int c = S.outdeg[j];\n"; break;
   }
-  s += "  const uint32_t sg = aij ? 0x80000000u : 0u;\n"
-       "  float f = 0.f, a = 0.f;\n";
+}
+void gen_index(Gen &g, int cfn) {
+  switch (cfn) {
+    case 4: g.s += "    const int idx = S.indeg[j] + 1 - aij;\n"; break;
+    case 7: g.s += "    const int idx = S.outdeg[j];\n"; break;
+    case 8: g.s += "    const int idx = ri_cj;\n"; break;
+    case 9: g.s += "    const int idx = ri_rj;\n"; break;
+    case 10: g.s += "    const int idx = ci_cj;\n"; break;
+    case 11: g.s += "    const int idx = ci_rj;\n"; break;
+    case 12: g.s += "    const int idx = j;\n"; break;
+    case 13: g.s += "    const int idx = S.z[j] - P.zlo;\n"; break;
+    case 14: g.s += "    const int idx = i * n + j;\n"; break;
+    default: g.s += "    const int idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo);\n"; break;
+  }
+}
+
+// jit_change_stats32<sfx> and jit_change_stats<sfx><TERMS> of one effect plan
+void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi) {
+  const int k = (int)J.kind.size();
+  const int fl = J.pc_flags;
+  const char *x = sfx.c_str();
+  // float32 pass (change_stats32)
+  g.put("__device__ __forceinline__ float jit_change_stats32%s(const DevProblem &P, const Slice &S,\n"
+        "    const StepCtx &X, int j, int aij, int aji, float *d32, float *absf) {\n", x);
+  g.s += "  const int n = P.n, W = P.W, i = X.i;\n"
+         "  (void)n; (void)W; (void)i; (void)aji;\n";
+  gen_pair_counts(g, fl);
+  g.s += "  const uint32_t sg = aij ? 0x80000000u : 0u;\n"
+         "  float f = 0.f, a = 0.f;\n";
   for (int e = 0; e < k; ++e) {
     const int kind = J.kind[e], cfn = J.cfn[e], t = J.tid[e];
-    put("  {  // effect %d: type %d, kind %d, function %d\n", e, t, kind, cfn);
-    s += "    float v, term = 0.f;\n    bool has_term = true;\n";
+    g.put("  {  // effect %d: type %d, kind %d, function %d\n", e, t, kind, cfn);
+    g.s += "    float v, term = 0.f;\n    bool has_term = true;\n";
     if (kind == K_CNT) {
-      switch (cfn) {
-        case 0: s += "    const int c = 1;\n"; break;
-        case 1: s += "    const int c = aji;\n"; break;
-        case 2: s += "    const int c = ri_cj + ri_rj;\n"; break;
-        case 3: s += "    const int c = rj_ci;\n"; break;
-        case 4: s += "    const int c = S.indeg[j] + 1 - aij;\n"; break;
-        case 5:
-          s += "    int c = 0;\n"
-               "    const uint32_t *eq = S.tpeq + (aij ? W : 0);\n"
-               "    for (int w = 0; w < W; ++w)\n"
-               "      c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);\n"
-               "    if (S.tp[j] > 0) ++c;\n";
-          break;
-        case 6: s += "    const int c = (aji ? ri_cj : 0) + ricirj;\n"; break;
-        default: s += "    const int c = S.outdeg[j];\n"; break;
-      }
-      put("    v = __uint_as_float(__float_as_uint((float)c) ^ sg);\n"
-          "    term = __fmul_rn(S.th32[%d], v);\n", e);
+      gen_count(g, cfn);
+      g.put("    v = __uint_as_float(__float_as_uint((float)c) ^ sg);\n"
+            "    term = __fmul_rn(S.th32[%d], v);\n", e);
     } else if (kind == K_LOOK) {
-      switch (cfn) {
-        case 4: s += "    const int idx = S.indeg[j] + 1 - aij;\n"; break;
-        case 7: s += "    const int idx = S.outdeg[j];\n"; break;
-        case 8: s += "    const int idx = ri_cj;\n"; break;
-        case 9: s += "    const int idx = ri_rj;\n"; break;
-        case 10: s += "    const int idx = ci_cj;\n"; break;
-        case 11: s += "    const int idx = ci_rj;\n"; break;
-        case 12: s += "    const int idx = j;\n"; break;
-        case 13: s += "    const int idx = S.z[j] - P.zlo;\n"; break;
-        case 14: s += "    const int idx = i * n + j;\n"; break;
-        default: s += "    const int idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo);\n"; break;
-      }
-      put("    v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[%d] + idx]) ^ sg);\n"
-          "    term = __fmul_rn(S.th32[%d], v);\n", e, e);
+      gen_index(g, cfn);
+      g.put("    v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[%d] + idx]) ^ sg);\n"
+            "    term = __fmul_rn(S.th32[%d], v);\n", e, e);
     } else if (kind == K_STEP) {
-      put("    const int q = 2 * aij + aji;\n"
-          "    v = S.stepd32[%d + q];\n    term = S.stept32[%d + q];\n", 4 * e, 4 * e);
+      g.put("    const int q = 2 * aij + aji;\n"
+            "    v = S.stepd32[%d + q];\n    term = S.stept32[%d + q];\n", 4 * e, 4 * e);
     } else if (kind == K_ZERO) {
-      s += "    v = 0.f;\n    has_term = false;\n";
+      g.s += "    v = 0.f;\n    has_term = false;\n";
+    } else if (multi && kind == K_CROSS) {
+      g.put("    const int c = cross_count(S, X, n, W, %d, S.eoffd[%d], i, j);\n"
+            "    const float m = (%d == 36 && S.p1[%d] >= 2.0) ? sqrtf((float)c) : (float)c;\n"
+            "    v = __uint_as_float(__float_as_uint(m) ^ sg);\n"
+            "    term = __fmul_rn(S.th32[%d], v);\n", cfn, e, cfn, e, e);
     } else if (t == 32) {
       const int c2 = J.i2[e];
-      put("    v = __fmul_rn(d32[%d], d32[%d]);\n", J.i0[e], J.i1[e]);
-      if (c2 >= 0) put("    v = __fmul_rn(v, d32[%d]);\n", c2);
-      else s += "    if (aij) v = -v;\n";
-      put("    term = __fmul_rn(S.th32[%d], v);\n", e);
+      g.put("    v = __fmul_rn(d32[%d], d32[%d]);\n", J.i0[e], J.i1[e]);
+      if (c2 >= 0) g.put("    v = __fmul_rn(v, d32[%d]);\n", c2);
+      else g.s += "    if (aij) v = -v;\n";
+      g.put("    term = __fmul_rn(S.th32[%d], v);\n", e);
     } else {
-      put("    v = (float)gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj,\n"
-          "                        nullptr);\n    term = __fmul_rn(S.th32[%d], v);\n", e, e);
+      g.put("    v = (float)gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj,\n"
+            "                        nullptr);\n    term = __fmul_rn(S.th32[%d], v);\n", e, e);
     }
-    if (J.ety[e] == 1) s += "    if (aij) { v = 0.f; has_term = false; }\n";
-    else if (J.ety[e] == 2) s += "    if (!aij) { v = 0.f; has_term = false; }\n";
-    put("    d32[%d] = v;\n", e);
-    s += "    if (has_term) {\n      f = __fadd_rn(f, term);\n      a = __fadd_rn(a, fabsf(term));\n"
-         "    }\n  }\n";
+    if (J.ety[e] == 1) g.s += "    if (aij) { v = 0.f; has_term = false; }\n";
+    else if (J.ety[e] == 2) g.s += "    if (!aij) { v = 0.f; has_term = false; }\n";
+    g.put("    d32[%d] = v;\n", e);
+    g.s += "    if (has_term) {\n      f = __fadd_rn(f, term);\n      a = __fadd_rn(a, fabsf(term));\n"
+           "    }\n  }\n";
   }
-  s += "  *absf = a;\n  return f;\n}\n";
-
-  // the float64 evaluation (the chosen alter and uncertified choices): the
-  // branches of change_stats (saom_kernel.cuh) in the same way
-  s += "template <bool TERMS>\n"
-       "__device__ __forceinline__ double jit_change_stats(const DevProblem &P, const Slice &S,\n"
-       "    const StepCtx &X, int j, int aij, int aji, double *d) {\n"
-       "  const int n = P.n, W = P.W, i = X.i;\n"
-       "  (void)n; (void)W; (void)i; (void)aji;\n"
-       "  const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;\n"
-       "  const bool ttab = (P.flags & F_THETA_TAB) != 0;\n  (void)ttab;\n"
-       "  int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;\n"
-       "  (void)ri_cj; (void)ri_rj; (void)rj_ci; (void)ci_cj; (void)ci_rj; (void)ricirj;\n";
-  if (fl & (F_PC_RI_CJ | F_PC_RI_RJ | F_PC_RJ_CI | F_PC_CI_CJ | F_PC_CI_RJ | F_PC_RICIRJ)) {
-    s += "  for (int w = 0; w < W; ++w) {\n"
-         "    const uint32_t ri = S.rowsT[w * n + i], rj = S.rowsT[w * n + j];\n"
-         "    const uint32_t ci = S.colsT[w * n + i], cj = S.colsT[w * n + j];\n"
-         "    (void)ri; (void)rj; (void)ci; (void)cj;\n";
-    if (fl & F_PC_RI_CJ) s += "    ri_cj += __popc(ri & cj);\n";
-    if (fl & F_PC_RI_RJ) s += "    ri_rj += __popc(ri & rj);\n";
-    if (fl & F_PC_RJ_CI) s += "    rj_ci += __popc(rj & ci);\n";
-    if (fl & F_PC_CI_CJ) s += "    ci_cj += __popc(ci & cj);\n";
-    if (fl & F_PC_CI_RJ) s += "    ci_rj += __popc(ci & rj);\n";
-    if (fl & F_PC_RICIRJ) s += "    ricirj += __popc(ri & ci & rj);\n";
-    s += "  }\n";
-  }
-  s += "  double f = 0.0;\n";
+  g.s += "  *absf = a;\n  return f;\n}\n";
+  // float64 evaluation (change_stats): the chosen alter and uncertified choices
+  g.put("template <bool TERMS>\n"
+        "__device__ __forceinline__ double jit_change_stats%s(const DevProblem &P, const Slice &S,\n"
+        "    const StepCtx &X, int j, int aij, int aji, double *d) {\n", x);
+  g.s += "  const int n = P.n, W = P.W, i = X.i;\n"
+         "  (void)n; (void)W; (void)i; (void)aji;\n"
+         "  const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;\n"
+         "  const bool ttab = (P.flags & F_THETA_TAB) != 0;\n  (void)ttab;\n";
+  gen_pair_counts(g, fl);
+  g.s += "  double f = 0.0;\n";
   for (int e = 0; e < k; ++e) {
     const int kind = J.kind[e], cfn = J.cfn[e];
-    put("  {  // effect %d\n", e);
-    s += "    double v, term = 0.0;\n    bool has_term = TERMS;\n";
+    g.put("  {  // effect %d\n", e);
+    g.s += "    double v, term = 0.0;\n    bool has_term = TERMS;\n";
     if (kind == K_CNT) {
-      switch (cfn) {
-        case 0: s += "    const int c = 1;\n"; break;
-        case 1: s += "    const int c = aji;\n"; break;
-        case 2: s += "    const int c = ri_cj + ri_rj;\n"; break;
-        case 3: s += "    const int c = rj_ci;\n"; break;
-        case 4: s += "    const int c = S.indeg[j] + 1 - aij;\n"; break;
-        case 5:
-          s += "    int c = 0;\n"
-               "    const uint32_t *eq = S.tpeq + (aij ? W : 0);\n"
-               "    for (int w = 0; w < W; ++w)\n"
-               "      c += __popc(S.rowsT[w * n + i] & S.rowsT[w * n + j] & eq[w]);\n"
-               "    if (S.tp[j] > 0) ++c;\n";
-          break;
-        case 6: s += "    const int c = (aji ? ri_cj : 0) + ricirj;\n"; break;
-        default: s += "    const int c = S.outdeg[j];\n"; break;
-      }
-      put("    v = flip(i2d(c), sg);\n"
-          "    if (TERMS) term = ttab ? flip(P.tab[S.eofft[%d] + c], sg) : __dmul_rn(S.th[%d], v);\n",
-          e, e);
+      gen_count(g, cfn);
+      g.put("    v = flip(i2d(c), sg);\n"
+            "    if (TERMS) term = ttab ? flip(P.tab[S.eofft[%d] + c], sg) : __dmul_rn(S.th[%d], v);\n",
+            e, e);
     } else if (kind == K_LOOK) {
-      switch (cfn) {
-        case 4: s += "    const int idx = S.indeg[j] + 1 - aij;\n"; break;
-        case 7: s += "    const int idx = S.outdeg[j];\n"; break;
-        case 8: s += "    const int idx = ri_cj;\n"; break;
-        case 9: s += "    const int idx = ri_rj;\n"; break;
-        case 10: s += "    const int idx = ci_cj;\n"; break;
-        case 11: s += "    const int idx = ci_rj;\n"; break;
-        case 12: s += "    const int idx = j;\n"; break;
-        case 13: s += "    const int idx = S.z[j] - P.zlo;\n"; break;
-        case 14: s += "    const int idx = i * n + j;\n"; break;
-        default: s += "    const int idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo);\n"; break;
-      }
-      put("    v = flip(P.tab[S.eoffd[%d] + idx], sg);\n"
-          "    if (TERMS) term = ttab ? flip(P.tab[S.eofft[%d] + idx], sg) : __dmul_rn(S.th[%d], v);\n",
-          e, e, e);
+      gen_index(g, cfn);
+      g.put("    v = flip(P.tab[S.eoffd[%d] + idx], sg);\n"
+            "    if (TERMS) term = ttab ? flip(P.tab[S.eofft[%d] + idx], sg) : __dmul_rn(S.th[%d], v);\n",
+            e, e, e);
     } else if (kind == K_STEP) {
-      put("    const int q = 2 * aij + aji;\n"
-          "    v = S.stepd[%d + q];\n    term = S.stept[%d + q];\n", 4 * e, 4 * e);
+      g.put("    const int q = 2 * aij + aji;\n"
+            "    v = S.stepd[%d + q];\n    term = S.stept[%d + q];\n", 4 * e, 4 * e);
     } else if (kind == K_ZERO) {
-      s += "    v = 0.0;\n    has_term = false;\n";
+      g.s += "    v = 0.0;\n    has_term = false;\n";
+    } else if (multi && kind == K_CROSS) {
+      g.put("    const int c = cross_count(S, X, n, W, %d, S.eoffd[%d], i, j);\n"
+            "    v = flip((%d == 36 && S.p1[%d] >= 2.0) ? sqrt(i2d(c)) : i2d(c), sg);\n"
+            "    if (TERMS) term = __dmul_rn(S.th[%d], v);\n", cfn, e, cfn, e, e);
     } else {
-      put("    v = gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, d);\n"
-          "    if (TERMS) term = __dmul_rn(S.th[%d], v);\n", e, e);
+      g.put("    v = gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, d);\n"
+            "    if (TERMS) term = __dmul_rn(S.th[%d], v);\n", e, e);
     }
-    if (J.ety[e] == 1) s += "    if (aij) { v = 0.0; has_term = false; }\n";
-    else if (J.ety[e] == 2) s += "    if (!aij) { v = 0.0; has_term = false; }\n";
-    put("    d[%d] = v;\n", e);
-    s += "    if (has_term) f = __dadd_rn(f, term);\n  }\n";
+    if (J.ety[e] == 1) g.s += "    if (aij) { v = 0.0; has_term = false; }\n";
+    else if (J.ety[e] == 2) g.s += "    if (!aij) { v = 0.0; has_term = false; }\n";
+    g.put("    d[%d] = v;\n", e);
+    g.s += "    if (has_term) f = __dadd_rn(f, term);\n  }\n";
   }
-  s += "  return f;\n}\n}  // namespace cusna\n";
-  return s;
+  g.s += "  return f;\n}\n";
+}
+
+}  // namespace
+
+std::string jit_spec_source(const JitPlan &J) {
+  Gen g;
+  g.put("#define CUSNA_JIT_SPEC 1\n#define CUSNA_JIT_K %d\nnamespace cusna {\n", (int)J.kind.size());
+  gen_functions(g, J, "", false);
+  g.s += "}  // namespace cusna\n";
+  return g.s;
+}
+
+std::string jit_multi_spec_source(const std::vector<JitPlan> &nets) {
+  Gen g;
+  g.s += std::string(kJitMultiTag) + "\n#define CUSNA_JIT_MULTI 1\nnamespace cusna {\n";
+  const int D = (int)nets.size();
+  for (int d = 0; d < D; ++d) gen_functions(g, nets[d], "_n" + std::to_string(d), true);
+  // the chosen network's plan (warp-uniform per ministep)
+  g.s += "__device__ __forceinline__ float jit_change_stats32(int net, const DevProblem &P,\n"
+         "    const Slice &S, const StepCtx &X, int j, int aij, int aji, float *d32, float *absf) {\n"
+         "  switch (net) {\n";
+  for (int d = 0; d < D; ++d)
+    g.put("    case %d: return jit_change_stats32_n%d(P, S, X, j, aij, aji, d32, absf);\n", d, d);
+  g.s += "    default: *absf = 0.f; return 0.f;\n  }\n}\n";
+  g.s += "template <bool TERMS>\n"
+         "__device__ __forceinline__ double jit_change_stats(int net, const DevProblem &P,\n"
+         "    const Slice &S, const StepCtx &X, int j, int aij, int aji, double *d) {\n"
+         "  switch (net) {\n";
+  for (int d = 0; d < D; ++d)
+    g.put("    case %d: return jit_change_stats_n%d<TERMS>(P, S, X, j, aij, aji, d);\n", d, d);
+  g.s += "    default: return 0.0;\n  }\n}\n}  // namespace cusna\n";
+  return g.s;
 }
 
 namespace {
@@ -288,7 +309,12 @@ const Driver &driver() {
 }
 
 // ---- compilation -------------------------------------------------------------
-const char *kNames[2] = {"cusna::period_kernel<256>", "cusna::period_kernel<512>"};
+const char *kPeriodNames[2] = {"cusna::period_kernel<256>", "cusna::period_kernel<512>"};
+const char *kMultiNames[2] = {"cusna::multi_kernel<256>", "cusna::multi_kernel<512>"};
+
+bool is_multi(const std::string &spec) {
+  return spec.compare(0, std::strlen(kJitMultiTag), kJitMultiTag) == 0;
+}
 
 struct Compiled {
   int status = -1;             // 0 ok
@@ -305,8 +331,11 @@ Compiled compile_spec(const std::string &spec) {
     C.log = "NVRTC is not available";
     return C;
   }
+  const bool multi = is_multi(spec);
+  const char *const *kNames = multi ? kMultiNames : kPeriodNames;
   const std::string src = std::string("#include \"saom_kernel.cuh\"\n") + spec +
-                          "#include \"saom_period.cuh\"\n";
+                          (multi ? "#include \"saom_multi_kernel.cuh\"\n"
+                                 : "#include \"saom_period.cuh\"\n");
   const auto t0 = std::chrono::steady_clock::now();
   nvrtcProgram prog = nullptr;
   if (N.create(&prog, src.c_str(), "cusna_period_jit.cu", kJitHeaderCount, kJitHeaderSources,
@@ -314,7 +343,7 @@ Compiled compile_spec(const std::string &spec) {
     C.log = "nvrtcCreateProgram failed";
     return C;
   }
-  for (const char *nm : kNames) N.add_name(prog, nm);
+  for (int q = 0; q < 2; ++q) N.add_name(prog, kNames[q]);
   // CUSNA_JIT_MINB: resident 256-thread CTAs per SM the register budget of
   // the 256-thread instantiation allows (default 3: 85 registers; measured
   // faster than 2 on the C2 workload, 75 vs 79 ms, and equal on C4)
@@ -432,7 +461,15 @@ bool load_entry(Entry &E) {
 
 }  // namespace
 
+namespace {
+std::atomic<int> g_mode_override{-1};   // -1: none
+}
+
+void jit_set_mode(int mode) { g_mode_override.store(mode); }
+
 int jit_mode() {
+  const int o = g_mode_override.load();
+  if (o >= 0) return o;
   static const int mode = [] {
     const char *s = std::getenv("CUSNA_JIT");
     if (!s) return 1;
@@ -446,6 +483,7 @@ int jit_mode() {
 bool jit_get(const std::string &spec, JitKernel *out, bool now) {
   const int mode = jit_mode();
   if (mode == 0) return false;
+  now = now || mode == 2;
   Registry &R = reg();
   Entry *E = nullptr;
   bool compile_now = false;
@@ -460,8 +498,8 @@ bool jit_get(const std::string &spec, JitKernel *out, bool now) {
     }
     if (E->state == S_FAILED) return false;
     ++E->uses;
-    if (E->state == S_IDLE && (now || mode == 2 || E->uses >= uses_before_compile())) {
-      if (now || mode == 2) {
+    if (E->state == S_IDLE && (now || E->uses >= uses_before_compile())) {
+      if (now) {
         E->state = S_QUEUED;
         compile_now = true;
       } else {
@@ -529,6 +567,28 @@ cudaError_t launch_period_jit(const JitKernel &K, const LaunchShape &sh, const D
   int G = sh.G;
   void *args[] = {&probs, &unit_start, &nprob, &total, &counter, &lay, &G, &cols_scratch,
                   &rows_scratch, &cols_words};
+  const CUresult r = D.launch(f, (unsigned)sh.ctas, 1, 1, (unsigned)threads, 1, 1, (unsigned)dyn,
+                              (CUstream)st, args, nullptr);
+  if (r != CUDA_SUCCESS) return cudaErrorLaunchFailure;
+  note_launch();
+  return cudaSuccess;
+}
+
+cudaError_t launch_multi_jit(const JitKernel &K, const LaunchShape &sh, const DevProblem *nets,
+                             const MultiDev &md, int M, unsigned long long *counter,
+                             uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
+                             cudaStream_t st) {
+  const Driver &D = driver();
+  const int threads = 32 * sh.G * sh.teams_per_cta;
+  const size_t dyn = sh.lay.bytes * md.D * sh.teams_per_cta;
+  CUfunction f = (CUfunction)(threads <= 256 ? K.f256 : K.f512);
+  if (!D.ok || !f) return cudaErrorInvalidDeviceFunction;
+  if (D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  MultiDev mdv = md;
+  SliceLayout lay = sh.lay;
+  int G = sh.G, Mv = M;
+  void *args[] = {&nets, &mdv, &Mv, &counter, &lay, &G, &cols_scratch, &rows_scratch, &cols_words};
   const CUresult r = D.launch(f, (unsigned)sh.ctas, 1, 1, (unsigned)threads, 1, 1, (unsigned)dyn,
                               (CUstream)st, args, nullptr);
   if (r != CUDA_SUCCESS) return cudaErrorLaunchFailure;

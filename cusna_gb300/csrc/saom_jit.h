@@ -24,13 +24,18 @@ struct JitPlan {
   std::vector<int> kind, cfn, tid, ety, i0, i1, i2;
 };
 
-// Source text of the specialised float32 effect evaluation (the key of the
-// compiled kernel).
+// Source text of the specialised effect evaluation (the key of the compiled
+// kernel): of the period kernel for one plan, or of the multi-network kernel
+// for the networks' plans (its text starts with kJitMultiTag).
 std::string jit_spec_source(const JitPlan &J);
+std::string jit_multi_spec_source(const std::vector<JitPlan> &nets);
+constexpr const char *kJitMultiTag = "// cusna specialisation: multi-network kernel";
 
 // 0: off, 1: background compilation after CUSNA_JIT_AFTER uses, 2: compile on
 // first use.
 int jit_mode();
+// Overrides CUSNA_JIT for the process (mode as jit_mode; -1 restores it).
+void jit_set_mode(int mode);
 
 // Handles of a compiled and loaded specialisation (CUfunction of the 256- and
 // 512-thread instantiations).
@@ -49,6 +54,10 @@ cudaError_t launch_period_jit(const JitKernel &K, const LaunchShape &sh, const D
                               const long long *unit_start, int nprob, long long total,
                               unsigned long long *counter, uint32_t *cols_scratch,
                               uint32_t *rows_scratch, size_t cols_words, cudaStream_t st);
+cudaError_t launch_multi_jit(const JitKernel &K, const LaunchShape &sh, const DevProblem *nets,
+                             const MultiDev &md, int M, unsigned long long *counter,
+                             uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
+                             cudaStream_t st);
 // NVRTC compile of spec without loading it (no device needed): 0 on success,
 // else the NVRTC log in *log.
 int jit_compile_only(const std::string &spec, std::string *log, double *seconds);

@@ -27,20 +27,7 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
                           cudaStream_t st);
 int period_blocks_per_sm(int threads, size_t dyn_smem);
 
-// Multi-network problem: what the kernel needs beyond the per-network problems
-// (one DevProblem per network, holding that network's effects).
-struct MultiDev {
-  int D, n, W, nact, k;
-  const int *act;                 // nact active actors first
-  const float *lam;               // M*D rates
-  uint32_t k0, k1;                // Philox key
-  int goff[CUSNA_MAXNET + 1];     // network d's effects: gidx[goff[d] .. goff[d+1])
-  const int *gidx;                // their indices in the caller's effect order
-  float *rscores, *scores;        // device outputs (any may be null)
-  double *ntim;
-  int *steps;
-  uint8_t *a_ends;
-};
+static_assert(kMaxNet == CUSNA_MAXNET, "network capacity of the kernels and the ABI");
 int multi_blocks_per_sm(int threads, size_t dyn_smem);
 cudaError_t launch_multi(const LaunchShape &sh, const DevProblem *nets, const MultiDev &md, int M,
                          unsigned long long *counter, uint32_t *cols_scratch,

@@ -45,6 +45,25 @@ def specialise_check(m: Marshalled) -> float:
     return sec.value
 
 
+def specialise_check_multi(m) -> float:
+    """specialise_check for a marshalled multi-network period (marshal_multi)."""
+    lib = load_library()
+    buf = C.create_string_buffer(1 << 16)
+    sec = C.c_double(0.0)
+    st = lib.cusna_saom_specialise_check_multi(C.byref(m.problem), buf, len(buf), C.byref(sec))
+    if st != 0:
+        raise RuntimeError(f"specialised multi-network kernel: status {st}: "
+                           f"{buf.value.decode()[:2000]}")
+    return sec.value
+
+
+def specialise_mode(mode: int) -> None:
+    """Override CUSNA_JIT for the process: 0 never, 1 background after a few
+    uses, 2 on first use, -1 back to the environment's setting."""
+    lib = load_library()
+    check(lib.cusna_saom_specialise_mode(int(mode)), "cusna_saom_specialise_mode", lib)
+
+
 def specialise_wait(seconds: float = 120.0) -> int:
     """Wait for background compilations of specialised kernels; returns how
     many have completed."""

@@ -425,6 +425,15 @@ CUSNA_API cusna_status cusna_measure_fp64_tflops(double *tflops);
 CUSNA_API cusna_status cusna_saom_specialise_check(const cusna_saom_problem *problem, char *log,
                                                    size_t log_len, double *seconds);
 CUSNA_API cusna_status cusna_saom_specialise_wait(double seconds, int32_t *compiled);
+/* Overrides CUSNA_JIT for the process: 0 never specialise, 1 compile in the
+ * background after a few uses, 2 compile on first use, -1 back to CUSNA_JIT. */
+CUSNA_API cusna_status cusna_saom_specialise_mode(int32_t mode);
+/* cusna_saom_specialise_check for the multi-network kernel (the networks'
+ * effect plans of a multi-network problem). cusna_saom_simulate_multi runs the
+ * specialised kernel once it is compiled, with bit-identical outputs. */
+CUSNA_API cusna_status cusna_saom_specialise_check_multi(const cusna_saom_multi_problem *problem,
+                                                         char *log, size_t log_len,
+                                                         double *seconds);
 
 /* ---- moment surrogate (no counterpart in the reference) --------------------
  * A multilayer perceptron n_in -> hidden -> hidden -> n_out with GELU

@@ -90,3 +90,34 @@ def test_gpu_plan_switches_to_the_specialised_kernel(gpu_lib):
                 np.testing.assert_array_equal(v, ref[key], err_msg=f"epoch {epoch}: {key}")
     finally:
         plan.close()
+
+
+def test_specialised_multi_network_source_compiles(built_lib):
+    from cusna_gb300 import sim
+    from cusna_gb300.glue import marshal_multi
+    ms = []
+    for kind in WL.MULTI_KINDS:
+        inp, seed, lam, th = WL.multi_case(kind, seed=1)
+        ms.append(marshal_multi(inp, 2, seed, lam, th))
+    with cf.ThreadPoolExecutor(max_workers=8) as ex:
+        secs = list(ex.map(sim.specialise_check_multi, ms))
+    assert all(s > 0 for s in secs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,D,n", [("cross", 2, 40), ("dyadic", 3, 33), ("symmetric", 4, 65),
+                                      ("empty_net", 3, 50)])
+def test_gpu_specialised_multi_network_kernel_is_bit_identical(gpu_lib, kind, D, n):
+    """With specialisation off the library kernel runs; with compile-on-first-use
+    the specialised kernel runs; the outputs are the same bit for bit."""
+    from cusna_gb300 import sim
+    from cusna_gb300.glue import marshal_multi
+    inp, seed, lam, th = WL.multi_case(kind, seed=n, n=n, M=6, D=D)
+    try:
+        sim.specialise_mode(0)
+        lib_out = sim.simulate_multi(marshal_multi(inp, 6, seed, lam, th))
+        sim.specialise_mode(2)
+        spec_out = sim.simulate_multi(marshal_multi(inp, 6, seed, lam, th))
+    finally:
+        sim.specialise_mode(-1)
+    assert_identical(lib_out, spec_out, f"{kind}/D={D}/n={n}")
