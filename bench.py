@@ -90,10 +90,16 @@ def smem_bytes_per_network_ministep(n, W):
 # captures of the bench's own timed launch (smsp__inst_executed.sum over the
 # launch's 6,557,430 network ministeps; n=200, k=8, 4096 chains, autotuned
 # shape): the kernel specialised to the effect plan and the library kernel.
-INST_PER_MINISTEP = {("c2", True): 6600.0, ("c2", False): 10100.0}
+INST_PER_MINISTEP = {("c2", True): 6280.0, ("c2", False): 10100.0}
+# DRAM bytes of one period-kernel launch per chain (the problem and the
+# outputs), from the full ncu capture of the specialised kernel at 1024 chains
+# (1.346 MB read + 0.203 MB written); a launch of M chains moves at most M times
+# this (the problem's share does not grow with M).
+DRAM_BYTES_PER_CHAIN = {"c2": (1346048.0 + 203008.0) / 1024}
 
 
-def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, specialised=True):
+def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, specialised=True,
+                    chains=0):
     """The period kernel is latency-bound: its state is on chip (DRAM moves only
     the problem and the outputs) and no pipe is busier than a quarter of its
     peak, so its ceiling is the SMs' instruction issue rate (4 warp-instructions
@@ -113,7 +119,11 @@ def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, spec
     flops = flops_per_network_ministep(n, k) * rate / 1e12
     return {"bound": "issue", "achieved": achieved, "peak": peak,
             "unit": "G warp-instructions/s", "frac": achieved / peak if achieved else None,
-            "traffic": None, "kernel_ms": kernel_ms, "network_ministeps_per_s": rate,
+            "traffic": (DRAM_BYTES_PER_CHAIN[workload] * chains
+                        if workload in DRAM_BYTES_PER_CHAIN and chains else None),
+            "traffic_source": "ncu dram__bytes_read+write per chain at 1024 chains, times the "
+                              "launch's chains (an upper bound)",
+            "kernel_ms": kernel_ms, "network_ministeps_per_s": rate,
             "inst_per_ministep": ipm, "sm_mhz": mhz,
             "peak_source": "4 warp-instructions per cycle per SM x SMs x sampled SM clock",
             "algorithmic": {
@@ -659,7 +669,7 @@ def main():
     clk = clocks.summary(local)
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     roofline = period_roofline(args.workload, n, (n + 31) // 32, k, net_steps, kern_avg_ms, sm_count,
-                               clk, specialised=all(specialised))
+                               clk, specialised=all(specialised), chains=M)
     line = {
         "metric": "ministeps/s", "value": value, "unit": "ministeps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
