@@ -217,7 +217,9 @@ struct KeyTop {
   int j1;
 };
 // alters reach a lane in ascending j: a key equal to the best is not better
-// (its upper bound then reaches b1, which sends the choice to float64)
+// (its upper bound then reaches b1, which sends the choice to float64). A NaN
+// key or bound (float32 overflow, or non-finite inputs) certifies nothing: it
+// raises ub2 to infinity, so the exact float64 keys decide.
 __device__ __forceinline__ void keytop_add(KeyTop &t, float g, float E, int j) {
   if (g > t.b1) {
     t.ub2 = fmaxf(t.ub2, __fadd_rn(t.b1, t.e1));
@@ -225,7 +227,8 @@ __device__ __forceinline__ void keytop_add(KeyTop &t, float g, float E, int j) {
     t.e1 = E;
     t.j1 = j;
   } else {
-    t.ub2 = fmaxf(t.ub2, __fadd_rn(g, E));   // fmaxf drops a NaN key
+    const float u = __fadd_rn(g, E);
+    t.ub2 = (u != u) ? INFINITY : fmaxf(t.ub2, u);
   }
 }
 __device__ __forceinline__ void keytop_merge(KeyTop &a, const KeyTop &c) {
@@ -420,9 +423,11 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
 
   // ---- the chosen alter ---------------------------------------------------
   // The float32 keys decide when the best key's lower bound exceeds every
-  // other alter's upper bound. Otherwise every alter whose upper bound
-  // reaches that lower bound gets its exact float64 key (the reference's
-  // f_j - log(-log u_j)) and those decide, ties to the smaller j.
+  // other alter's upper bound. Otherwise every permitted alter whose upper
+  // bound is not below that lower bound (a NaN on either side counts as
+  // reaching it) gets its exact float64 key (the reference's
+  // f_j - log(-log u_j)) and those decide, ties to the smaller j. The "no
+  // change" alter always has a finite key, so a choice always exists.
   int jstar;
   const float lb = __fsub_rn(top.b1, top.e1);
   if (lb > top.ub2) {
@@ -431,7 +436,8 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     long long bk = dkey(-1e300);
     int bj = 0x7FFFFFFF;
     for (int j = T.tl; j < n; j += L) {
-      if (S.gbuf[j] >= lb) {
+      const bool okj = (S.okbits[j >> 5] >> (j & 31)) & 1u;
+      if (okj && !(S.gbuf[j] < lb)) {
         double f = 0.0;
         if (j != i) {
           const int aij = bit_of(S.rowsT, n, i, j);
@@ -453,6 +459,8 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     }
     jstar = team_argmax(T, bk, bj, S.red + 29 * T.G);
   }
+  // never an index outside the network, whatever the inputs
+  if ((unsigned)jstar >= (unsigned)n) jstar = i;
 
   // ---- score update (lane e updates effect e) and toggle ----------------
   // the chosen alter's change statistics in float64, as the reference adds them

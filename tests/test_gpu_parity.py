@@ -201,3 +201,21 @@ def test_gpu_large_n_rows_in_global_scratch(gpu_lib, port):
     c = WL.parity_case("conditional", seed=3, n=1500, M=2)
     c["inp"].target_dist = 400
     assert_parity(run_case(GpuEngine(), c), run_case(port, c), "n1500")
+
+
+def test_gpu_predictors_beyond_float32_range_choose_as_the_reference(gpu_lib, port):
+    """A parameter near the float32 maximum makes float32 predictors infinite
+    or NaN: those keys certify nothing, the exact float64 keys decide, and the
+    trajectories still equal the CPU engine's (the float32 log-sum-exp scores
+    are not compared: their terms overflow)."""
+    c = WL.parity_case("structural", seed=8, n=40, M=4)
+    th = np.asarray(c["theta"], dtype=np.float64).copy()
+    th[1] = 3.0e38
+    c = dict(c, theta=th)
+    for spec in (-1, 1):
+        got = run_case(GpuEngine(specialise=spec), c)
+        ref = run_case(port, c)
+        for key in ("steps", "dist", "dist_stat", "a_ends"):
+            if key in ref:
+                np.testing.assert_array_equal(got[key], ref[key], err_msg=f"{spec}:{key}")
+        np.testing.assert_allclose(got["ntim"], ref["ntim"], rtol=1e-13, atol=0)
