@@ -289,7 +289,7 @@ __device__ __forceinline__ void block_lse(float *rec, float w, const float *d32,
   if (writer && q <= k) rec[q] = v[0];
 }
 
-// The block records of one pass combined by the team's warp 0: lane l takes
+// The block records of one pass combined by one warp of the team: lane l takes
 // blocks l, l+32, ... in order and adds each block's sums rescaled to the
 // overall maximum (float32), then a fixed butterfly adds the lanes' partial
 // sums (warp_multi_sum). Quantity q lands in S.red[32G + q], past the warp
@@ -297,7 +297,6 @@ __device__ __forceinline__ void block_lse(float *rec, float w, const float *d32,
 // block index only, so the result is the same for every team size.
 template <int V>
 __device__ __forceinline__ void combine_blocks(const Team &T, const Slice &S, int n, int k) {
-  if (T.warp != 0) return;
   const int nb = (n + 31) >> 5;
   float M = -INFINITY;
   for (int b = T.lane; b < nb; b += 32) M = fmaxf(M, S.blk[(size_t)b * (k + 2)]);
@@ -410,15 +409,6 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
 #endif
   }
   T.sync();
-  // the block records combined into quantity q (0: sum of weights, 1+e:
-  // weighted sum of d_e) rescaled to the overall maximum, in S.red[32G + q]
-#ifdef CUSNA_JIT_SPEC
-  combine_blocks<(CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))>(T, S, n, CUSNA_JIT_K);
-#else
-  if (k + 1 <= 8) combine_blocks<8>(T, S, n, k);
-  else if (k + 1 <= 16) combine_blocks<16>(T, S, n, k);
-  else combine_blocks<32>(T, S, n, k);
-#endif
   const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
 
   // ---- the chosen alter ---------------------------------------------------
@@ -461,6 +451,22 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   }
   // never an index outside the network, whatever the inputs
   if ((unsigned)jstar >= (unsigned)n) jstar = i;
+
+  // the block records combined into quantity q (0: sum of weights, 1+e:
+  // weighted sum of d_e) rescaled to the overall maximum, in S.red[32G + q];
+  // with several warps, by a warp other than the chosen alter's owner, which
+  // meanwhile forms the chosen alter's float64 statistics
+  const int owner_warp = (jstar % L) >> 5;
+  if (T.warp == (T.G > 1 ? (owner_warp + 1) % T.G : 0)) {
+#ifdef CUSNA_JIT_SPEC
+    combine_blocks<(CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))>(T, S, n,
+                                                                                  CUSNA_JIT_K);
+#else
+    if (k + 1 <= 8) combine_blocks<8>(T, S, n, k);
+    else if (k + 1 <= 16) combine_blocks<16>(T, S, n, k);
+    else combine_blocks<32>(T, S, n, k);
+#endif
+  }
 
   // ---- score update (lane e updates effect e) and toggle ----------------
   // the chosen alter's change statistics in float64, as the reference adds them
