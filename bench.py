@@ -117,10 +117,17 @@ def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, spec
     fp32_peak = 256.0 * sm_count * hz / 1e12          # TFLOP/s, 128 FMA per cycle per SM
     smem = smem_bytes_per_network_ministep(n, W) * rate / 1e12
     flops = flops_per_network_ministep(n, k) * rate / 1e12
+    traffic = (DRAM_BYTES_PER_CHAIN[workload] * chains
+               if workload in DRAM_BYTES_PER_CHAIN and chains else None)
+    hbm_peak, hbm_src = measured_hbm_gbs()
+    dram = None
+    if traffic is not None:
+        gbps = traffic / (kernel_ms / 1e3) / 1e9
+        dram = {"GBps": gbps, "peak_GBps": hbm_peak, "frac": gbps / hbm_peak,
+                "peak_source": hbm_src}
     return {"bound": "issue", "achieved": achieved, "peak": peak,
             "unit": "G warp-instructions/s", "frac": achieved / peak if achieved else None,
-            "traffic": (DRAM_BYTES_PER_CHAIN[workload] * chains
-                        if workload in DRAM_BYTES_PER_CHAIN and chains else None),
+            "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read+write per chain at 1024 chains, times the "
                               "launch's chains (an upper bound)",
             "kernel_ms": kernel_ms, "network_ministeps_per_s": rate,
@@ -130,7 +137,19 @@ def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, spec
                 "smem_bytes_per_ministep": smem_bytes_per_network_ministep(n, W),
                 "smem_TBps": smem, "smem_peak_TBps": smem_peak, "smem_frac": smem / smem_peak,
                 "flops_per_ministep": flops_per_network_ministep(n, k),
-                "fp32_TFLOPs": flops, "fp32_peak_TFLOPs": fp32_peak, "fp32_frac": flops / fp32_peak}}
+                "fp32_TFLOPs": flops, "fp32_peak_TFLOPs": fp32_peak, "fp32_frac": flops / fp32_peak,
+                "dram": dram}}
+
+
+def measured_hbm_gbs():
+    """HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json beside
+    this file), else the recipe's fallback figure."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback (6.8 TB/s, one earlier GB300 measurement)"
 
 
 class Clocks:
