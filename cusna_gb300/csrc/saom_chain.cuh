@@ -502,8 +502,8 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
   const double pnet = __ddiv_rn(lam, __dadd_rn(lam, lamb));
   long long dist = 0, bdist = 0, ms = 0, msb = 0;
   double t = 0.0, rho = 0.0;
-  double d[24];
-  float d32[24];
+  double d[kMaxEff];
+  float d32[kMaxEff];
 
   for (;;) {
     int i;

@@ -20,6 +20,7 @@ namespace cusna {
 
 // Runaway-chain cap of the CPU engine (src/libcusna_saom_cpu.cpp:115).
 constexpr long long kMaxSteps = 4000000;
+constexpr int kMaxEff = 24;  // network effects per model (CUSNA_MAXEFF)
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
 // Problem flags (DevProblem::flags).

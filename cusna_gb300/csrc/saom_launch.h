@@ -28,6 +28,7 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
 int period_blocks_per_sm(int threads, size_t dyn_smem);
 
 static_assert(kMaxNet == CUSNA_MAXNET, "network capacity of the kernels and the ABI");
+static_assert(kMaxEff == CUSNA_MAXEFF, "effect capacity of the kernels and the ABI");
 int multi_blocks_per_sm(int threads, size_t dyn_smem);
 cudaError_t launch_multi(const LaunchShape &sh, const DevProblem *nets, const MultiDev &md, int M,
                          unsigned long long *counter, uint32_t *cols_scratch,

@@ -39,8 +39,8 @@ static __device__ void run_chain_multi(const Team &T, const DevProblem *nets, co
   const double den = __dmul_rn((double)md.nact, lam_tot);
   long long ms = 0, msd[kMaxNet] = {};
   double t = 0.0;
-  double dbuf[24];
-  float d32[24];
+  double dbuf[kMaxEff];
+  float d32[kMaxEff];
   const Slice S0 = multi_slice(base, lay, 0, cols_g, rows_g, cols_words);
   // network w's rows: rows0 + w*net_stride words (in shared memory the slices
   // follow one another; in global scratch each network has cols_words)
