@@ -358,8 +358,9 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   // The log-sum-exp sums are formed per block of 32 alters (alter j on lane
   // j mod 32, whatever the team size): the block maximum and the block's
   // sums of exp(f - max) and exp(f - max) d_e with a fixed warp reduction,
-  // stored per block and combined in block order after the pass, so the
-  // scores do not depend on the launch shape.
+  // stored per block and combined after the choice in an order fixed by the
+  // block index (combine_blocks), so the scores do not depend on the launch
+  // shape.
   KeyTop best{-INFINITY, 0.f, -INFINITY, 0x7FFFFFFF};
   const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
   for (int jb = 32 * T.warp; jb < n; jb += L) {
