@@ -113,7 +113,9 @@ T *at(size_t off) {
 // Per-problem host-side facts read during validation, and the effect plan.
 struct Facts {
   std::vector<int> tid, i0, i1, i2, rk, ety;
-  std::string spec;                        // effect plan of the specialised kernel (saom_jit.h)
+  // effect plan of the specialised kernel (saom_jit.h): with the problem's
+  // word count compiled in (spec_w), and with it read at run time (spec)
+  std::string spec, spec_w;
   JitPlan jplan;
   int flags = 0;
   std::vector<int> kind, cfn, offd, offt;  // effect plan, k each
@@ -383,7 +385,12 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
                             F_PC_RICIRJ);
     J.kind = F.kind; J.cfn = F.cfn; J.tid = F.tid; J.ety = F.ety;
     J.i0 = F.i0; J.i1 = F.i1; J.i2 = F.i2;
-    if (!F.multi) F.spec = jit_spec_source(J);
+    if (!F.multi) {
+      F.spec = jit_spec_source(J);
+      J.W = p->W;
+      F.spec_w = jit_spec_source(J);
+      J.W = 0;
+    }
   }
   // gwdsp change statistics index the weight table at p+1 with p <= n-2 on a
   // network without self-ties; a self-tie in the start network could push p to
@@ -814,13 +821,26 @@ TuneKey tune_key(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bo
 
 // The specialised kernel of a launch: every problem must have the same effect
 // plan. spec_mode: 0 as CUSNA_JIT says, -1 never, 1 compile now if needed.
+// The specialisation a launch of these problems can use: with the word count
+// compiled in when every problem has the same, else with it read at run time;
+// "" when the effect plans differ.
+std::string launch_spec(const std::vector<Job> &jobs) {
+  if (jobs.empty() || jobs[0].F.spec.empty()) return "";
+  bool same_w = true, same = true;
+  for (const Job &J : jobs) {
+    same_w = same_w && J.F.spec_w == jobs[0].F.spec_w;
+    same = same && J.F.spec == jobs[0].F.spec;
+  }
+  return same_w ? jobs[0].F.spec_w : (same ? jobs[0].F.spec : "");
+}
+
 bool jit_for(const std::vector<Job> &jobs, int spec_mode, JitKernel *jk) {
-  if (spec_mode < 0 || jobs.empty() || jobs[0].F.spec.empty()) return false;
-  for (const Job &J : jobs)
-    if (J.F.spec != jobs[0].F.spec) return false;
+  if (spec_mode < 0) return false;
+  const std::string spec = launch_spec(jobs);
+  if (spec.empty()) return false;
   // spec_mode 1: compile and load now (tests, and callers that know the
   // effect plan will run long enough)
-  return jit_get(jobs[0].F.spec, jk, spec_mode > 0);
+  return jit_get(spec, jk, spec_mode > 0);
 }
 
 // the model's two best shapes of each team size, in the model's order
@@ -1129,7 +1149,10 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
   }
   // the multi-network kernel specialised to the networks' effect plans
   std::vector<JitPlan> jplans;
-  for (int d = 0; d < D; ++d) jplans.push_back(jobs[d].F.jplan);
+  for (int d = 0; d < D; ++d) {
+    jplans.push_back(jobs[d].F.jplan);
+    jplans.back().W = W;   // the networks share the actors
+  }
   const std::string mspec = jit_multi_spec_source(jplans);
   if (check_only) {
     if (jit_compile_only(mspec, log, seconds) != 0) {
@@ -1385,9 +1408,7 @@ cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *
   P->cols = o_cols == NONE ? nullptr : at<uint32_t>(o_cols);
   P->rows = o_rows == NONE ? nullptr : at<uint32_t>(o_rows);
   P->cols_words = cols_words;
-  bool same = true;
-  for (auto &J : jobs) same = same && J.F.spec == jobs[0].F.spec;
-  if (same) P->spec = jobs[0].F.spec;
+  P->spec = launch_spec(jobs);
   *out = P;
   return CUSNA_OK;
 }
@@ -1528,7 +1549,7 @@ CUSNA_API cusna_status cusna_saom_specialise_check(const cusna_saom_problem *pro
   if (s != CUSNA_OK) return s;
   std::string text;
   double sec = 0.0;
-  const int st = jit_compile_only(F.spec, &text, &sec);
+  const int st = jit_compile_only(F.spec_w, &text, &sec);
   if (seconds) *seconds = sec;
   if (log && log_len) {
     const size_t m = std::min(log_len - 1, text.size());
