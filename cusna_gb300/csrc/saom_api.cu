@@ -114,7 +114,7 @@ T *at(size_t off) {
 struct Facts {
   std::vector<int> tid, i0, i1, i2, rk, ety;
   // effect plan of the specialised kernel (saom_jit.h): with the problem's
-  // word count compiled in (spec_w), and with it read at run time (spec)
+  // actor count compiled in (spec_w), and with it read at run time (spec)
   std::string spec, spec_w;
   JitPlan jplan;
   int flags = 0;
@@ -387,9 +387,9 @@ cusna_status validate(const cusna_saom_problem *p, const cusna_saom_result *r, b
     J.i0 = F.i0; J.i1 = F.i1; J.i2 = F.i2;
     if (!F.multi) {
       F.spec = jit_spec_source(J);
-      J.W = p->W;
+      J.n = p->n;
       F.spec_w = jit_spec_source(J);
-      J.W = 0;
+      J.n = 0;
     }
   }
   // gwdsp change statistics index the weight table at p+1 with p <= n-2 on a
@@ -821,7 +821,7 @@ TuneKey tune_key(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bo
 
 // The specialised kernel of a launch: every problem must have the same effect
 // plan. spec_mode: 0 as CUSNA_JIT says, -1 never, 1 compile now if needed.
-// The specialisation a launch of these problems can use: with the word count
+// The specialisation a launch of these problems can use: with the actor count
 // compiled in when every problem has the same, else with it read at run time;
 // "" when the effect plans differ.
 std::string launch_spec(const std::vector<Job> &jobs) {
@@ -1151,7 +1151,7 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
   std::vector<JitPlan> jplans;
   for (int d = 0; d < D; ++d) {
     jplans.push_back(jobs[d].F.jplan);
-    jplans.back().W = W;   // the networks share the actors
+    jplans.back().n = n;   // the networks share the actors
   }
   const std::string mspec = jit_multi_spec_source(jplans);
   if (check_only) {

@@ -95,10 +95,10 @@ void gen_index(Gen &g, int cfn) {
   }
 }
 
-// the word count: a constant when the plan fixes it
-void gen_words(Gen &g, const JitPlan &J) {
-  if (J.W > 0) g.put("  constexpr int W = %d;\n", J.W);
-  else g.s += "  const int W = P.W;\n";
+// the actor and word counts: constants when the plan fixes them
+void gen_shape(Gen &g, const JitPlan &J) {
+  if (J.n > 0) g.put("  constexpr int n = %d, W = %d;\n", J.n, (J.n + 31) / 32);
+  else g.s += "  const int n = P.n, W = P.W;\n";
 }
 
 // jit_change_stats32<sfx> and jit_change_stats<sfx><TERMS> of one effect plan
@@ -109,8 +109,8 @@ void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi)
   // float32 pass (change_stats32)
   g.put("__device__ __forceinline__ float jit_change_stats32%s(const DevProblem &P, const Slice &S,\n"
         "    const StepCtx &X, int j, int aij, int aji, float *d32, float *absf) {\n", x);
-  g.s += "  const int n = P.n, i = X.i;\n";
-  gen_words(g, J);
+  g.s += "  const int i = X.i;\n";
+  gen_shape(g, J);
   g.s += "  (void)n; (void)W; (void)i; (void)aji;\n";
   gen_pair_counts(g, fl);
   g.s += "  const uint32_t sg = aij ? 0x80000000u : 0u;\n"
@@ -158,8 +158,8 @@ void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi)
   g.put("template <bool TERMS>\n"
         "__device__ __forceinline__ double jit_change_stats%s(const DevProblem &P, const Slice &S,\n"
         "    const StepCtx &X, int j, int aij, int aji, double *d) {\n", x);
-  g.s += "  const int n = P.n, i = X.i;\n";
-  gen_words(g, J);
+  g.s += "  const int i = X.i;\n";
+  gen_shape(g, J);
   g.s += "  (void)n; (void)W; (void)i; (void)aji;\n"
          "  const unsigned long long sg = aij ? 0x8000000000000000ull : 0ull;\n"
          "  const bool ttab = (P.flags & F_THETA_TAB) != 0;\n  (void)ttab;\n";

@@ -21,8 +21,9 @@ namespace cusna {
 // The effect plan the specialised code is generated from.
 struct JitPlan {
   int pc_flags = 0;  // F_PC_* popcount needs
-  int W = 0;         // words per bit row when every problem of the launch has
-                     // it (compiled in: the popcount loops unroll), else 0
+  int n = 0;         // actors when every problem of the launch has the same
+                     // number (compiled in with W: the popcount loops unroll
+                     // and the strides are constants), else 0
   std::vector<int> kind, cfn, tid, ety, i0, i1, i2;
 };
 
