@@ -142,6 +142,12 @@ def test_gpu_surrogate_fit_matches_plain_fit_with_fewer_simulations():
     est = mom.mom_estimator(D.build_saom_data(waves), WL.c5_effects(cov), None, None, False,
                             dict(mom.DEFAULT_CONTROL), engine=eng)
     centre = WL.c5_theta_true()
+    # both fits run the period kernel specialised to this model: compiled
+    # first (the library compiles it in the background after a few uses)
+    from cusna_gb300 import sim
+    for _ in range(3):
+        mom.mom_simulate(est, centre, 64, np.random.default_rng(0), eng)
+    sim.specialise_wait(900.0)
     sf = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng)
     plain = mom.mom_run(est, theta0=centre, engine=eng)
     fs = sf.fit
