@@ -826,7 +826,12 @@ TuneKey tune_key(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp, bo
 // "" when the effect plans differ.
 std::string launch_spec(const std::vector<Job> &jobs) {
   if (jobs.empty() || jobs[0].F.spec.empty()) return "";
-  bool same_w = true, same = true;
+  // CUSNA_JIT_FIXED_N=0: never compile the actor count in
+  static const bool fixed_n = [] {
+    const char *e = std::getenv("CUSNA_JIT_FIXED_N");
+    return !(e && e[0] == '0');
+  }();
+  bool same_w = fixed_n, same = true;
   for (const Job &J : jobs) {
     same_w = same_w && J.F.spec_w == jobs[0].F.spec_w;
     same = same && J.F.spec == jobs[0].F.spec;

@@ -148,6 +148,11 @@ def test_gpu_surrogate_fit_matches_plain_fit_with_fewer_simulations():
     for _ in range(3):
         mom.mom_simulate(est, centre, 64, np.random.default_rng(0), eng)
     sim.specialise_wait(900.0)
+    # and the network's kernels and training graphs are warm (a tiny fit)
+    r = np.random.default_rng(0)
+    S.MlpSurrogate(S.N_IN, est.k + 1, S.HIDDEN).fit(r.standard_normal((2048, S.N_IN)),
+                                                      r.standard_normal((2048, est.k + 1)),
+                                                      epochs=2, n_group=S.N_IN - est.k - 1)
     sf = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng)
     plain = mom.mom_run(est, theta0=centre, engine=eng)
     fs = sf.fit
