@@ -90,7 +90,7 @@ def smem_bytes_per_network_ministep(n, W):
 # captures of the bench's own timed launch (smsp__inst_executed.sum over the
 # launch's 6,557,430 network ministeps; n=200, k=8, 4096 chains, autotuned
 # shape): the kernel specialised to the effect plan and the library kernel.
-INST_PER_MINISTEP = {("c2", True): 6035.0, ("c2", False): 10100.0}
+INST_PER_MINISTEP = {("c2", True): 5813.0, ("c2", False): 10100.0}
 # DRAM bytes of one period-kernel launch per chain (the problem and the
 # outputs), from the full ncu capture of the specialised kernel at 1024 chains
 # (1.478 MB read + 0.209 MB written); a launch of M chains moves at most M times
