@@ -283,6 +283,7 @@ const Nvrtc &nvrtc() {
 struct Driver {
   bool ok = false;
   decltype(&cuModuleLoadData) load = nullptr;
+  decltype(&cuModuleUnload) unload = nullptr;
   decltype(&cuModuleGetFunction) get_function = nullptr;
   decltype(&cuFuncSetAttribute) set_attr = nullptr;
   decltype(&cuLaunchKernel) launch = nullptr;
@@ -306,6 +307,9 @@ Driver load_driver() {
   sym(D.set_attr, "cuFuncSetAttribute");
   sym(D.launch, "cuLaunchKernel");
   sym(D.occupancy, "cuOccupancyMaxActiveBlocksPerMultiprocessor");
+  const bool required = ok;
+  sym(D.unload, "cuModuleUnload");   // optional: only a failed load's clean-up
+  ok = required;
   cudaGetLastError();
   D.ok = ok;
   return D;
@@ -461,7 +465,11 @@ bool load_entry(Entry &E) {
   if (D.load(&E.mod, E.comp.cubin.data()) != CUDA_SUCCESS) return false;
   CUfunction f[2];
   for (int q = 0; q < 2; ++q)
-    if (D.get_function(&f[q], E.mod, E.comp.lowered[q].c_str()) != CUDA_SUCCESS) return false;
+    if (D.get_function(&f[q], E.mod, E.comp.lowered[q].c_str()) != CUDA_SUCCESS) {
+      if (D.unload) D.unload(E.mod);
+      E.mod = nullptr;
+      return false;
+    }
   E.k.f256 = (void *)f[0];
   E.k.f512 = (void *)f[1];
   return true;
@@ -527,10 +535,14 @@ bool jit_get(const std::string &spec, JitKernel *out, bool now) {
   }
   if (compile_now) {
     Compiled c = compile_spec(spec);
-    std::lock_guard<std::mutex> lk(R.mu);
-    E->comp = std::move(c);
-    E->state = E->comp.status == 0 ? S_COMPILED : S_FAILED;
-    if (E->state == S_COMPILED) ++R.compiled;
+    {
+      std::lock_guard<std::mutex> lk(R.mu);
+      E->comp = std::move(c);
+      E->state = E->comp.status == 0 ? S_COMPILED : S_FAILED;
+      if (E->state == S_COMPILED) ++R.compiled;
+    }
+    // other threads asking for the same plan now wait on its state
+    R.cv.notify_all();
   }
   std::unique_lock<std::mutex> lk(R.mu);
   // asked for it now while the background compiler has it: wait for that
