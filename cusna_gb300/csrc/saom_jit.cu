@@ -358,7 +358,8 @@ Compiled compile_spec(const std::string &spec) {
   for (int q = 0; q < 2; ++q) N.add_name(prog, kNames[q]);
   // CUSNA_JIT_MINB: resident 256-thread CTAs per SM the register budget of
   // the 256-thread instantiation allows (default 3: 85 registers; measured
-  // faster than 2 on the C2 workload, 75 vs 79 ms, and equal on C4)
+  // on the n=200, 4096-chain workload against 2, 75 vs 79 ms, and against 4,
+  // 62.4 vs 66.5 ms; equal to 2 at n=1000)
   std::string minb = "-DCUSNA_MINB_256=3";
   if (const char *m = std::getenv("CUSNA_JIT_MINB")) minb = std::string("-DCUSNA_MINB_256=") + m;
   const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false",
