@@ -50,7 +50,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 from cusna_gb300 import workloads as WL  # noqa: E402
-from cusna_gb300.glue import marshal_period, result_dict  # noqa: E402
+from cusna_gb300.glue import marshal_period  # noqa: E402
 
 WORKLOADS = {
     "c2": "n=200 actors, wave-1 density 0.03, 8 effects (density, recip, transTrip, cycle3, "

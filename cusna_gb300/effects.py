@@ -8,7 +8,7 @@ reference fixture tests/testthat/fixtures/effects/effects.json.gz pins it.
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

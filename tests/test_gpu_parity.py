@@ -174,7 +174,6 @@ def test_gpu_network_and_behavior_stats(gpu_lib, port):
 
 
 def test_gpu_error_statuses(gpu_lib):
-    from cusna_gb300.abi import SaomProblem, SaomResult
     lib = gpu_lib
     assert lib.cusna_saom_simulate_period(None, None) == ERR_NULL_ARG
     c = WL.parity_case("baseline", seed=1)
