@@ -194,8 +194,7 @@ cudaError_t launch_gof(const uint8_t *a, int n, int M, int kind, const int *levl
                        int smem_optin, cudaStream_t st) {
   if (kind == 0 || kind == 1) {
     const size_t dyn = (size_t)(n + 1) * 4;
-    cudaError_t e = cudaFuncSetAttribute(degree_dist_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    cudaError_t e = raise_dyn_smem((const void *)degree_dist_kernel, dyn);
     if (e != cudaSuccess) return e;
     degree_dist_kernel<<<M, 512, dyn, st>>>(a, n, kind, levls, nlev, out);
     return cudaGetLastError();
@@ -211,8 +210,7 @@ cudaError_t launch_gof(const uint8_t *a, int n, int M, int kind, const int *levl
     const size_t rows_bytes = (size_t)n * W * 4;
     const int in_smem = scratch + rows_bytes <= (size_t)smem_optin;
     const size_t dyn = scratch + (in_smem ? rows_bytes : 0);
-    e = cudaFuncSetAttribute(geodesic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)dyn);
+    e = raise_dyn_smem((const void *)geodesic_kernel, dyn);
     if (e != cudaSuccess) return e;
     geodesic_kernel<<<M, threads, dyn, st>>>(rows, n, W, K, in_smem, added);
     e = cudaGetLastError();

@@ -562,12 +562,26 @@ bool jit_get(const std::string &spec, JitKernel *out, bool now) {
   return true;
 }
 
+// The dynamic shared memory limit of a loaded function only rises, for the
+// reason raise_dyn_smem gives (one value per function, shared by threads).
+static bool raise_jit_dyn_smem(CUfunction f, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_map<CUfunction, size_t> limit;
+  const Driver &D = driver();
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[f];
+  if (bytes <= cur) return true;
+  if (D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)bytes) != CUDA_SUCCESS)
+    return false;
+  cur = bytes;
+  return true;
+}
+
 int jit_blocks_per_sm(const JitKernel &K, int threads, size_t dyn_smem) {
   const Driver &D = driver();
   CUfunction f = (CUfunction)(threads <= 256 ? K.f256 : K.f512);
   if (!D.ok || !f) return 0;
-  if (D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn_smem) != CUDA_SUCCESS)
-    return 0;
+  if (!raise_jit_dyn_smem(f, dyn_smem)) return 0;
   int blocks = 0;
   if (D.occupancy(&blocks, f, threads, dyn_smem) != CUDA_SUCCESS) return 0;
   return blocks;
@@ -582,8 +596,7 @@ cudaError_t launch_period_jit(const JitKernel &K, const LaunchShape &sh, const D
   const size_t dyn = sh.lay.bytes * sh.teams_per_cta;
   CUfunction f = (CUfunction)(threads <= 256 ? K.f256 : K.f512);
   if (!D.ok || !f) return cudaErrorInvalidDeviceFunction;
-  if (D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn) != CUDA_SUCCESS)
-    return cudaErrorInvalidValue;
+  if (!raise_jit_dyn_smem(f, dyn)) return cudaErrorInvalidValue;
   SliceLayout lay = sh.lay;
   int G = sh.G;
   void *args[] = {&probs, &unit_start, &nprob, &total, &counter, &lay, &G, &cols_scratch,
@@ -604,8 +617,7 @@ cudaError_t launch_multi_jit(const JitKernel &K, const LaunchShape &sh, const De
   const size_t dyn = sh.lay.bytes * md.D * sh.teams_per_cta;
   CUfunction f = (CUfunction)(threads <= 256 ? K.f256 : K.f512);
   if (!D.ok || !f) return cudaErrorInvalidDeviceFunction;
-  if (D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn) != CUDA_SUCCESS)
-    return cudaErrorInvalidValue;
+  if (!raise_jit_dyn_smem(f, dyn)) return cudaErrorInvalidValue;
   MultiDev mdv = md;
   SliceLayout lay = sh.lay;
   int G = sh.G, Mv = M;

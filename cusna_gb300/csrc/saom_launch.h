@@ -68,6 +68,9 @@ cudaError_t launch_plan_prologue(DevProblem *probs, const unsigned long long *ba
                                  cudaStream_t st);
 long long kernel_launches();  // kernels launched so far by the calling thread
 void note_launch();           // counts a launch made outside the wrappers here
+// Raises a kernel's dynamic shared memory limit on the current device to at
+// least `bytes`; never lowers it (see saom_sim.cu).
+cudaError_t raise_dyn_smem(const void *func, size_t bytes);
 void set_last_error(const char *msg);  // text of cusna_last_error() for this thread
 cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
                             cudaStream_t st);

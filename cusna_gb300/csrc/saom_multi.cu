@@ -8,8 +8,7 @@ namespace cusna {
 int multi_blocks_per_sm(int threads, size_t dyn_smem) {
   int blocks = 0;
   auto kern = threads <= 256 ? multi_kernel<256> : multi_kernel<512>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem) !=
-      cudaSuccess) {
+  if (raise_dyn_smem((const void *)kern, dyn_smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -27,7 +26,7 @@ cudaError_t launch_multi(const LaunchShape &sh, const DevProblem *nets, const Mu
   const int threads = 32 * sh.G * sh.teams_per_cta;
   const size_t dyn = sh.lay.bytes * md.D * sh.teams_per_cta;
   auto kern = threads <= 256 ? multi_kernel<256> : multi_kernel<512>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  cudaError_t e = raise_dyn_smem((const void *)kern, dyn);
   if (e != cudaSuccess) return e;
   kern<<<sh.ctas, threads, dyn, st>>>(nets, md, M, counter, sh.lay, sh.G, cols_scratch,
                                       rows_scratch, cols_words);

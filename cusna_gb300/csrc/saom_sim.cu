@@ -4,6 +4,10 @@
 #include "saom_period.cuh"
 #include "saom_launch.h"
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace cusna {
 
 // ---- standalone statistics (cusna_network_stats_gpu / behavior_stats_gpu) ----
@@ -169,10 +173,27 @@ static cudaError_t counted(cudaError_t e) {
   return e;
 }
 
+// A kernel's dynamic shared memory limit is one value per function and
+// device, shared by every host thread. Setting it to each launch's own size
+// would let one thread lower it between another thread's setting and launch,
+// and fail that launch; so the limit only rises.
+cudaError_t raise_dyn_smem(const void *func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[{dev, func}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 template <int MAXT>
 static int blocks_per_sm_t(int threads, size_t dyn_smem) {
-  if (cudaFuncSetAttribute(period_kernel<MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)dyn_smem) != cudaSuccess) {
+  if (raise_dyn_smem((const void *)period_kernel<MAXT>, dyn_smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -197,7 +218,7 @@ cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const 
   const int threads = 32 * sh.G * sh.teams_per_cta;
   const size_t dyn = sh.lay.bytes * sh.teams_per_cta;
   auto kern = threads <= 256 ? period_kernel<256> : period_kernel<512>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  cudaError_t e = raise_dyn_smem((const void *)kern, dyn);
   if (e != cudaSuccess) return e;
   kern<<<sh.ctas, threads, dyn, st>>>(probs, unit_start, nprob, total, counter, sh.lay, sh.G,
                                       cols_scratch, rows_scratch, cols_words);
@@ -252,8 +273,7 @@ cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *
   int warps = (int)((200 * 1024) / slice);
   if (warps > 8) warps = 8;
   if (warps < 1) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(netstats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(slice * warps));
+  cudaError_t e = raise_dyn_smem((const void *)netstats_kernel, slice * warps);
   if (e != cudaSuccess) return e;
   int blocks = (M + warps - 1) / warps;
   if (blocks > 4 * sms) blocks = 4 * sms;
@@ -268,8 +288,7 @@ cudaError_t launch_behstats(const int *z, int n, int M, int kb, const int *bty, 
   int warps = (int)((200 * 1024) / per);
   if (warps > 8) warps = 8;
   if (warps < 1) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(behstats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(per * warps));
+  cudaError_t e = raise_dyn_smem((const void *)behstats_kernel, per * warps);
   if (e != cudaSuccess) return e;
   int blocks = (M + warps - 1) / warps;
   if (blocks > 4 * sms) blocks = 4 * sms;
