@@ -95,6 +95,15 @@ class GpuOptions(C.Structure):
     ]
 
 
+class ValidationOptions(C.Structure):
+    """cusna_validation_options (extension, include/libcusna.h)."""
+    _fields_ = [
+        ("struct_version", C.c_int32), ("trace_cap", C.c_int32), ("trace", _p),
+        ("ustream_steps", C.c_int32), ("ustream", _p), ("lse64", C.c_int32),
+        ("warps_per_chain", C.c_int32), ("chains_per_cta", C.c_int32),
+    ]
+
+
 def _here() -> str:
     return os.path.dirname(os.path.abspath(__file__))
 
@@ -138,10 +147,11 @@ def load_library(path: str | None = None):
     lib.cusna_behavior_stats_gpu.argtypes = [_p, i32, i32, i32, _p, _p, _p,
                                              C.c_double, C.c_double, C.c_double, _p]
     lib.cusna_behavior_stats_gpu.restype = i32
+    lib.cusna_saom_simulate_period_validate.argtypes = [P(SaomProblem), P(SaomResult),
+                                                        P(ValidationOptions)]
+    lib.cusna_saom_simulate_period_validate.restype = i32
     lib.cusna_saom_simulate_period_static.argtypes = [P(SaomProblem), P(SaomResult), _p]
     lib.cusna_saom_simulate_period_static.restype = i32
-    lib.cusna_measure_fp64_tflops.argtypes = [P(C.c_double)]
-    lib.cusna_measure_fp64_tflops.restype = i32
     lib.cusna_saom_plan_create.argtypes = [P(SaomProblem), P(SaomResult), i32, i32, P(_p)]
     lib.cusna_saom_plan_create.restype = i32
     lib.cusna_saom_plan_launch.argtypes = [_p, _p, i32]
@@ -202,8 +212,8 @@ EXPORTED_SYMBOLS = [
     "cusna_saom_simulate_period", "cusna_pack_bits", "cusna_philox4x32",
     "cusna_abi_version", "cusna_version_string", "cusna_has_cuda", "cusna_last_error",
     "cusna_saom_simulate_period_ex", "cusna_saom_simulate_batch",
-    "cusna_network_stats_gpu", "cusna_behavior_stats_gpu", "cusna_measure_fp64_tflops",
-    "cusna_saom_simulate_period_static",
+    "cusna_network_stats_gpu", "cusna_behavior_stats_gpu",
+    "cusna_saom_simulate_period_static", "cusna_saom_simulate_period_validate",
     "cusna_saom_plan_create", "cusna_saom_plan_launch", "cusna_saom_plan_set_epoch",
     "cusna_saom_plan_shape", "cusna_saom_plan_destroy",
     "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",

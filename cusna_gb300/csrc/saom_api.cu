@@ -423,7 +423,7 @@ struct ProbBufs {
   size_t x0T, x0cT, simT, simcT, kdistT, permT, keepT, forceT, keepcT, forcecT;
   size_t vmat, wtab, p1, p2, vb, ralpha, ru;
   size_t etypes, dyn, i0, i1, i2, act, z0, bkdist, inact, vmiss;
-  size_t ekind, ecfn, eoffd, eofft, pool, pool32;
+  size_t ekind, ecfn, eoffd, eofft, pool, pool32, pool32lo;
   // raw copies (host mode)
   size_t r_x0, r_sim, r_kd, r_pm, r_keep, r_force, r_theta, r_lam, r_lamb, r_thetab, r_tid,
       r_ety, r_dyn, r_i0, r_i1, r_i2, r_vmat64, r_vmat32, r_wtab64, r_wtab32, r_p164, r_p132,
@@ -466,6 +466,7 @@ void plan_problem(Planner &pl, Job &J, bool dev) {
   B.ekind = pl.take(k * 4); B.ecfn = pl.take(k * 4); B.eoffd = pl.take(k * 4);
   B.eofft = pl.take(k * 4); B.pool = pl.take(J.F.pool.size() * 8);
   B.pool32 = pl.take(J.F.pool.size() * 4);
+  B.pool32lo = pl.take(J.F.pool.size() * 4);
   if (!dev) {
     B.r_x0 = pl.take(n * W * 4);
     B.r_sim = maybe(pl, p->sim_out, n * W * 4);
@@ -651,14 +652,22 @@ cusna_status prepare(Job &J, bool dev, DevProblem &D, uint32_t chain_offset) {
   CU(cudaMemcpyAsync(at<int>(B.eofft), J.F.offt.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<double>(B.pool), J.F.pool.data(), J.F.pool.size() * 8, cudaMemcpyHostToDevice, st));
   {
-    // float32 lookup values for the float32 pass (a pageable copy is staged
-    // before cudaMemcpyAsync returns, so the local vector may go)
-    std::vector<float> p32(J.F.pool.size());
-    for (size_t x = 0; x < p32.size(); ++x) p32[x] = (float)J.F.pool[x];
+    // float32 lookup values for the float32 pass and their float32
+    // remainders, which make them double-float pairs for the score sums (a
+    // pageable copy is staged before cudaMemcpyAsync returns, so the local
+    // vectors may go)
+    std::vector<float> p32(J.F.pool.size()), p32lo(J.F.pool.size());
+    for (size_t x = 0; x < p32.size(); ++x) {
+      p32[x] = (float)J.F.pool[x];
+      p32lo[x] = (float)(J.F.pool[x] - (double)p32[x]);
+    }
     CU(cudaMemcpyAsync(at<float>(B.pool32), p32.data(), p32.size() * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(at<float>(B.pool32lo), p32lo.data(), p32lo.size() * 4,
+                       cudaMemcpyHostToDevice, st));
   }
   D.ekind = at<int>(B.ekind); D.ecfn = at<int>(B.ecfn); D.eoffd = at<int>(B.eoffd);
   D.eofft = at<int>(B.eofft); D.tab = at<double>(B.pool); D.tab32 = at<float>(B.pool32);
+  D.tab32lo = at<float>(B.pool32lo);
   auto out = [&](void *user, size_t off) -> void * {
     if (!user) return nullptr;
     return dev ? user : (off == NONE ? nullptr : at<char>(off));
@@ -726,7 +735,7 @@ cusna_status fetch_outputs(Job &J) {
 std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, int nrmax, bool tp,
                                      bool gw, bool tq, long long total_units, int force_G,
                                      int force_tpc, int nets = 1,
-                                     const JitKernel *jk = nullptr) {
+                                     const JitKernel *jk = nullptr, bool valid = false) {
   const Ctx &c = g_ctx;
   std::vector<std::pair<double, LaunchShape>> all;
   const int Gs[5] = {1, 2, 4, 8, 16};
@@ -746,12 +755,12 @@ std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, in
       for (int tpc = 1; tpc <= 16; tpc *= 2) {
         if (force_tpc && tpc != force_tpc) continue;
         const int threads = 32 * G * tpc;
-        if (threads > 512 || (G > 1 && tpc > 15)) continue;
+        if (threads > (valid ? 256 : 512) || (G > 1 && tpc > 15)) continue;
         const size_t dyn = sh.lay.bytes * nets * tpc;
         if (dyn > (size_t)c.smem_optin) continue;
         const int per_sm = jk ? jit_blocks_per_sm(*jk, threads, dyn)
                               : (nets > 1 ? multi_blocks_per_sm(threads, dyn)
-                                          : period_blocks_per_sm(threads, dyn));
+                                          : period_blocks_per_sm(threads, dyn, valid));
         if (per_sm < 1) continue;
         const double teams_sm = (double)per_sm * tpc;
         const double chains_sm = (double)total_units / c.sms;
@@ -898,7 +907,8 @@ void tuner_record(const TuneKey &key, int trial, float ms) {
 
 // Register limit check of a shape: the kernel is compiled for 512 threads with
 // the full register file, so any CTA size up to 512 fits.
-cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts) {
+cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts,
+                      const cusna_validation_options *vo = nullptr) {
   cusna_status s;
   if ((s = ensure_ctx()) != CUSNA_OK) return s;
   if (opts && opts->stream) {
@@ -922,12 +932,15 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
     tq |= (J.F.flags & F_NEED_GW30) != 0;
     total += J.p->M;
   }
-  const int fG = opts ? opts->warps_per_chain : 0, fT = opts ? opts->chains_per_cta : 0;
+  const bool valid = vo != nullptr;
+  const int fG = valid ? vo->warps_per_chain : (opts ? opts->warps_per_chain : 0);
+  const int fT = valid ? vo->chains_per_cta : (opts ? opts->chains_per_cta : 0);
   JitKernel jk;
-  const bool use_jit = jit_for(jobs, opts ? opts->specialise : 0, &jk);
-  const std::vector<LaunchShape> ranked =
+  // the validation build is the library kernel's
+  const bool use_jit = !valid && jit_for(jobs, opts ? opts->specialise : 0, &jk);
+  std::vector<LaunchShape> ranked =
       rank_shapes(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, fG, fT, 1,
-                  use_jit ? &jk : nullptr);
+                  use_jit ? &jk : nullptr, valid);
   if (ranked.empty()) {
     set_err("no launch shape fits n=%d in shared memory", nmax);
     return CUSNA_ERR_UNSUPPORTED;
@@ -936,9 +949,16 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
   // timing one of its candidates in this call)
   int trial = -1;
   const TuneKey tkey = tune_key(nmax, Wmax, kmax, kbmax, nrmax, tp, gw, tq, total, use_jit);
-  const LaunchShape sh = (fG || fT) ? ranked[0] : tuner_pick(tkey, tuning_candidates(ranked), &trial);
+  const LaunchShape sh = (fG || fT || valid) ? ranked[0]
+                                             : tuner_pick(tkey, tuning_candidates(ranked), &trial);
   Planner pl;
   for (auto &J : jobs) plan_problem(pl, J, dev);
+  // validation: the trace records and the supplied words of the (one) problem
+  const size_t trace_words = valid ? (size_t)jobs[0].p->M * vo->trace_cap * 4 : 0;
+  const size_t us_words =
+      valid ? (size_t)jobs[0].p->M * vo->ustream_steps * (4 + (size_t)jobs[0].p->n) : 0;
+  const size_t o_trace = trace_words ? pl.take(trace_words * 4) : NONE;
+  const size_t o_us = us_words ? pl.take(us_words * 4) : NONE;
   const size_t o_probs = pl.take(sizeof(DevProblem) * jobs.size());
   const size_t o_units = pl.take(sizeof(long long) * (jobs.size() + 1));
   const size_t o_counter = pl.take(sizeof(unsigned long long));
@@ -953,6 +973,21 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
   for (size_t q = 0; q < jobs.size(); ++q) {
     if ((s = prepare(jobs[q], dev, hp[q], off0)) != CUSNA_OK) return s;
     units[q + 1] = units[q] + jobs[q].p->M;
+  }
+  if (valid) {
+    DevProblem &D = hp[0];
+    if (vo->lse64) D.flags |= F_LSE64;
+    if (o_trace != NONE) {
+      // records of ministeps a chain does not reach stay -1
+      CU(cudaMemsetAsync(at<char>(o_trace), 0xFF, trace_words * 4, st));
+      D.trace = at<int>(o_trace);
+      D.trace_cap = vo->trace_cap;
+    }
+    if (o_us != NONE) {
+      CU(cudaMemcpyAsync(at<char>(o_us), vo->ustream, us_words * 4, cudaMemcpyHostToDevice, st));
+      D.ustream = at<uint32_t>(o_us);
+      D.ustream_steps = vo->ustream_steps;
+    }
   }
   CU(cudaMemcpyAsync(at<char>(o_probs), hp.data(), sizeof(DevProblem) * hp.size(),
                      cudaMemcpyHostToDevice, st));
@@ -969,11 +1004,13 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts)
     CU(launch_period(sh, at<DevProblem>(o_probs), at<long long>(o_units), (int)jobs.size(), total,
                      at<unsigned long long>(o_counter),
                      o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
-                     o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
+                     o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st, valid));
   CU(cudaEventRecord(g_ctx.ev1, st));
   if (!dev)
     for (auto &J : jobs)
       if ((s = fetch_outputs(J)) != CUSNA_OK) return s;
+  if (o_trace != NONE)
+    CU(cudaMemcpyAsync(vo->trace, at<char>(o_trace), trace_words * 4, cudaMemcpyDeviceToHost, st));
   CU(cudaStreamSynchronize(st));
   float ms = 0.f;
   CU(cudaEventElapsedTime(&ms, g_ctx.ev0, g_ctx.ev1));
@@ -1533,6 +1570,37 @@ CUSNA_API cusna_status cusna_saom_simulate_period_ex(const cusna_saom_problem *p
   g_err.clear();
   if (!problem || !result) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
   return simulate(problem, result, 1, opts);
+}
+
+CUSNA_API cusna_status cusna_saom_simulate_period_validate(const cusna_saom_problem *problem,
+                                                           cusna_saom_result *result,
+                                                           const cusna_validation_options *vo) {
+  using namespace cusna;
+  g_err.clear();
+  if (!problem || !result || !vo) { set_err("problem, result or options is NULL"); return CUSNA_ERR_NULL_ARG; }
+  if (vo->struct_version != CUSNA_ABI_VERSION) {
+    set_err("validation options struct_version %d", vo->struct_version);
+    return CUSNA_ERR_SHAPE;
+  }
+  if (vo->trace_cap < 0 || vo->ustream_steps < 0 || (vo->trace_cap > 0 && !vo->trace) ||
+      (vo->ustream_steps > 0 && !vo->ustream)) {
+    set_err("trace or ustream is NULL (or a negative count)");
+    return CUSNA_ERR_NULL_ARG;
+  }
+  if (vo->warps_per_chain < 0 || vo->warps_per_chain > 8 || vo->chains_per_cta < 0 ||
+      32 * (vo->warps_per_chain ? vo->warps_per_chain : 1) *
+              (vo->chains_per_cta ? vo->chains_per_cta : 1) > 256) {
+    set_err("the validation build runs CTAs of at most 256 threads");
+    return CUSNA_ERR_UNSUPPORTED;
+  }
+  Job J;
+  J.p = problem;
+  J.r = result;
+  cusna_status s = validate(problem, result, false, J.F);
+  if (s != CUSNA_OK) return s;
+  if ((s = ensure_ctx()) != CUSNA_OK) return s;
+  std::vector<Job> jobs(1, J);
+  return run_jobs(jobs, false, nullptr, vo);
 }
 
 CUSNA_API cusna_status cusna_saom_simulate_batch(const cusna_saom_problem *problems,

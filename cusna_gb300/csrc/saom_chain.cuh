@@ -45,6 +45,10 @@ __device__ __forceinline__ void chain_init(const Team &T, const DevProblem &P, c
     for (int x = T.tl; x < n; x += L) S.z[x] = P.z0[x];
   if (P.nrate > 0)
     for (int x = T.tl; x < n; x += L) S.crate[x] = 1.0;
+  if (T.tl == 0) {
+    S.misc[12] = -1;  // last ministep whose score sums need the float64 path
+    S.misc[13] = c;   // the chain's index within its problem (validation words)
+  }
   T.sync();
   for (int x = T.tl; x < n; x += L) {
     int od = 0, id = 0;
@@ -88,9 +92,38 @@ __device__ __forceinline__ void step_helpers(const Team &T, const DevProblem &P,
   }
 }
 
+// The four Philox words of ministep ms, counter (ms, chain, 0, 0) as the
+// reference draws them (src/libcusna_saom_cpu.cpp:167); in validation mode
+// (VALID) the caller's words for that ministep while they last.
+template <bool VALID>
+__device__ __forceinline__ void step_words(const DevProblem &P, const Slice &S, long long ms,
+                                           uint32_t chain, uint32_t out[4]) {
+  if (VALID && P.ustream && ms < P.ustream_steps) {
+    const uint32_t *u =
+        P.ustream + ((size_t)S.misc[13] * P.ustream_steps + (size_t)ms) * (4 + (size_t)P.n);
+    out[0] = u[0]; out[1] = u[1]; out[2] = u[2]; out[3] = u[3];
+    return;
+  }
+  philox10((uint32_t)ms, chain, 0u, 0u, P.k0, P.k1, out);
+}
+
+// The Gumbel word of alter j in ministep ms: first output of counter
+// (ms, chain, 1, j) (src/libcusna_saom_cpu.cpp:266), or the caller's word.
+template <bool VALID>
+__device__ __forceinline__ uint32_t alter_word(const DevProblem &P, const Slice &S, long long ms,
+                                               uint32_t chain, int j) {
+  if (VALID && P.ustream && ms < P.ustream_steps)
+    return P.ustream[((size_t)S.misc[13] * P.ustream_steps + (size_t)ms) * (4 + (size_t)P.n) + 4 +
+                     (size_t)j];
+  uint32_t ph[4];
+  philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
+  return ph[0];
+}
+
 // Behaviour ministep (src/libcusna_saom_cpu.cpp:202-227), run by the team's
-// lane 0 in the reference's order. Returns nothing; updates z, bsc, *bdist.
-static __device__ void beh_step(const DevProblem &P, const Slice &S, int i, uint32_t r3,
+// lane 0 in the reference's order. Updates z, bsc, *bdist; returns the step
+// d in {-1, 0, 1}.
+static __device__ int beh_step(const DevProblem &P, const Slice &S, int i, uint32_t r3,
                          long long *bdist) {
   const int n = P.n, W = P.W, kb = P.kb;
   const int zi = S.z[i];
@@ -143,6 +176,7 @@ static __device__ void beh_step(const DevProblem &P, const Slice &S, int i, uint
     }
     S.z[i] = zi + d;
   }
+  return d;
 }
 
 // Non-basic rate draw (src/libcusna_saom_cpu.cpp:170-193). The actor rates are
@@ -272,61 +306,167 @@ __device__ __forceinline__ bool is_nan64(double x) {
   return ((b >> 52) & 0x7FF) == 0x7FF && (b & 0xFFFFFFFFFFFFFull) != 0;
 }
 
-// Sums of one block of 32 alters (one per lane): quantity 0 is the weight w
-// of the lane's alter, quantity 1+e its weight times d_e (0 for the "no change"
-// alter and for non-permitted alters); the fixed recursive-halving warp
-// reduction leaves quantity q's block sum on the lanes reporting q, which
-// store it in rec[q].
-template <int V>
-__device__ __forceinline__ void block_lse(float *rec, float w, const float *d32, bool weighted,
-                                          int k, int lane) {
-  float v[V];
-  v[0] = w;
+// Score sums of one block of 32 alters (one per lane), as double-float pairs:
+// quantity 0 is the weight w = exp(f_j) of the lane's alter (relative to the
+// "no change" alter, whose predictor is 0), quantity 1+e is w * d_e (0 for the
+// "no change" alter and for non-permitted alters). The fixed recursive-halving
+// warp reduction leaves quantity q's block sum on the lanes reporting q, which
+// store it as the pair rec[2q], rec[2q+1]. LOMASK: bit e set when d_e may have
+// a nonzero double-float remainder (the integer counts have none).
+template <int V, unsigned LOMASK>
+__device__ __forceinline__ void block_lse(float *rec, float wh, float wl, const float *d32,
+                                          const float *d32lo, bool weighted, int k, int lane) {
+  float h[V], l[V];
+  h[0] = wh;
+  l[0] = wl;
 #pragma unroll
-  for (int q = 1; q < V; ++q) v[q] = (weighted && q - 1 < k) ? __fmul_rn(w, d32[q - 1]) : 0.f;
-  const int q = warp_multi_sum<V>(v, lane);
+  for (int q = 1; q < V; ++q) {
+    h[q] = 0.f;
+    l[q] = 0.f;
+    if (weighted && q - 1 < k) {
+      const float dh = d32[q - 1];
+      const float p = __fmul_rn(wh, dh);
+      h[q] = p;
+      if ((LOMASK >> (q - 1)) & 1u)
+        l[q] = __fadd_rn(fmaf(wh, dh, -p), fmaf(wh, d32lo[q - 1], __fmul_rn(wl, dh)));
+      else
+        l[q] = fmaf(wl, dh, fmaf(wh, dh, -p));
+    }
+  }
+  const int q = warp_multi_sum_ff<V>(h, l, lane);
   const bool writer = (V >= 32) || ((lane & ((32 / V) - 1)) == 0);
-  if (writer && q <= k) rec[q] = v[0];
+  if (writer && q <= k) {
+    rec[2 * q] = h[0];
+    rec[2 * q + 1] = l[0];
+  }
 }
 
-// The block records of one pass combined by one warp of the team: lane l takes
-// blocks l, l+32, ... in order and adds each block's sums rescaled to the
-// overall maximum (float32), then a fixed butterfly adds the lanes' partial
-// sums (warp_multi_sum). Quantity q lands in S.red[32G + q], past the warp
-// slots the team reductions use. The order of every addition depends on the
-// block index only, so the result is the same for every team size.
+// The block records of one pass combined by one warp of the team: lane l adds
+// blocks l, l+32, ... in order (double-float), then a fixed butterfly adds the
+// lanes' partial sums. Quantity q lands in S.red[32G + q] as a double, past
+// the warp slots the team reductions use. The order of every addition depends
+// on the block index only, so the result is the same for every team size.
 template <int V>
 __device__ __forceinline__ void combine_blocks(const Team &T, const Slice &S, int n, int k) {
   const int nb = (n + 31) >> 5;
-  float M = -INFINITY;
-  for (int b = T.lane; b < nb; b += 32) M = fmaxf(M, S.blk[(size_t)b * (k + 2)]);
-  M = warp_max_f(M);
-  float v[V];
+  float h[V], l[V];
 #pragma unroll
-  for (int q = 0; q < V; ++q) v[q] = 0.f;
+  for (int q = 0; q < V; ++q) {
+    h[q] = 0.f;
+    l[q] = 0.f;
+  }
   for (int b = T.lane; b < nb; b += 32) {
-    const float *rec = S.blk + (size_t)b * (k + 2);
-    const float r = rec[0] == M ? 1.f : expf(__fsub_rn(rec[0], M));
+    const float *rec = S.blk + (size_t)b * 2 * (k + 1);
 #pragma unroll
     for (int q = 0; q < V; ++q)
-      if (q <= k) v[q] = __fadd_rn(v[q], __fmul_rn(rec[1 + q], r));
+      if (q <= k) ff_add(h[q], l[q], rec[2 * q], rec[2 * q + 1]);
   }
-  const int q = warp_multi_sum<V>(v, T.lane);
+  const int q = warp_multi_sum_ff<V>(h, l, T.lane);
   const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
-  if (writer && q <= k) S.red[32 * T.G + q] = (double)v[0];
+  if (writer && q <= k) S.red[32 * T.G + q] = __dadd_rn((double)h[0], (double)l[0]);
 }
 
+// The float64 predictor f_j of alter j (and its change statistics in d): the
+// reference's value bit for bit (effect order, separately rounded products
+// and sums).
+template <bool MULTI>
+__device__ __forceinline__ double f64_of(const DevProblem &P, const Slice &S, const StepCtx &X,
+                                         int j, double *d, int net) {
+  const int n = P.n, i = X.i;
+  const int aij = bit_of(S.rowsT, n, i, j), aji = bit_of(S.colsT, n, i, j);
+  (void)net;
+#if defined(CUSNA_JIT_SPEC)
+  return jit_change_stats<true>(P, S, X, j, aij, aji, d);
+#elif defined(CUSNA_JIT_MULTI)
+  return jit_change_stats<true>(net, P, S, X, j, aij, aji, d);
+#else
+  return change_stats<true, MULTI>(P, S, X, j, aij, aji, d);
+#endif
+}
+
+// The score sums in float64 as the reference forms them
+// (src/libcusna_saom_cpu.cpp:271-274): lmax = the largest predictor of a
+// permitted alter (at least the "no change" alter's 0), then sume = sum of
+// exp(f_j - lmax) and wsum_e = sum of exp(f_j - lmax) d_je over permitted
+// alters, every f_j and d_je the reference's float64 value. The sums run per
+// 32-alter block (fixed warp reduction) and over blocks in order, so they do
+// not depend on the team size; results land in S.red[32G + q]. Used when a
+// predictor leaves the double-float exponential's range or is not finite,
+// and at every ministep under F_LSE64. Called by the whole team.
+template <bool MULTI, int V>
+static __device__ __noinline__ void lse_float64(const Team &T, const DevProblem &P,
+                                                const Slice &S, const StepCtx &X, double *d,
+                                                int net) {
+  const int n = P.n, k = P.k, L = T.L, i = X.i;
+  long long mk = dkey(0.0);
+  for (int j = T.tl; j < n; j += L) {
+    if (j == i || !((S.okbits[j >> 5] >> (j & 31)) & 1u)) continue;
+    const double f = f64_of<MULTI>(P, S, X, j, d, net);
+    if (!is_nan64(f)) {
+      const long long kf = dkey(f);
+      mk = kf > mk ? kf : mk;
+    }
+  }
+  const double lmax = dunkey(team_max_ll(T, mk, S.red));
+  double *rec64 = (double *)S.blk;
+  for (int jb = 32 * T.warp; jb < n; jb += L) {
+    const int j = jb + T.lane;
+    double w = 0.0;
+    bool weighted = false;
+    if (j < n && ((S.okbits[j >> 5] >> (j & 31)) & 1u)) {
+      if (j == i) {
+        w = exp(-lmax);
+      } else {
+        w = exp(__dsub_rn(f64_of<MULTI>(P, S, X, j, d, net), lmax));
+        weighted = true;
+      }
+    }
+    double v[V];
+    v[0] = w;
+#pragma unroll
+    for (int q = 1; q < V; ++q) v[q] = (weighted && q - 1 < k) ? __dmul_rn(w, d[q - 1]) : 0.0;
+    const int q = warp_multi_sum<V>(v, T.lane);
+    const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
+    if (writer && q <= k) rec64[(size_t)(jb >> 5) * (k + 1) + q] = v[0];
+  }
+  T.sync();
+  if (T.warp == 0) {
+    const int nb = (n + 31) >> 5;
+    double v[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) v[q] = 0.0;
+    for (int b = T.lane; b < nb; b += 32)
+#pragma unroll
+      for (int q = 0; q < V; ++q)
+        if (q <= k) v[q] = __dadd_rn(v[q], rec64[(size_t)b * (k + 1) + q]);
+    const int q = warp_multi_sum<V>(v, T.lane);
+    const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
+    if (writer && q <= k) S.red[32 * T.G + q] = v[0];
+  }
+}
+
+// Compile-time width of the score sums (k + 1 quantities, a power of two) and
+// the mask of effects whose change statistic can have a double-float remainder.
+#if defined(CUSNA_JIT_SPEC)
+#define CUSNA_LSE_V (CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))
+#define CUSNA_LSE_LOMASK CUSNA_JIT_LOMASK
+#else
+#define CUSNA_LSE_LOMASK 0xFFFFFFFFu
+#endif
+
 // One network ministep of focal actor i on the network of slice S, up to the
-// choice: change statistics, float32 keys and log-sum-exp, the certified or
-// exact float64 choice, and the chosen alter's float64 change statistics in
-// S.dstar. Returns j*. The log-sum-exp sums are left in S.red[32G + q] for the
-// score update. d (float64) and d32 are per-thread scratch of k values.
+// choice: change statistics, float32 keys and the double-float score sums, the
+// certified or exact float64 choice, and the chosen alter's float64 change
+// statistics in S.dstar. Returns j*. The score sums are left in S.red[32G + q]
+// (float64) for the score update. d (float64), d32 and d32lo are per-thread
+// scratch of k values.
 // MULTI: the network is one of a multi-network problem's, whose network w has
 // its rows at rows0 + w*net_stride words (cross effects read them).
-template <bool MULTI>
+// VALID: validation mode (caller-supplied words in place of Philox).
+template <bool MULTI, bool VALID = false>
 __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, const Slice &S,
                                           int i, long long ms, uint32_t chain, double *d,
-                                          float *d32, const uint32_t *rows0 = nullptr,
+                                          float *d32, float *d32lo, const uint32_t *rows0 = nullptr,
                                           size_t net_stride = 0, int net = 0) {
   const int n = P.n, W = P.W, k = P.k, L = T.L;
   (void)net;
@@ -355,18 +495,23 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   // of the float64 key f_j - log(-log u_j): (k + 8) u absf_j for f32_j, 4e-6
   // for loglog_est and u (absf_j + 23) for the subtraction (|f32_j| <= absf_j,
   // |log(-log u)| < 23). gbuf[j] keeps the upper bound g_j + E_j.
-  // The log-sum-exp sums are formed per block of 32 alters (alter j on lane
-  // j mod 32, whatever the team size): the block maximum and the block's
-  // sums of exp(f - max) and exp(f - max) d_e with a fixed warp reduction,
-  // stored per block and combined after the choice in an order fixed by the
-  // block index (combine_blocks), so the scores do not depend on the launch
-  // shape.
+  // The score sums are formed per block of 32 alters (alter j on lane j mod
+  // 32, whatever the team size) in double-float arithmetic: the predictor as
+  // the pair f32_j + flo_j (within ~2^-47 absf_j of the reference's float64
+  // f_j), its exponential relative to the "no change" alter (exp_ff, relative
+  // error ~2e-14), and the weighted change statistics; the blocks are
+  // combined after the choice in an order fixed by the block index
+  // (combine_blocks), so the scores do not depend on the launch shape. A
+  // predictor outside [-60, 60] (or not finite) sends the ministep's sums to
+  // the float64 path (lse_float64), as does F_LSE64.
   KeyTop best{-INFINITY, 0.f, -INFINITY, 0x7FFFFFFF};
   const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
+  const bool fast_sums = (P.flags & F_LSE64) == 0;
+  bool wide = false;
   for (int jb = 32 * T.warp; jb < n; jb += L) {
     const int j = jb + T.lane;
     bool ok = false, stay = false;
-    float f = 0.f;
+    float f = 0.f, flo = 0.f;
     if (j < n) {
       const int aij = bit_of(S.rowsT, n, i, j);
       float ub = -INFINITY;
@@ -376,16 +521,18 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
         float absf = 0.f;
 #if defined(CUSNA_JIT_SPEC)
         // the effect plan compiled in (saom_jit.cu): the same float32 values
-        if (!stay) f = jit_change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+        if (!stay)
+          f = jit_change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo, &absf, &flo);
 #elif defined(CUSNA_JIT_MULTI)
         if (!stay)
-          f = jit_change_stats32(net, P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+          f = jit_change_stats32(net, P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo, &absf,
+                                 &flo);
 #else
-        if (!stay) f = change_stats32<MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, &absf);
+        if (!stay)
+          f = change_stats32<MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo, &absf,
+                                    &flo);
 #endif
-        uint32_t ph[4];
-        philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-        const float g = __fsub_rn(f, loglog_est(ph[0]));
+        const float g = __fsub_rn(f, loglog_est(alter_word<VALID>(P, S, ms, chain, j)));
         const float E = __fadd_rn(__fmul_rn(ecoef, absf), 6e-6f);
         ub = __fadd_rn(g, E);
         keytop_add(best, g, E, j);
@@ -394,21 +541,25 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     }
     const uint32_t okb = __ballot_sync(kFull, ok);
     if (T.lane == 0) S.okbits[jb >> 5] = okb;
-    // a NaN predictor turns the sums into NaN, as exp(NaN - lmax) does in
-    // the reference, and never wins the choice (its key compares false)
-    const float mb = warp_max_f(ok ? f : -INFINITY);
-    const float w = ok ? expf(__fsub_rn(f, mb)) : 0.f;
-    float *rec = S.blk + (size_t)(jb >> 5) * (k + 2);
-    if (T.lane == 0) rec[0] = mb;
-#ifdef CUSNA_JIT_SPEC
-    block_lse<(CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))>(
-        rec + 1, w, d32, ok && !stay, CUSNA_JIT_K, T.lane);
+    if (fast_sums) {
+      float wh = 0.f, wl = 0.f;
+      if (ok) {
+        if (stay) wh = 1.f;
+        else if (fabsf(f) <= kFFExpMax) exp_ff(f, flo, S.etab, wh, wl);
+        else wide = true;  // also NaN
+      }
+      float *rec = S.blk + (size_t)(jb >> 5) * 2 * (k + 1);
+#ifdef CUSNA_LSE_V
+      block_lse<CUSNA_LSE_V, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, CUSNA_JIT_K,
+                                               T.lane);
 #else
-    if (k + 1 <= 8) block_lse<8>(rec + 1, w, d32, ok && !stay, k, T.lane);
-    else if (k + 1 <= 16) block_lse<16>(rec + 1, w, d32, ok && !stay, k, T.lane);
-    else block_lse<32>(rec + 1, w, d32, ok && !stay, k, T.lane);
+      if (k + 1 <= 8) block_lse<8, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, k, T.lane);
+      else if (k + 1 <= 16) block_lse<16, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, k, T.lane);
+      else block_lse<32, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, k, T.lane);
 #endif
+    }
   }
+  if (__any_sync(kFull, wide) && T.lane == 0) S.misc[12] = (int)ms;
   T.sync();
   const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
 
@@ -429,20 +580,8 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     for (int j = T.tl; j < n; j += L) {
       const bool okj = (S.okbits[j >> 5] >> (j & 31)) & 1u;
       if (okj && !(S.gbuf[j] < lb)) {
-        double f = 0.0;
-        if (j != i) {
-          const int aij = bit_of(S.rowsT, n, i, j);
-#if defined(CUSNA_JIT_SPEC)
-          f = jit_change_stats<true>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
-#elif defined(CUSNA_JIT_MULTI)
-          f = jit_change_stats<true>(net, P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
-#else
-          f = change_stats<true, MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d);
-#endif
-        }
-        uint32_t ph[4];
-        philox10((uint32_t)ms, chain, 1u, (uint32_t)j, P.k0, P.k1, ph);
-        const double g = __dsub_rn(f, log(-log(unif01(ph[0]))));
+        const double f = j != i ? f64_of<MULTI>(P, S, X, j, d, net) : 0.0;
+        const double g = __dsub_rn(f, log(-log(unif01(alter_word<VALID>(P, S, ms, chain, j)))));
         if (is_nan64(g)) continue;
         const long long kg = dkey(g);
         if (kg > bk || (kg == bk && j < bj)) { bk = kg; bj = j; }
@@ -453,24 +592,33 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   // never an index outside the network, whatever the inputs
   if ((unsigned)jstar >= (unsigned)n) jstar = i;
 
-  // the block records combined into quantity q (0: sum of weights, 1+e:
-  // weighted sum of d_e) rescaled to the overall maximum, in S.red[32G + q];
-  // with several warps, by a warp other than the chosen alter's owner, which
-  // meanwhile forms the chosen alter's float64 statistics
-  const int owner_warp = (jstar % L) >> 5;
-  if (T.warp == (T.G > 1 ? (owner_warp + 1) % T.G : 0)) {
-#ifdef CUSNA_JIT_SPEC
-    combine_blocks<(CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))>(T, S, n,
-                                                                                  CUSNA_JIT_K);
+  // the score sums: normally the block records combined into quantity q (0:
+  // sum of weights, 1+e: weighted sum of d_e), by a warp other than the
+  // chosen alter's owner, which meanwhile forms the chosen alter's float64
+  // statistics; on the float64 path, the whole team
+  const bool sums64 = !fast_sums || S.misc[12] == (int)ms;
+  if (sums64) {
+#ifdef CUSNA_LSE_V
+    lse_float64<MULTI, CUSNA_LSE_V>(T, P, S, X, d, net);
 #else
-    if (k + 1 <= 8) combine_blocks<8>(T, S, n, k);
-    else if (k + 1 <= 16) combine_blocks<16>(T, S, n, k);
-    else combine_blocks<32>(T, S, n, k);
+    if (k + 1 <= 8) lse_float64<MULTI, 8>(T, P, S, X, d, net);
+    else if (k + 1 <= 16) lse_float64<MULTI, 16>(T, P, S, X, d, net);
+    else lse_float64<MULTI, 32>(T, P, S, X, d, net);
 #endif
+  } else {
+    const int owner_warp = (jstar % L) >> 5;
+    if (T.warp == (T.G > 1 ? (owner_warp + 1) % T.G : 0)) {
+#ifdef CUSNA_LSE_V
+      combine_blocks<CUSNA_LSE_V>(T, S, n, CUSNA_JIT_K);
+#else
+      if (k + 1 <= 8) combine_blocks<8>(T, S, n, k);
+      else if (k + 1 <= 16) combine_blocks<16>(T, S, n, k);
+      else combine_blocks<32>(T, S, n, k);
+#endif
+    }
   }
 
-  // ---- score update (lane e updates effect e) and toggle ----------------
-  // the chosen alter's change statistics in float64, as the reference adds them
+  // ---- the chosen alter's change statistics, in float64 as the reference adds them
   if (T.tl == jstar % L) {
     if (jstar == i) {
       for (int e = 0; e < k; ++e) S.dstar[e] = 0.0;
@@ -490,7 +638,22 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   return jstar;
 }
 
+// Validation trace record of ministep ms (validation mode only): (step,
+// focal actor, choice, change of the distance); the choice is the chosen alter
+// of a network ministep, or -(d + 2) for a behaviour step d.
+template <bool VALID>
+__device__ __forceinline__ void trace_put(const DevProblem &P, int c, long long ms, int actor,
+                                          int choice, long long delta) {
+  if (!VALID || !P.trace || ms >= P.trace_cap) return;
+  int *t = P.trace + ((size_t)c * P.trace_cap + (size_t)ms) * 4;
+  t[0] = (int)ms;
+  t[1] = actor;
+  t[2] = choice;
+  t[3] = (int)delta;
+}
+
 // One chain: the ministep loop and the chain's outputs.
+template <bool VALID>
 static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice &S, int c) {
   const int n = P.n, k = P.k;
   const uint32_t chain = P.chain_offset + (uint32_t)c;
@@ -504,7 +667,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
   long long dist = 0, bdist = 0, ms = 0, msb = 0;
   double t = 0.0, rho = 0.0;
   double d[kMaxEff];
-  float d32[kMaxEff];
+  float d32[kMaxEff], d32lo[kMaxEff];
 
   for (;;) {
     int i;
@@ -512,7 +675,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
     uint32_t r3;
     if (P.nrate > 0) {
       uint32_t rr[4];
-      philox10((uint32_t)ms, chain, 0u, 0u, P.k0, P.k1, rr);
+      step_words<VALID>(P, S, ms, chain, rr);
       i = rate_draw(T, P, S, rr, lam, t, rho);
       if (i < 0) break;
       is_net = true;
@@ -525,7 +688,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
       if (slot == 0) {
         if (T.warp == 0) {
           uint32_t rr[4];
-          philox10((uint32_t)(ms + T.lane), chain, 0u, 0u, P.k0, P.k1, rr);
+          step_words<VALID>(P, S, ms + T.lane, chain, rr);
           S.rtau[T.lane] = __ddiv_rn(-log(unif01(rr[0])), den);
           S.rnet[T.lane] = (P.kb == 0 || unif01(rr[1]) < pnet) ? 1 : 0;
           long long idx = (long long)__dmul_rn(unif01(rr[2]), (double)P.nact);
@@ -543,7 +706,11 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
     }
 
     if (!is_net) {
-      if (T.tl == 0) beh_step(P, S, i, r3, &bdist);
+      if (T.tl == 0) {
+        const long long bd0 = bdist;
+        const int dz = beh_step(P, S, i, r3, &bdist);
+        trace_put<VALID>(P, c, ms, i, -(dz + 2), bdist - bd0);
+      }
       T.sync();
       ++msb;
       ++ms;
@@ -552,7 +719,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
       continue;
     }
 
-    const int jstar = net_choice<false>(T, P, S, i, ms, chain, d, d32);
+    const int jstar = net_choice<false, VALID>(T, P, S, i, ms, chain, d, d32, d32lo);
     const int aij_star = bit_of(S.rowsT, n, i, jstar);
     T.sync();
     if (T.tl < k) {
@@ -560,6 +727,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
       const double s0 = S.red[32 * T.G], se = S.red[32 * T.G + 1 + e];
       S.sc[e] = __dadd_rn(S.sc[e], __dsub_rn(S.dstar[e], __ddiv_rn(se, s0)));
     }
+    const long long dist0 = dist;
     ++ms;
     if (jstar != i) {
       const int j = jstar;
@@ -580,6 +748,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
         }
       }
     }
+    if (T.tl == 0) trace_put<VALID>(P, c, ms - 1, i, jstar, dist - dist0);
     if (P.nrate > 0 && T.tl == 0) {
       for (int q = 0; q < P.nrate; ++q) {
         const int rk = S.rkind[q];

@@ -41,6 +41,7 @@ enum : int {
   F_THETA_TAB = 1 << 13,   // term tables hold theta_e * d for every chain
   F_HAS_STEP = 1 << 14,    // some effect is constant within a ministep
   F_HAS_Z = 1 << 15,       // behaviour values are read (behaviour or dynamic covariates)
+  F_LSE64 = 1 << 16,       // score log-sum-exp in float64 at every ministep (validation)
 };
 
 // How the change statistic d_e of toggling i -> j is formed (DevProblem::ekind).
@@ -113,7 +114,8 @@ struct DevProblem {
   // effect plan (k each) and its table pool
   const int *ekind, *ecfn, *eoffd, *eofft;
   const double *tab;
-  const float *tab32;  // float32 copy of tab's lookup values (the float32 pass)
+  const float *tab32;    // float32 rounding of tab's lookup values (the float32 pass)
+  const float *tab32lo;  // tab - tab32, rounded to float32: tab32 + tab32lo is tab to ~2^-48
 
   // outputs (chain-major), any may be null
   double *stats, *ntim;
@@ -125,6 +127,15 @@ struct DevProblem {
   float *rscores;
   int *actor_dist;
   uint8_t *a_ends;
+
+  // validation mode (period_kernel<MAXT, true> only): per-ministep trace
+  // records (step, actor, choice, distance change), trace_cap per chain, and
+  // caller-supplied words replacing the Philox outputs of the first
+  // ustream_steps ministeps of each chain (4 + n words per ministep)
+  int *trace;
+  int trace_cap;
+  const uint32_t *ustream;
+  int ustream_steps;
 };
 
 // ---- Philox4x32-10 (the generator of src/libcusna_saom_cpu.cpp:32-45) ----
@@ -181,5 +192,97 @@ __device__ __forceinline__ float loglog_est(uint32_t x) {
   return logf(L);
 }
 
+// ---- double-float arithmetic ------------------------------------------------
+// An unevaluated pair (h, l) of float32 values stands for h + l, with |l| at
+// most about 2^-24 |h|: 48 significant bits on the float32 pipes, which on
+// this GPU run 64 times as many operations per cycle as the float64 pipe.
+// The error-free transformations are Knuth's TwoSum and Dekker's product
+// through a fused multiply-add (T. J. Dekker, "A floating-point technique for
+// extending the available precision", Numer. Math. 18, 1971). Every sum uses
+// the _rn intrinsics, so no compiler contraction or reassociation can change
+// the result.
+
+// s + e = a + b exactly, s = fl(a + b).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (ah, al) += (bh, bl), keeping the pair unnormalised: the rounding error of
+// the high sum joins the low parts, whose own rounding is ~2^-24 of them.
+__device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl) {
+  float s, e;
+  two_sum(ah, bh, s, e);
+  ah = s;
+  al = __fadd_rn(__fadd_rn(al, bl), e);
+}
+
+// Largest |x| the double-float exponential accepts; the score sums fall back
+// to float64 when a predictor leaves this range (or is not finite).
+constexpr float kFFExpMax = 60.f;
+
+// ln(2)/64 split as C1 + C2 + C3: C1 has 11 significant bits, so N*C1 is exact
+// for |N| < 2^13 (|x| <= 60 gives |N| <= 5540); C2 and C3 are the next two
+// float32 roundings of the remainder (the split leaves 1.8e-22).
+constexpr float kLn2o64C1 = 0x1.63p-7f;
+constexpr float kLn2o64C2 = -0x1.bd0106p-19f;
+constexpr float kLn2o64C3 = 0x1.cf79acp-46f;
+constexpr float k64oLn2 = 0x1.715476p+6f;   // 64/ln(2), only to choose N
+
+// The table 2^(j/64), j = 0..63, as double-float pairs (h, l): computed from
+// the float64 exp2, whose error is far below the pair's 2^-48.
+__device__ __forceinline__ void fill_exp_table(float2 *tab, int tl, int L) {
+  for (int j = tl; j < 64; j += L) {
+    const double v = exp2((double)j * 0.015625);
+    const float h = (float)v;
+    tab[j] = make_float2(h, (float)__dsub_rn(v, (double)h));
+  }
+}
+
+// exp(xh + xl) as a double-float pair (wh, wl) for |xh| <= kFFExpMax, relative
+// error below about 2e-14. Tang's table-driven method (P. T. P. Tang, "Table-
+// driven implementation of the exponential function in IEEE floating-point
+// arithmetic", ACM TOMS 15(2), 1989) in double-float arithmetic:
+//   x = N ln2/64 + r, |r| <= ln2/128 (Cody-Waite reduction with the three-part
+//   constant above, the first product exact, the second through Dekker's
+//   product, so r is known to ~1e-18);
+//   exp(r) - 1 = r + r^2/2 + r^3/6 + r^4/24 + r^5/120 (the omitted terms are
+//   below 4e-17): the first two terms in double-float, the rest in float32
+//   (their sum is below 2.7e-8, so its rounding is below 2e-15);
+//   exp(x) = 2^(N>>6) * 2^((N&63)/64) * exp(r), the table entry multiplied in
+//   double-float and the power of two applied exactly to both halves.
+__device__ __forceinline__ void exp_ff(float xh, float xl, const float2 *tab, float &wh,
+                                       float &wl) {
+  const float Nf = rintf(__fmul_rn(xh, k64oLn2));
+  const int N = (int)Nf;
+  const float t1 = fmaf(-Nf, kLn2o64C1, xh);  // exact
+  const float p = __fmul_rn(Nf, kLn2o64C2);
+  const float pe = fmaf(Nf, kLn2o64C2, -p);  // p + pe = N C2 exactly
+  float rh, e;
+  two_sum(t1, -p, rh, e);
+  const float rl = __fadd_rn(__fsub_rn(__fsub_rn(e, pe), __fmul_rn(Nf, kLn2o64C3)), xl);
+  // r^2 = sqh + sql (dropping rl^2 < 1e-19)
+  const float sqh = __fmul_rn(rh, rh);
+  const float sql = fmaf(__fmul_rn(2.f, rh), rl, fmaf(rh, rh, -sqh));
+  // r^3/6 + r^4/24 + r^5/120, plus the r^2 rl / 2 part of the cubic term
+  const float q = fmaf(__fmul_rn(sqh, rh),
+                       fmaf(rh, fmaf(rh, 8.3333333333e-3f, 4.1666666667e-2f), 1.6666666667e-1f),
+                       __fmul_rn(__fmul_rn(0.5f, sqh), rl));
+  float sh, e1;
+  two_sum(rh, __fmul_rn(0.5f, sqh), sh, e1);
+  const float sl = __fadd_rn(__fadd_rn(__fadd_rn(rl, __fmul_rn(0.5f, sql)), q), e1);
+  // T (1 + sh + sl), T = 2^((N & 63)/64) in [1, 2) as (T.x, T.y)
+  const float2 T = tab[N & 63];
+  const float ph = __fmul_rn(T.x, sh);
+  const float pl = fmaf(T.x, sh, -ph);
+  const float h = __fadd_rn(T.x, ph);  // |T.x| >= 1 > |ph|: Fast2Sum
+  float l = __fsub_rn(ph, __fsub_rn(h, T.x));
+  l = __fadd_rn(l, __fadd_rn(pl, fmaf(T.x, sl, fmaf(T.y, sh, T.y))));
+  // 2^(N >> 6), N >> 6 in [-87, 86]: a normal float32
+  const float s = __int_as_float(((N >> 6) + 127) << 23);
+  wh = __fmul_rn(h, s);
+  wl = __fmul_rn(l, s);
+}
 
 }  // namespace cusna

@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -106,54 +107,79 @@ void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi)
   const int k = (int)J.kind.size();
   const int fl = J.pc_flags;
   const char *x = sfx.c_str();
-  // float32 pass (change_stats32)
+  // float32 pass (change_stats32), with the double-float remainders of the
+  // change statistics and of the predictor for the score sums
   g.put("__device__ __forceinline__ float jit_change_stats32%s(const DevProblem &P, const Slice &S,\n"
-        "    const StepCtx &X, int j, int aij, int aji, float *d32, float *absf) {\n", x);
+        "    const StepCtx &X, int j, int aij, int aji, float *d32, float *d32lo, float *absf,\n"
+        "    float *flo) {\n", x);
   g.s += "  const int i = X.i;\n";
   gen_shape(g, J);
-  g.s += "  (void)n; (void)W; (void)i; (void)aji;\n";
+  g.s += "  (void)n; (void)W; (void)i; (void)aji; (void)d32lo;\n";
   gen_pair_counts(g, fl);
   g.s += "  const uint32_t sg = aij ? 0x80000000u : 0u;\n"
-         "  float f = 0.f, a = 0.f;\n";
+         "  float f = 0.f, a = 0.f, fo = 0.f;\n";
   for (int e = 0; e < k; ++e) {
     const int kind = J.kind[e], cfn = J.cfn[e], t = J.tid[e];
     g.put("  {  // effect %d: type %d, kind %d, function %d\n", e, t, kind, cfn);
-    g.s += "    float v, term = 0.f;\n    bool has_term = true;\n";
+    g.put("    const float th = S.th32[%d];\n", e);
+    g.s += "    float v, vlo = 0.f, term = 0.f, tlo = 0.f;\n    bool has_term = true;\n"
+           "    (void)th; (void)vlo;\n";
     if (kind == K_CNT) {
       gen_count(g, cfn);
-      g.put("    v = __uint_as_float(__float_as_uint((float)c) ^ sg);\n"
-            "    term = __fmul_rn(S.th32[%d], v);\n", e);
+      g.s += "    v = __uint_as_float(__float_as_uint((float)c) ^ sg);\n"
+             "    term = __fmul_rn(th, v);\n";
+      // c in {0, 1} (density, reciprocity): theta * v is exact
+      if (cfn != 0 && cfn != 1) g.s += "    tlo = fmaf(th, v, -term);\n";
     } else if (kind == K_LOOK) {
       gen_index(g, cfn);
       g.put("    v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[%d] + idx]) ^ sg);\n"
-            "    term = __fmul_rn(S.th32[%d], v);\n", e, e);
+            "    vlo = __uint_as_float(__float_as_uint(P.tab32lo[S.eoffd[%d] + idx]) ^ sg);\n"
+            "    term = __fmul_rn(th, v);\n"
+            "    tlo = fmaf(th, vlo, fmaf(th, v, -term));\n", e, e);
     } else if (kind == K_STEP) {
       g.put("    const int q = 2 * aij + aji;\n"
-            "    v = S.stepd32[%d + q];\n    term = S.stept32[%d + q];\n", 4 * e, 4 * e);
+            "    v = S.stepd32[%d + q];\n    vlo = S.stepdlo32[%d + q];\n"
+            "    term = S.stept32[%d + q];\n    tlo = S.steptlo32[%d + q];\n",
+            4 * e, 4 * e, 4 * e, 4 * e);
     } else if (kind == K_ZERO) {
       g.s += "    v = 0.f;\n    has_term = false;\n";
     } else if (multi && kind == K_CROSS) {
       g.put("    const int c = cross_count(S, X, n, W, %d, S.eoffd[%d], i, j);\n"
-            "    const float m = (%d == 36 && S.p1[%d] >= 2.0) ? sqrtf((float)c) : (float)c;\n"
+            "    const bool rt = %d == 36 && S.p1[%d] >= 2.0;\n"
+            "    const float m = rt ? sqrtf((float)c) : (float)c;\n"
+            "    const float mlo = (rt && c > 0) ? __fdiv_rn(fmaf(-m, m, (float)c), __fmul_rn(2.f, m)) : 0.f;\n"
             "    v = __uint_as_float(__float_as_uint(m) ^ sg);\n"
-            "    term = __fmul_rn(S.th32[%d], v);\n", cfn, e, cfn, e, e);
+            "    vlo = __uint_as_float(__float_as_uint(mlo) ^ sg);\n"
+            "    term = __fmul_rn(th, v);\n"
+            "    tlo = fmaf(th, vlo, fmaf(th, v, -term));\n", cfn, e, cfn, e);
     } else if (t == 32) {
-      const int c2 = J.i2[e];
-      g.put("    v = __fmul_rn(d32[%d], d32[%d]);\n", J.i0[e], J.i1[e]);
-      if (c2 >= 0) g.put("    v = __fmul_rn(v, d32[%d]);\n", c2);
-      else g.s += "    if (aij) v = -v;\n";
-      g.put("    term = __fmul_rn(S.th32[%d], v);\n", e);
+      const int c0 = J.i0[e], c1 = J.i1[e], c2 = J.i2[e];
+      g.put("    v = __fmul_rn(d32[%d], d32[%d]);\n"
+            "    vlo = __fadd_rn(fmaf(d32[%d], d32[%d], -v),\n"
+            "                    fmaf(d32[%d], d32lo[%d], __fmul_rn(d32lo[%d], d32[%d])));\n",
+            c0, c1, c0, c1, c0, c1, c0, c1);
+      if (c2 >= 0)
+        g.put("    {\n      const float v2 = __fmul_rn(v, d32[%d]);\n"
+              "      vlo = __fadd_rn(fmaf(v, d32[%d], -v2), fmaf(v, d32lo[%d], __fmul_rn(vlo, d32[%d])));\n"
+              "      v = v2;\n    }\n", c2, c2, c2, c2);
+      else g.s += "    if (aij) { v = -v; vlo = -vlo; }\n";
+      g.s += "    term = __fmul_rn(th, v);\n"
+             "    tlo = fmaf(th, vlo, fmaf(th, v, -term));\n";
     } else {
-      g.put("    v = (float)gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj,\n"
-            "                        nullptr);\n    term = __fmul_rn(S.th32[%d], v);\n", e, e);
+      g.put("    {\n      const double v64 = gen_stat(P, S, X, %d, j, aij, aji, ri_cj, ri_rj, rj_ci,\n"
+            "                                  ci_cj, ci_rj, nullptr);\n"
+            "      v = (float)v64;\n      vlo = (float)__dsub_rn(v64, (double)v);\n    }\n"
+            "    term = __fmul_rn(th, v);\n"
+            "    tlo = fmaf(th, vlo, fmaf(th, v, -term));\n", e);
     }
-    if (J.ety[e] == 1) g.s += "    if (aij) { v = 0.f; has_term = false; }\n";
-    else if (J.ety[e] == 2) g.s += "    if (!aij) { v = 0.f; has_term = false; }\n";
-    g.put("    d32[%d] = v;\n", e);
-    g.s += "    if (has_term) {\n      f = __fadd_rn(f, term);\n      a = __fadd_rn(a, fabsf(term));\n"
-           "    }\n  }\n";
+    if (J.ety[e] == 1) g.s += "    if (aij) { v = 0.f; vlo = 0.f; has_term = false; }\n";
+    else if (J.ety[e] == 2) g.s += "    if (!aij) { v = 0.f; vlo = 0.f; has_term = false; }\n";
+    g.put("    d32[%d] = v;\n    d32lo[%d] = vlo;\n", e, e);
+    g.s += "    if (has_term) {\n      float err;\n      two_sum(f, term, f, err);\n"
+           "      fo = __fadd_rn(fo, __fadd_rn(err, tlo));\n"
+           "      a = __fadd_rn(a, fabsf(term));\n    }\n  }\n";
   }
-  g.s += "  *absf = a;\n  return f;\n}\n";
+  g.s += "  *absf = a;\n  *flo = fo;\n  return f;\n}\n";
   // float64 evaluation (change_stats): the chosen alter and uncertified choices
   g.put("template <bool TERMS>\n"
         "__device__ __forceinline__ double jit_change_stats%s(const DevProblem &P, const Slice &S,\n"
@@ -202,9 +228,19 @@ void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi)
 
 }  // namespace
 
+// Effects whose change statistic can have a double-float remainder: every
+// kind but the integer counts (and the zero dyadic covariate).
+unsigned lo_mask(const JitPlan &J) {
+  unsigned m = 0;
+  for (size_t e = 0; e < J.kind.size(); ++e)
+    if (J.kind[e] != K_CNT && J.kind[e] != K_ZERO) m |= 1u << e;
+  return m;
+}
+
 std::string jit_spec_source(const JitPlan &J) {
   Gen g;
-  g.put("#define CUSNA_JIT_SPEC 1\n#define CUSNA_JIT_K %d\nnamespace cusna {\n", (int)J.kind.size());
+  g.put("#define CUSNA_JIT_SPEC 1\n#define CUSNA_JIT_K %d\n#define CUSNA_JIT_LOMASK 0x%xu\n"
+        "namespace cusna {\n", (int)J.kind.size(), lo_mask(J));
   gen_functions(g, J, "", false);
   g.s += "}  // namespace cusna\n";
   return g.s;
@@ -217,11 +253,13 @@ std::string jit_multi_spec_source(const std::vector<JitPlan> &nets) {
   for (int d = 0; d < D; ++d) gen_functions(g, nets[d], "_n" + std::to_string(d), true);
   // the chosen network's plan (warp-uniform per ministep)
   g.s += "__device__ __forceinline__ float jit_change_stats32(int net, const DevProblem &P,\n"
-         "    const Slice &S, const StepCtx &X, int j, int aij, int aji, float *d32, float *absf) {\n"
+         "    const Slice &S, const StepCtx &X, int j, int aij, int aji, float *d32, float *d32lo,\n"
+         "    float *absf, float *flo) {\n"
          "  switch (net) {\n";
   for (int d = 0; d < D; ++d)
-    g.put("    case %d: return jit_change_stats32_n%d(P, S, X, j, aij, aji, d32, absf);\n", d, d);
-  g.s += "    default: *absf = 0.f; return 0.f;\n  }\n}\n";
+    g.put("    case %d: return jit_change_stats32_n%d(P, S, X, j, aij, aji, d32, d32lo, absf, flo);\n",
+          d, d);
+  g.s += "    default: *absf = 0.f; *flo = 0.f; return 0.f;\n  }\n}\n";
   g.s += "template <bool TERMS>\n"
          "__device__ __forceinline__ double jit_change_stats(int net, const DevProblem &P,\n"
          "    const Slice &S, const StepCtx &X, int j, int aij, int aji, double *d) {\n"
@@ -348,6 +386,17 @@ Compiled compile_spec(const std::string &spec) {
   const std::string src = std::string("#include \"saom_kernel.cuh\"\n") + spec +
                           (multi ? "#include \"saom_multi_kernel.cuh\"\n"
                                  : "#include \"saom_period.cuh\"\n");
+  // CUSNA_JIT_SOURCE_DIR: also write the generated translation unit there (a
+  // file per plan, named by a hash of its text), so it can be read, or
+  // compiled offline with nvcc against csrc/ for its register report
+  if (const char *dir = std::getenv("CUSNA_JIT_SOURCE_DIR")) {
+    char name[64];
+    std::snprintf(name, sizeof name, "/cusna_jit_%016zx.cu", std::hash<std::string>{}(src));
+    if (FILE *f = std::fopen((std::string(dir) + name).c_str(), "w")) {
+      std::fwrite(src.data(), 1, src.size(), f);
+      std::fclose(f);
+    }
+  }
   const auto t0 = std::chrono::steady_clock::now();
   nvrtcProgram prog = nullptr;
   if (N.create(&prog, src.c_str(), "cusna_period_jit.cu", kJitHeaderCount, kJitHeaderSources,

@@ -38,7 +38,8 @@ struct Slice {
   short *indeg, *outdeg;  // n each (degrees < 2^15 as n <= 8192)
   int *z;
   float *gbuf;       // n   upper bounds of the float32 Gumbel keys
-  float *blk;        // ceil(n/32)*(k+2)  per 32-alter block: max and log-sum-exp sums
+  float *blk;        // ceil(n/32)*2*(k+1)  per 32-alter block: the score sums as
+                     //   double-float pairs (or k+1 doubles on the float64 path)
   uint32_t *okbits;  // W
   int *tp;           // n   (transTies / gwdsp)
   int *tq;           // n   (gwdspFB)
@@ -59,14 +60,16 @@ struct Slice {
   uint32_t *rr3;     //   behaviour uniform
   int *ekind, *ecfn, *eoffd, *eofft;  // k  effect plan
   double *stepd, *stept;  // 4k  per-ministep K_STEP magnitudes and terms
-  float *stepd32, *stept32;  // 4k  their float32 images
+  float *stepd32, *stept32;  // 4k  their float32 roundings
+  float *stepdlo32, *steptlo32;  // 4k  and the remainders (double-float pairs)
+  float2 *etab;      // 64   2^(j/64) as double-float pairs (the score exponential)
 };
 
 struct SliceLayout {
   size_t bytes;  // per team
   size_t o_rows, o_cols, o_indeg, o_outdeg, o_z, o_g, o_blk, o_ok, o_tp, o_tq, o_tpeq, o_crate, o_red, o_th, o_sc, o_dstar, o_thb, o_bsc, o_rsc, o_p1, o_p2, o_tid,
       o_ety, o_dyn, o_i0, o_i1, o_i2, o_bty, o_rkind, o_misc, o_rtau, o_rnet, o_rfocal, o_rr3, o_ekind, o_ecfn, o_eoffd, o_eofft,
-      o_stepd, o_stept, o_th32, o_stepd32, o_stept32;
+      o_stepd, o_stept, o_th32, o_stepd32, o_stept32, o_stepdlo32, o_steptlo32, o_etab;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -84,7 +87,7 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_outdeg, (size_t)n * 2);
   put(s.o_z, (size_t)n * 4);
   put(s.o_g, (size_t)n * 4);
-  put(s.o_blk, (size_t)((n + 31) / 32) * (k + 2) * 4);
+  put(s.o_blk, (size_t)((n + 31) / 32) * 2 * (k + 1) * 4);
   put(s.o_ok, (size_t)W * 4);
   put(s.o_tp, need_tp || need_gw ? (size_t)n * 4 : 0);
   put(s.o_tq, need_tq ? (size_t)n * 4 : 0);
@@ -121,6 +124,9 @@ __host__ __device__ inline SliceLayout make_layout(int n, int W, int k, int kb, 
   put(s.o_th32, (size_t)k * 4);
   put(s.o_stepd32, (size_t)k * 4 * 4);
   put(s.o_stept32, (size_t)k * 4 * 4);
+  put(s.o_stepdlo32, (size_t)k * 4 * 4);
+  put(s.o_steptlo32, (size_t)k * 4 * 4);
+  put(s.o_etab, (size_t)64 * 8);
   s.bytes = al16(o);
   return s;
 }
@@ -171,6 +177,9 @@ __device__ __forceinline__ Slice carve(unsigned char *base, const SliceLayout &L
   s.th32 = (float *)(base + L.o_th32);
   s.stepd32 = (float *)(base + L.o_stepd32);
   s.stept32 = (float *)(base + L.o_stept32);
+  s.stepdlo32 = (float *)(base + L.o_stepdlo32);
+  s.steptlo32 = (float *)(base + L.o_steptlo32);
+  s.etab = (float2 *)(base + L.o_etab);
   return s;
 }
 
@@ -211,6 +220,39 @@ __device__ __forceinline__ int warp_multi_sum(R (&v)[V], int lane) {
   for (int s = 0; s < 5; ++s) {
     const int o = 16 >> s;
     if ((1 << s) >= V) v[0] = radd(v[0], __shfl_xor_sync(kFull, v[0], o));
+  }
+  return q;
+}
+
+// The same recursive halving over V double-float pairs (h[q], l[q]). ff_add is
+// symmetric in its operands (TwoSum's error term is exact), so the lanes that
+// share a quantity in the final stages agree.
+template <int V>
+__device__ __forceinline__ int warp_multi_sum_ff(float (&h)[V], float (&l)[V], int lane) {
+  int q = 0;
+#pragma unroll
+  for (int s = 0; (1 << s) < V; ++s) {
+    const int o = 16 >> s;
+    const int half = V >> (s + 1);
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int x = 0; x < half; ++x) {
+      const float sh = up ? h[x] : h[x + half], sl = up ? l[x] : l[x + half];
+      float kh = up ? h[x + half] : h[x], kl = up ? l[x + half] : l[x];
+      const float gh = __shfl_xor_sync(kFull, sh, o), gl = __shfl_xor_sync(kFull, sl, o);
+      ff_add(kh, kl, gh, gl);
+      h[x] = kh;
+      l[x] = kl;
+    }
+    if (up) q += half;
+  }
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int o = 16 >> s;
+    if ((1 << s) >= V) {
+      const float gh = __shfl_xor_sync(kFull, h[0], o), gl = __shfl_xor_sync(kFull, l[0], o);
+      ff_add(h[0], l[0], gh, gl);
+    }
   }
   return q;
 }
@@ -418,10 +460,14 @@ __device__ __forceinline__ void step_values(const Team &T, const DevProblem &P, 
         break;
       default: v = 0.0; break;
     }
+    const double tv = __dmul_rn(S.th[e], v);
+    const float v32 = (float)v, t32 = (float)tv;
     S.stepd[x] = v;
-    S.stept[x] = __dmul_rn(S.th[e], v);
-    S.stepd32[x] = (float)v;
-    S.stept32[x] = (float)S.stept[x];
+    S.stept[x] = tv;
+    S.stepd32[x] = v32;
+    S.stept32[x] = t32;
+    S.stepdlo32[x] = (float)__dsub_rn(v, (double)v32);
+    S.steptlo32[x] = (float)__dsub_rn(tv, (double)t32);
   }
 }
 
@@ -563,10 +609,18 @@ __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice 
 // interaction product, one in the product with theta) and the k additions add
 // at most (k-1)u absf, so |f32 - f| <= (k + 8) u absf for the float64 predictor
 // f of change_stats<true> (itself within 2^-50 absf of the exact sum).
+//
+// The same pass carries the double-float images the score sums use:
+// d32lo[e] with d32[e] + d32lo[e] = d_e to about 2^-48 (0 for the integer
+// counts), and *flo with f32 + *flo = f to about 2^-47 absf: each term's
+// remainder (an exact Dekker product for integer counts; theta times the
+// table's float32 remainder for looked-up values) plus the exact TwoSum error
+// of each float32 addition.
 template <bool MULTI>
 __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice &S,
                                                 const StepCtx &X, int j, int aij, int aji,
-                                                float *d32, float *absf) {
+                                                float *d32, float *d32lo, float *absf,
+                                                float *flo) {
   const int n = P.n, W = P.W, k = P.k, i = X.i;
   const int fl = P.flags;
   int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;
@@ -584,11 +638,12 @@ __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice
     }
   }
   const uint32_t sg = aij ? 0x80000000u : 0u;
-  float f = 0.f, a = 0.f;
+  float f = 0.f, a = 0.f, fo = 0.f;
 #pragma unroll 1
   for (int e = 0; e < k; ++e) {
     const int kind = S.ekind[e], cfn = S.ecfn[e];
-    float v, term = 0.f;
+    const float th = S.th32[e];
+    float v, vlo = 0.f, term = 0.f, tlo = 0.f;
     bool has_term = true;
     if (kind == K_CNT) {
       int c;
@@ -610,7 +665,8 @@ __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice
         default: c = S.outdeg[j]; break;  // 7
       }
       v = __uint_as_float(__float_as_uint((float)c) ^ sg);
-      term = __fmul_rn(S.th32[e], v);
+      term = __fmul_rn(th, v);
+      tlo = fmaf(th, v, -term);
     } else if (kind == K_LOOK) {
       int idx;
       switch (cfn) {
@@ -626,40 +682,66 @@ __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice
         default: idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo); break;  // 15
       }
       v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[e] + idx]) ^ sg);
-      term = __fmul_rn(S.th32[e], v);
+      vlo = __uint_as_float(__float_as_uint(P.tab32lo[S.eoffd[e] + idx]) ^ sg);
+      term = __fmul_rn(th, v);
+      tlo = fmaf(th, vlo, fmaf(th, v, -term));
     } else if (kind == K_STEP) {
       const int q = 2 * aij + aji;
       v = S.stepd32[4 * e + q];
+      vlo = S.stepdlo32[4 * e + q];
       term = S.stept32[4 * e + q];
+      tlo = S.steptlo32[4 * e + q];
     } else if (kind == K_ZERO) {
       v = 0.f;
       has_term = false;
     } else if (MULTI && kind == K_CROSS) {
       const int c = cross_count(S, X, n, W, cfn, S.eoffd[e], i, j);
-      const float m = (cfn == 36 && S.p1[e] >= 2.0) ? sqrtf((float)c) : (float)c;
+      const bool rt = cfn == 36 && S.p1[e] >= 2.0;
+      const float m = rt ? sqrtf((float)c) : (float)c;
+      // sqrt(c) = m + (c - m^2) / (2m) to ~2^-48 (one Newton step; the residual is exact)
+      const float mlo = (rt && c > 0) ? __fdiv_rn(fmaf(-m, m, (float)c), __fmul_rn(2.f, m)) : 0.f;
       v = __uint_as_float(__float_as_uint(m) ^ sg);
-      term = __fmul_rn(S.th32[e], v);
+      vlo = __uint_as_float(__float_as_uint(mlo) ^ sg);
+      term = __fmul_rn(th, v);
+      tlo = fmaf(th, vlo, fmaf(th, v, -term));
     } else if (S.tid[e] == 32) {
-      const int c2 = S.i2[e];
-      v = __fmul_rn(d32[S.i0[e]], d32[S.i1[e]]);
-      if (c2 >= 0) v = __fmul_rn(v, d32[c2]);
-      else if (aij) v = -v;
-      term = __fmul_rn(S.th32[e], v);
+      const int c0 = S.i0[e], c1 = S.i1[e], c2 = S.i2[e];
+      v = __fmul_rn(d32[c0], d32[c1]);
+      vlo = __fadd_rn(fmaf(d32[c0], d32[c1], -v),
+                      fmaf(d32[c0], d32lo[c1], __fmul_rn(d32lo[c0], d32[c1])));
+      if (c2 >= 0) {
+        const float v2 = __fmul_rn(v, d32[c2]);
+        vlo = __fadd_rn(fmaf(v, d32[c2], -v2), fmaf(v, d32lo[c2], __fmul_rn(vlo, d32[c2])));
+        v = v2;
+      } else if (aij) {
+        v = -v;
+        vlo = -vlo;
+      }
+      term = __fmul_rn(th, v);
+      tlo = fmaf(th, vlo, fmaf(th, v, -term));
     } else {
-      v = (float)gen_stat(P, S, X, e, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, nullptr);
-      term = __fmul_rn(S.th32[e], v);
+      const double v64 = gen_stat(P, S, X, e, j, aij, aji, ri_cj, ri_rj, rj_ci, ci_cj, ci_rj, nullptr);
+      v = (float)v64;
+      vlo = (float)__dsub_rn(v64, (double)v);
+      term = __fmul_rn(th, v);
+      tlo = fmaf(th, vlo, fmaf(th, v, -term));
     }
     if ((S.ety[e] == 1 && aij) || (S.ety[e] == 2 && !aij)) {
       v = 0.f;
+      vlo = 0.f;
       has_term = false;
     }
     d32[e] = v;
+    d32lo[e] = vlo;
     if (has_term) {
-      f = __fadd_rn(f, term);
+      float err;
+      two_sum(f, term, f, err);
+      fo = __fadd_rn(fo, __fadd_rn(err, tlo));
       a = __fadd_rn(a, fabsf(term));
     }
   }
   *absf = a;
+  *flo = fo;
   return f;
 }
 

@@ -24,8 +24,10 @@ struct LaunchShape {
 cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const long long *unit_start,
                           int nprob, long long total, unsigned long long *counter,
                           uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
-                          cudaStream_t st);
-int period_blocks_per_sm(int threads, size_t dyn_smem);
+                          cudaStream_t st, bool valid = false);
+// valid: the validation build of the period kernel (trace, supplied words;
+// CTAs of at most 256 threads)
+int period_blocks_per_sm(int threads, size_t dyn_smem, bool valid = false);
 
 static_assert(kMaxNet == CUSNA_MAXNET, "network capacity of the kernels and the ABI");
 static_assert(kMaxEff == CUSNA_MAXEFF, "effect capacity of the kernels and the ABI");

@@ -123,7 +123,8 @@ __device__ void chain_finish(const Team &T, const DevProblem &P, const Slice &S,
 #ifndef CUSNA_MINB_256
 #define CUSNA_MINB_256 2  // resident 256-thread CTAs per SM the register budget allows
 #endif
-template <int MAXT>
+// VALID: the validation build (trace records and caller-supplied words).
+template <int MAXT, bool VALID = false>
 __global__ void __launch_bounds__(MAXT, MAXT == 512 ? 1 : CUSNA_MINB_256)
 period_kernel(const DevProblem *__restrict__ probs, const long long *__restrict__ unit_start,
               int nprob, long long total, unsigned long long *counter, SliceLayout lay, int G,
@@ -142,6 +143,7 @@ period_kernel(const DevProblem *__restrict__ probs, const long long *__restrict_
   Slice S = carve(smem + (size_t)tw * lay.bytes, lay,
                   cols_scratch ? cols_scratch + slot * cols_words : nullptr,
                   rows_scratch ? rows_scratch + slot * cols_words : nullptr);
+  fill_exp_table(S.etab, T.tl, T.L);  // ordered before its first use by chain_init's barriers
   for (;;) {
     long long u = 0;
     if (T.tl == 0) u = (long long)atomicAdd(counter, 1ull);
@@ -160,7 +162,7 @@ period_kernel(const DevProblem *__restrict__ probs, const long long *__restrict_
       if (unit_start[mid] <= u) lo = mid; else hi = mid - 1;
     }
     const DevProblem &P = probs[lo];
-    run_chain(T, P, S, (int)(u - unit_start[lo]));
+    run_chain<VALID>(T, P, S, (int)(u - unit_start[lo]));
   }
 }
 

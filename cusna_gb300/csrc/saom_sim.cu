@@ -191,33 +191,37 @@ cudaError_t raise_dyn_smem(const void *func, size_t bytes) {
   return e;
 }
 
-template <int MAXT>
+template <int MAXT, bool VALID>
 static int blocks_per_sm_t(int threads, size_t dyn_smem) {
-  if (raise_dyn_smem((const void *)period_kernel<MAXT>, dyn_smem) != cudaSuccess) {
+  if (raise_dyn_smem((const void *)period_kernel<MAXT, VALID>, dyn_smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   int b = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, period_kernel<MAXT>, threads, dyn_smem) !=
-      cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, period_kernel<MAXT, VALID>, threads,
+                                                    dyn_smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return b;
 }
 
-int period_blocks_per_sm(int threads, size_t dyn_smem) {
-  return threads <= 256 ? blocks_per_sm_t<256>(threads, dyn_smem)
-                        : blocks_per_sm_t<512>(threads, dyn_smem);
+// The validation build exists for CTAs of up to 256 threads only.
+int period_blocks_per_sm(int threads, size_t dyn_smem, bool valid) {
+  if (valid) return threads <= 256 ? blocks_per_sm_t<256, true>(threads, dyn_smem) : 0;
+  return threads <= 256 ? blocks_per_sm_t<256, false>(threads, dyn_smem)
+                        : blocks_per_sm_t<512, false>(threads, dyn_smem);
 }
 
 cudaError_t launch_period(const LaunchShape &sh, const DevProblem *probs, const long long *unit_start,
                           int nprob, long long total, unsigned long long *counter,
                           uint32_t *cols_scratch, uint32_t *rows_scratch, size_t cols_words,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool valid) {
   const int threads = 32 * sh.G * sh.teams_per_cta;
   const size_t dyn = sh.lay.bytes * sh.teams_per_cta;
-  auto kern = threads <= 256 ? period_kernel<256> : period_kernel<512>;
+  if (valid && threads > 256) return cudaErrorInvalidConfiguration;
+  auto kern = valid ? period_kernel<256, true>
+                    : (threads <= 256 ? period_kernel<256, false> : period_kernel<512, false>);
   cudaError_t e = raise_dyn_smem((const void *)kern, dyn);
   if (e != cudaSuccess) return e;
   kern<<<sh.ctas, threads, dyn, st>>>(probs, unit_start, nprob, total, counter, sh.lay, sh.G,

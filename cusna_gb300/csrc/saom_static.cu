@@ -81,11 +81,14 @@ struct Bump {
   }
 };
 
-// Reads `cnt` ints of a device array into host storage (fixed-size, no heap).
-bool read_ints(const int32_t *src, int cnt, int *dst, int def) {
+// Queues a read of `cnt` ints of a device array into host storage (fixed-size,
+// no heap) on the caller's stream, so it follows the caller's own writes of
+// those inputs on that stream; the caller synchronises the stream before
+// reading dst.
+bool read_ints(const int32_t *src, int cnt, int *dst, int def, cudaStream_t s) {
   for (int q = 0; q < cnt; ++q) dst[q] = def;
   if (!src || cnt == 0) return true;
-  return cudaMemcpy(dst, src, (size_t)cnt * 4, cudaMemcpyDeviceToHost) == cudaSuccess;
+  return cudaMemcpyAsync(dst, src, (size_t)cnt * 4, cudaMemcpyDeviceToHost, s) == cudaSuccess;
 }
 
 thread_local int t_act[CUSNA_MAX_N];  // static storage for validating act
@@ -133,14 +136,16 @@ extern "C" CUSNA_API cusna_status cusna_saom_simulate_period_static(
 
   // ---- small descriptors, read into fixed host storage --------------------
   int tid[CUSNA_MAXEFF], i0[CUSNA_MAXEFF], i1[CUSNA_MAXEFF], i2[CUSNA_MAXEFF], dyn[CUSNA_MAXEFF];
-  if (!read_ints(p->type_ids, k, tid, 0) || !read_ints(p->int0, k, i0, -1) ||
-      !read_ints(p->int1, k, i1, -1) || !read_ints(p->int2, k, i2, -1) ||
-      !read_ints(p->dyn_flags, k, dyn, 0)) {
+  if (!read_ints(p->type_ids, k, tid, 0, s) || !read_ints(p->int0, k, i0, -1, s) ||
+      !read_ints(p->int1, k, i1, -1, s) || !read_ints(p->int2, k, i2, -1, s) ||
+      !read_ints(p->dyn_flags, k, dyn, 0, s) ||
+      (p->act && !read_ints(p->act, p->nact, t_act, 0, s)) ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaGetLastError();
     set_last_error("reading effect descriptors from the device failed");
     return CUSNA_ERR_CUDA;
   }
   if (p->act) {
-    if (!read_ints(p->act, p->nact, t_act, 0)) { set_last_error("reading act failed"); return CUSNA_ERR_CUDA; }
     for (int q = 0; q < p->nact; ++q)
       if (t_act[q] < 0 || t_act[q] >= n) { set_last_error("act entry out of range"); return CUSNA_ERR_SHAPE; }
   }
@@ -327,6 +332,7 @@ extern "C" CUSNA_API cusna_status cusna_saom_simulate_period_static(
   D.ekind = I32(oKind); D.ecfn = I32(oCfn); D.eoffd = I32(oOffd); D.eofft = I32(oOffd);
   D.tab = F64(oTab);
   D.tab32 = nullptr;  // no lookup tables in this plan
+  D.tab32lo = nullptr;
   D.stats = r->stats; D.ntim = r->ntim; D.scores = r->scores; D.dist = r->dist;
   D.dist_stat = r->dist_stat; D.steps = r->steps;
   if (kb) { D.bdist = r->bdist; D.bscores = r->bscores; D.z_end = r->z_end; }

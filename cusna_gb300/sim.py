@@ -13,7 +13,8 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import (ABI_VERSION, GpuOptions, SaomProblem, SaomResult, check, load_library)
+from .abi import (ABI_VERSION, GpuOptions, SaomProblem, SaomResult, ValidationOptions, check,
+                  load_library)
 from .glue import Marshalled, result_dict
 
 
@@ -85,6 +86,34 @@ def simulate_ex(m: Marshalled, opts: GpuOptions) -> dict:
     st = lib.cusna_saom_simulate_period_ex(C.byref(m.problem), C.byref(m.result), C.byref(opts))
     check(st, "cusna_saom_simulate_period_ex", lib)
     return result_dict(m)
+
+
+def simulate_validate(m: Marshalled, trace_cap: int = 0, ustream=None, lse64: bool = False,
+                      warps_per_chain: int = 0, chains_per_cta: int = 0):
+    """Validation mode (cusna_saom_simulate_period_validate): the outputs and
+    the per-ministep trace, an int32 array M x trace_cap x 4 of (step, focal
+    actor, choice, distance change), -1 past a chain's last ministep; the
+    choice is the chosen alter, or -(d + 2) for a behaviour step d. ustream
+    (M x steps x (4 + n) uint32) replaces the Philox outputs of each chain's
+    first `steps` ministeps; lse64 forms the score sums in float64 at every
+    ministep."""
+    lib = load_library()
+    M = int(m.problem.M)
+    tr = np.full((M, max(int(trace_cap), 0), 4), -1, dtype=np.int32)
+    us = None if ustream is None else np.ascontiguousarray(ustream, dtype=np.uint32)
+    o = ValidationOptions()
+    C.memset(C.addressof(o), 0, C.sizeof(o))
+    o.struct_version = ABI_VERSION
+    o.trace_cap = int(trace_cap)
+    o.trace = tr.ctypes.data if trace_cap else None
+    o.ustream_steps = 0 if us is None else int(us.shape[1])
+    o.ustream = None if us is None else us.ctypes.data
+    o.lse64 = int(bool(lse64))
+    o.warps_per_chain = int(warps_per_chain)
+    o.chains_per_cta = int(chains_per_cta)
+    st = lib.cusna_saom_simulate_period_validate(C.byref(m.problem), C.byref(m.result), C.byref(o))
+    check(st, "cusna_saom_simulate_period_validate", lib)
+    return result_dict(m), tr
 
 
 def simulate_batch(ms: list[Marshalled], opts: GpuOptions | None = None) -> list[dict]:

@@ -233,6 +233,48 @@ CUSNA_API cusna_status cusna_saom_simulate_batch(
     const cusna_saom_problem *problems, cusna_saom_result *results,
     int32_t count, cusna_gpu_options *opts);
 
+/* ---- validation mode (no counterpart in the reference) ----------------------
+ * cusna_saom_simulate_period with a per-ministep trace, for checking a
+ * trajectory step by step against the reference chooser
+ * (src/libcusna_saom_cpu.cpp:166-287), and optionally with caller-supplied
+ * random words in place of the Philox outputs. Every pointer is a host pointer.
+ *
+ * trace (trace_cap > 0): M*trace_cap records of 4 int32, chain-major; record s
+ * of chain c is (s, focal actor, choice, distance change) for the chain's
+ * ministep s < trace_cap. The choice of a network ministep is the chosen alter
+ * (the actor itself for "no change"), of a behaviour ministep -(d + 2) for the
+ * step d in {-1, 0, 1}; the change is that of the network distance (of the
+ * behaviour distance for a behaviour ministep). Records past a chain's last
+ * ministep are -1.
+ *
+ * ustream (ustream_steps > 0): M*ustream_steps*(4 + n) uint32 words,
+ * chain-major; for ministep s < ustream_steps of chain c the 4 + n words at
+ * ((c*ustream_steps + s)*(4 + n)) replace the Philox outputs: words 0-3 those
+ * of counter (s, c, 0, 0) (waiting time, network/behaviour choice, focal
+ * actor, behaviour step), word 4 + j the first output of counter (s, c, 1, j)
+ * (alter j's Gumbel draw). Later ministeps draw from Philox as usual.
+ *
+ * lse64 = 1 forms the score sums in float64 at every ministep, as the
+ * reference does (otherwise in double-float, with float64 only where a
+ * predictor leaves [-60, 60]). warps_per_chain / chains_per_cta (0: chosen by
+ * the library) force the launch shape; the validation build runs CTAs of at
+ * most 256 threads. The call runs the library's own kernel, never a
+ * specialised one, and no result depends on the launch shape. */
+typedef struct cusna_validation_options {
+    int32_t  struct_version;   /* CUSNA_ABI_VERSION                           */
+    int32_t  trace_cap;        /* trace records per chain (0: no trace)        */
+    int32_t *trace;            /* [opt] M*trace_cap*4 int32                   */
+    int32_t  ustream_steps;    /* ministeps per chain with supplied words      */
+    const uint32_t *ustream;   /* [opt] M*ustream_steps*(4+n) uint32           */
+    int32_t  lse64;            /* 1: score sums in float64 at every ministep   */
+    int32_t  warps_per_chain;  /* 0 = library's choice, else 1, 2, 4 or 8      */
+    int32_t  chains_per_cta;   /* 0 = library's choice                         */
+} cusna_validation_options;
+
+CUSNA_API cusna_status cusna_saom_simulate_period_validate(
+    const cusna_saom_problem *problem, cusna_saom_result *result,
+    const cusna_validation_options *opts);
+
 /* Evaluation statistics of M end networks on the GPU: the batched device
  * counterpart of the reference's host cusna_network_stats
  * (src/libcusna_saom_cpu.cpp:619-689). `a_batch` is M*n*n dense uint8 (the
@@ -402,11 +444,6 @@ CUSNA_API cusna_status cusna_typed_stats(
 CUSNA_API cusna_status cusna_gof_distribution(
     const uint8_t *a_batch, int32_t n, int32_t M, int32_t kind,
     const int32_t *levls, int32_t nlev, double *out);
-
-/* Measured float64 FMA throughput of the current device in TFLOP/s (an FMA
- * counts 2 flops): the peak against which the simulator's float64 work is
- * reported. Runs a short synthetic kernel. */
-CUSNA_API cusna_status cusna_measure_fp64_tflops(double *tflops);
 
 /* ---- period kernel specialised to an effect plan (no counterpart) ----------
  * The library's period kernel evaluates the model's effects through a per-

@@ -21,7 +21,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libcusna_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libcusna_ref.so")
-REF_SRC = os.environ.get("CUSNA_REFERENCE_DIR", "/root/reference")
+# the reference package checked out beside this repository, unless
+# CUSNA_REFERENCE_DIR names another place; absent on machines without it
+REF_SRC = os.environ.get("CUSNA_REFERENCE_DIR",
+                         os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def build(ref: bool = True) -> None:
@@ -77,6 +80,9 @@ class Oracle:
         self._gof.argtypes = [vp, i32, i32, i32, vp, i32, vp]
         self._gof.restype = i32
         if kind == "port":
+            self._val = self.lib.oracle_simulate_period_validate
+            self._val.argtypes = [C.POINTER(SaomProblem), C.POINTER(SaomResult), vp, i32, vp, i32]
+            self._val.restype = i32
             self._ph = self.lib.oracle_philox4x32
             self._ph.argtypes = [vp, vp, vp]
             self._ph.restype = i32
@@ -96,6 +102,23 @@ class Oracle:
         if st != 0:
             raise RuntimeError(f"{self.kind} simulate_period status {st}")
         return result_dict(m)
+
+    def simulate_validate(self, m, trace_cap: int = 0, ustream=None, threads: int = 0):
+        """Validation mode of the port (no counterpart in the reference): the
+        outputs and the per-ministep trace (M x trace_cap x 4 int32: step,
+        actor, choice, distance change; -1 past a chain's end), optionally
+        with supplied words (M x steps x (4 + n) uint32) in place of Philox."""
+        from cusna_gb300.glue import result_dict
+        M = int(m.problem.M)
+        tr = np.full((M, max(int(trace_cap), 0), 4), -1, dtype=np.int32)
+        us = None if ustream is None else np.ascontiguousarray(ustream, dtype=np.uint32)
+        steps = 0 if us is None else int(us.shape[1])
+        m.problem.threads = int(threads)
+        st = self._val(C.byref(m.problem), C.byref(m.result), tr.ctypes.data if trace_cap else None,
+                       int(trace_cap), None if us is None else us.ctypes.data, steps)
+        if st != 0:
+            raise RuntimeError(f"{self.kind} simulate_period_validate status {st}")
+        return result_dict(m), tr
 
     def simulate_multi(self, m) -> dict:
         """A marshalled multi-network period (cusna_gb300.glue.marshal_multi)."""

@@ -71,7 +71,41 @@ typedef struct {
     const uint8_t *inact;
     uint32_t k0, k1;
     int need_tp, need_rdeg;
+    /* validation mode (no counterpart in the reference): a per-ministep trace
+     * and caller-supplied 32-bit words in place of the Philox outputs */
+    int32_t *trace;          /* M*trace_cap records (step, actor, choice, delta) */
+    int trace_cap;
+    const uint32_t *us;      /* M*us_steps*(4+n) words, or NULL */
+    int us_steps;
 } octx;
+
+/* The four words of ministep ms of chain c: Philox counter (ms, c, 0, 0)
+ * (src/libcusna_saom_cpu.cpp:167), or the supplied words while they last. */
+static void step_words(const octx *C, uint32_t chain, long ms, uint32_t rr[4]) {
+    if (C->us && ms < C->us_steps) {
+        const uint32_t *u = C->us + ((size_t)chain * C->us_steps + (size_t)ms) * (4 + (size_t)C->n);
+        rr[0] = u[0]; rr[1] = u[1]; rr[2] = u[2]; rr[3] = u[3];
+    } else {
+        ph4((uint32_t)ms, chain, 0u, 0u, C->k0, C->k1, rr);
+    }
+}
+
+/* The Gumbel word of alter j in ministep ms: Philox counter (ms, c, 1, j),
+ * first output (src/libcusna_saom_cpu.cpp:266), or the supplied word. */
+static uint32_t alter_word(const octx *C, uint32_t chain, long ms, int j) {
+    uint32_t rr[4];
+    if (C->us && ms < C->us_steps)
+        return C->us[((size_t)chain * C->us_steps + (size_t)ms) * (4 + (size_t)C->n) + 4 + (size_t)j];
+    ph4((uint32_t)ms, chain, 1u, (uint32_t)j, C->k0, C->k1, rr);
+    return rr[0];
+}
+
+/* Record one ministep of chain `chain` in the validation trace. */
+static void trace_put(const octx *C, uint32_t chain, long ms, int actor, int choice, long delta) {
+    if (!C->trace || ms >= C->trace_cap) return;
+    int32_t *t = C->trace + ((size_t)chain * C->trace_cap + (size_t)ms) * 4;
+    t[0] = (int32_t)ms; t[1] = actor; t[2] = choice; t[3] = (int32_t)delta;
+}
 
 /* Change statistic of toggling i->j for one effect type, mutable state `a`
  * (dense), degrees, two-path counts tp (type 5). src/libcusna_saom_cpu.cpp:49-101. */
@@ -207,7 +241,7 @@ static void run_chain(const octx *C, uint32_t chain, uint8_t *a, int32_t *z,
 
     for (;;) {
         int is_net;
-        ph4((uint32_t)ms, chain, 0u, 0u, C->k0, C->k1, rr);
+        step_words(C, chain, ms, rr);
         if (nr > 0) {                       /* :170-193 non-basic rate draw */
             double S0 = 0.0, tau, tau_eff, tgt, acc;
             int idx;
@@ -288,9 +322,13 @@ static void run_chain(const octx *C, uint32_t chain, uint8_t *a, int32_t *z,
                 if (dn) s -= pd * cdn[e];
                 bsc[e] += s;
             }
-            if (d != 0) {
-                if (C->bkd[i]) bdist += labs((long)(zi + d - C->z0[i])) - labs((long)zi - C->z0[i]);
-                z[i] = zi + d;
+            {
+                long bd0 = bdist;
+                if (d != 0) {
+                    if (C->bkd[i]) bdist += labs((long)(zi + d - C->z0[i])) - labs((long)zi - C->z0[i]);
+                    z[i] = zi + d;
+                }
+                trace_put(C, chain, ms, i, -(d + 2), bdist - bd0);
             }
             msb++; ms++;
             if (C->cond && dist >= C->target) break;
@@ -355,9 +393,8 @@ static void run_chain(const octx *C, uint32_t chain, uint8_t *a, int32_t *z,
             okb[j] = (uint8_t)ok;
             fj[j] = f;
             if (ok && f > lmax) lmax = f;
-            ph4((uint32_t)ms, chain, 1u, (uint32_t)j, C->k0, C->k1, rr);
             if (ok) {
-                double g = f - log(-log(unif(rr[0])));
+                double g = f - log(-log(unif(alter_word(C, chain, ms, j))));
                 if (g > gbest || (g == gbest && j < jstar)) { gbest = g; jstar = j; }
             }
         }
@@ -374,6 +411,8 @@ static void run_chain(const octx *C, uint32_t chain, uint8_t *a, int32_t *z,
                 }
             for (e = 0; e < k; ++e) sc[e] += dsb[(size_t)jstar * k + e] - wsum[e] / sume;
         }
+        long dist0 = dist;
+        long ms0 = ms;
         ms++;
 
         /* :277-282 toggle */
@@ -390,6 +429,7 @@ static void run_chain(const octx *C, uint32_t chain, uint8_t *a, int32_t *z,
                 a[(size_t)jj * n + i] = (uint8_t)(1 - a[(size_t)jj * n + i]);
             }
         }
+        trace_put(C, chain, ms0, i, jstar, dist - dist0);
         if (nr > 0)
             for (q = 0; q < nr; ++q)
                 rsc[q] += C->rk[q] == 0 ? C->ru[(size_t)q * n + i]
@@ -604,8 +644,11 @@ cusna_status oracle_behavior_stats(const int32_t *z_batch, int32_t n, int32_t M,
 }
 
 /* Entry point, src/libcusna_saom_cpu.cpp:315-425. `threads` > 0 caps the
- * OpenMP team (the reference reads its thread count from the OpenMP runtime). */
-cusna_status oracle_simulate_period(const cusna_saom_problem *pb, cusna_saom_result *r) {
+ * OpenMP team (the reference reads its thread count from the OpenMP runtime).
+ * trace / us: the validation mode's trace and supplied words (NULL: none). */
+static cusna_status simulate_period(const cusna_saom_problem *pb, cusna_saom_result *r,
+                                    int32_t *trace, int32_t trace_cap, const uint32_t *us,
+                                    int32_t us_steps) {
     if (!pb || !r) return CUSNA_ERR_NULL_ARG;
     if (pb->struct_version != CUSNA_ABI_VERSION) return CUSNA_ERR_SHAPE;
     const int n = pb->n, W = pb->W, k = pb->k, M = pb->M, kb = pb->kb, nr = pb->nrate;
@@ -676,6 +719,8 @@ cusna_status oracle_simulate_period(const cusna_saom_problem *pb, cusna_saom_res
     C.cond = pb->conditional; C.target = pb->target_dist;
     C.k0 = (uint32_t)(pb->seed & 0xFFFFFFFFu); C.k1 = (uint32_t)(pb->seed >> 32);
     C.need_tp = need_tp; C.need_rdeg = need_rdeg;
+    C.trace = trace_cap > 0 ? trace : NULL; C.trace_cap = trace_cap;
+    C.us = us_steps > 0 ? us : NULL; C.us_steps = us_steps;
 
     /* The reference dereferences etypes, dyn_flags and dyc_idx for every
      * effect; the glue always passes them. Default them here so the oracle
@@ -750,6 +795,28 @@ cusna_status oracle_simulate_period(const cusna_saom_problem *pb, cusna_saom_res
     free(th); free(wt); free(p1); free(p2); free(vm); free(vb); free(ru); free(dym);
     free(z0); free(bkd); free(act); free(inact); free(zeros); free(minus);
     return CUSNA_OK;
+}
+
+cusna_status oracle_simulate_period(const cusna_saom_problem *pb, cusna_saom_result *r) {
+    return simulate_period(pb, r, NULL, 0, NULL, 0);
+}
+
+/* Validation mode (no counterpart in the reference): the same simulation,
+ * writing for each ministep s < trace_cap of chain c the record
+ * trace[(c*trace_cap + s)*4 ..] = (s, focal actor, choice, distance change),
+ * where the choice is the chosen alter of a network ministep (the actor itself
+ * for "no change") or -(d + 2) for a behaviour step d in {-1, 0, 1}, and the
+ * change is that of the network distance (of the behaviour distance for a
+ * behaviour ministep); and, for ministeps s < us_steps, reading the 4 + n
+ * words us[((c*us_steps + s)*(4 + n) ..] in place of the Philox outputs: words
+ * 0-3 replace counter (s, c, 0, 0), word 4 + j the first output of counter
+ * (s, c, 1, j). Records of unused slots are left as they were. */
+cusna_status oracle_simulate_period_validate(const cusna_saom_problem *pb, cusna_saom_result *r,
+                                             int32_t *trace, int32_t trace_cap,
+                                             const uint32_t *us, int32_t us_steps) {
+    if (trace_cap < 0 || us_steps < 0 || (trace_cap > 0 && !trace) || (us_steps > 0 && !us))
+        return CUSNA_ERR_NULL_ARG;
+    return simulate_period(pb, r, trace, trace_cap, us, us_steps);
 }
 
 cusna_status oracle_philox4x32(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]) {

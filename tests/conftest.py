@@ -7,7 +7,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = os.environ.get("CUSNA_REFERENCE_DIR", "/root/reference")
+# the reference package checked out beside this repository (or where
+# CUSNA_REFERENCE_DIR says); tests that read it skip where it is absent
+REFERENCE = os.environ.get("CUSNA_REFERENCE_DIR", os.path.join(os.path.dirname(ROOT), "reference"))
 FIXTURES = os.path.join(REFERENCE, "tests", "testthat", "fixtures")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 

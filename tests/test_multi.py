@@ -11,7 +11,7 @@ GPU (`-m gpu`): the library against the same golden vectors and against the
 oracle on wider cases (3 and 4 networks, word-edge n, networks too large for
 shared memory). Bar, as for the single-network simulator: trajectories, steps,
 rate scores and end networks identical; ntim within 1e-13 relative; float32
-scores within 1e-5 of the score scale.
+scores within one float32 ulp.
 """
 import ctypes as C
 import os
@@ -23,6 +23,7 @@ from cusna_gb300 import abi
 from cusna_gb300 import workloads as WL
 from cusna_gb300.glue import marshal_multi
 from tests.conftest import GOLDEN
+from tests.test_gpu_parity import assert_within_one_ulp
 from tests.golden.make_golden import (CROSS_TYPES, MULTI_M, SEEDS, cross_case, multi_digest,
                                       run_multi)
 
@@ -39,8 +40,7 @@ def assert_multi_parity(got: dict, ref: dict, tag=""):
         elif key == "ntim":
             np.testing.assert_allclose(a, b, rtol=1e-13, atol=0, err_msg=msg)
         else:  # float32 scores
-            scale = max(1.0, float(np.abs(b).max()))
-            np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-5 * scale, err_msg=msg)
+            assert_within_one_ulp(a, b, msg)
 
 
 def golden(kind, seed):

@@ -1,9 +1,11 @@
 """cusna_saom_simulate_period_static, the entry point for callers that cannot
-allocate device memory (for example inside CUDA-graph capture, or under a
-host that owns all device memory through its own allocator). It must give
-the same results as cusna_saom_simulate_period on the same problem, call
-after call, although all its scratch is one fixed device array that every
-call reuses. The file name makes pytest run it after every other test."""
+allocate device memory: a host whose device memory is all handed out by its
+own allocator (an R session that reserved the GPU for another framework, an
+embedding application with a fixed memory budget), or a latency-bound loop
+that must not enter the allocator. It must give the same results as
+cusna_saom_simulate_period on the same problem, call after call, although all
+its scratch is one fixed device array that every call reuses. The file name
+makes pytest run it after every other test."""
 import ctypes as C
 
 import numpy as np
@@ -37,7 +39,11 @@ def _outputs(m, dev):
 
 
 @pytest.mark.parametrize("kind,n,M", [("covariate", 60, 7), ("coevol", 45, 5),
-                                      ("structural", 70, 4), ("gw", 50, 6), ("masks", 41, 5)])
+                                      ("structural", 70, 4), ("gw", 50, 6), ("masks", 41, 5),
+                                      ("baseline", 33, 3), ("covariate_all", 40, 4),
+                                      ("interaction", 40, 4), ("typed", 40, 4),
+                                      ("conditional", 40, 4), ("composition", 40, 4),
+                                      ("symmetric", 40, 4), ("rates", 40, 4)])
 def test_static_entry_point_matches_allocating_one(gpu_lib, kind, n, M):
     torch = pytest.importorskip("torch")
     c = WL.parity_case(kind, seed=21, n=n, M=M)
