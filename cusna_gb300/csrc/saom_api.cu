@@ -423,7 +423,7 @@ struct ProbBufs {
   size_t x0T, x0cT, simT, simcT, kdistT, permT, keepT, forceT, keepcT, forcecT;
   size_t vmat, wtab, p1, p2, vb, ralpha, ru;
   size_t etypes, dyn, i0, i1, i2, act, z0, bkdist, inact, vmiss;
-  size_t ekind, ecfn, eoffd, eofft, pool, pool32, pool32lo;
+  size_t ekind, ecfn, eoffd, eofft, pool, pool2;
   // raw copies (host mode)
   size_t r_x0, r_sim, r_kd, r_pm, r_keep, r_force, r_theta, r_lam, r_lamb, r_thetab, r_tid,
       r_ety, r_dyn, r_i0, r_i1, r_i2, r_vmat64, r_vmat32, r_wtab64, r_wtab32, r_p164, r_p132,
@@ -465,8 +465,7 @@ void plan_problem(Planner &pl, Job &J, bool dev) {
   B.vmiss = NONE;
   B.ekind = pl.take(k * 4); B.ecfn = pl.take(k * 4); B.eoffd = pl.take(k * 4);
   B.eofft = pl.take(k * 4); B.pool = pl.take(J.F.pool.size() * 8);
-  B.pool32 = pl.take(J.F.pool.size() * 4);
-  B.pool32lo = pl.take(J.F.pool.size() * 4);
+  B.pool2 = pl.take(J.F.pool.size() * 8);
   if (!dev) {
     B.r_x0 = pl.take(n * W * 4);
     B.r_sim = maybe(pl, p->sim_out, n * W * 4);
@@ -652,22 +651,19 @@ cusna_status prepare(Job &J, bool dev, DevProblem &D, uint32_t chain_offset) {
   CU(cudaMemcpyAsync(at<int>(B.eofft), J.F.offt.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<double>(B.pool), J.F.pool.data(), J.F.pool.size() * 8, cudaMemcpyHostToDevice, st));
   {
-    // float32 lookup values for the float32 pass and their float32
-    // remainders, which make them double-float pairs for the score sums (a
+    // lookup values as double-float pairs: the float32 rounding (the float32
+    // pass) and the float32 rounding of the remainder (the score sums); a
     // pageable copy is staged before cudaMemcpyAsync returns, so the local
-    // vectors may go)
-    std::vector<float> p32(J.F.pool.size()), p32lo(J.F.pool.size());
-    for (size_t x = 0; x < p32.size(); ++x) {
-      p32[x] = (float)J.F.pool[x];
-      p32lo[x] = (float)(J.F.pool[x] - (double)p32[x]);
+    // vector may go
+    std::vector<float> p2(2 * J.F.pool.size());
+    for (size_t x = 0; x < J.F.pool.size(); ++x) {
+      p2[2 * x] = (float)J.F.pool[x];
+      p2[2 * x + 1] = (float)(J.F.pool[x] - (double)p2[2 * x]);
     }
-    CU(cudaMemcpyAsync(at<float>(B.pool32), p32.data(), p32.size() * 4, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(at<float>(B.pool32lo), p32lo.data(), p32lo.size() * 4,
-                       cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(at<float>(B.pool2), p2.data(), p2.size() * 4, cudaMemcpyHostToDevice, st));
   }
   D.ekind = at<int>(B.ekind); D.ecfn = at<int>(B.ecfn); D.eoffd = at<int>(B.eoffd);
-  D.eofft = at<int>(B.eofft); D.tab = at<double>(B.pool); D.tab32 = at<float>(B.pool32);
-  D.tab32lo = at<float>(B.pool32lo);
+  D.eofft = at<int>(B.eofft); D.tab = at<double>(B.pool); D.tab2 = at<float2>(B.pool2);
   auto out = [&](void *user, size_t off) -> void * {
     if (!user) return nullptr;
     return dev ? user : (off == NONE ? nullptr : at<char>(off));
@@ -972,6 +968,8 @@ cusna_status run_jobs(std::vector<Job> &jobs, bool dev, cusna_gpu_options *opts,
   std::vector<long long> units(jobs.size() + 1, 0);
   for (size_t q = 0; q < jobs.size(); ++q) {
     if ((s = prepare(jobs[q], dev, hp[q], off0)) != CUSNA_OK) return s;
+    // no scores requested: the kernel forms no score sums
+    if (!hp[q].scores) hp[q].flags |= F_NO_SCORES;
     units[q + 1] = units[q] + jobs[q].p->M;
   }
   if (valid) {
@@ -1417,6 +1415,7 @@ cusna_status plan_create(const cusna_saom_problem *problems, cusna_saom_result *
   std::vector<unsigned long long> seeds(count);
   for (int q = 0; q < count; ++q) {
     if ((s = prepare(jobs[q], true, hp[q], 0)) != CUSNA_OK) { plan_free(P); return s; }
+    if (!hp[q].scores) hp[q].flags |= F_NO_SCORES;  // no score sums without scores
     hp[q].prow = one ? 0 : 1;
     units[q + 1] = units[q] + jobs[q].p->M;
     seeds[q] = (unsigned long long)jobs[q].p->seed;

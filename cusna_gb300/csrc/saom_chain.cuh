@@ -306,63 +306,86 @@ __device__ __forceinline__ bool is_nan64(double x) {
   return ((b >> 52) & 0x7FF) == 0x7FF && (b & 0xFFFFFFFFFFFFFull) != 0;
 }
 
-// Score sums of one block of 32 alters (one per lane), as double-float pairs:
-// quantity 0 is the weight w = exp(f_j) of the lane's alter (relative to the
-// "no change" alter, whose predictor is 0), quantity 1+e is w * d_e (0 for the
-// "no change" alter and for non-permitted alters). The fixed recursive-halving
-// warp reduction leaves quantity q's block sum on the lanes reporting q, which
-// store it as the pair rec[2q], rec[2q+1]. LOMASK: bit e set when d_e may have
-// a nonzero double-float remainder (the integer counts have none).
+// The score sums are formed per alter group: the 32-alter blocks b (alter j
+// in block j >> 5, on lane j & 31) fall into nsb groups, block b into group
+// b mod nsb, with nsb fixed by n alone (about two blocks per group, an even
+// count where there are several, so a team of G warps, which takes groups
+// g, g+G, ..., shares them evenly for G up to nsb). A lane adds its alters of
+// a group in ascending block order into double-float accumulators, one warp
+// reduction per group follows, and the group records are combined in group
+// order: every sum's order depends on n and j only, never on the team size.
+__host__ __device__ __forceinline__ int lse_groups(int nb) {
+  const int g = 2 * ((nb + 3) / 4);
+  return g < nb ? g : nb;
+}
+
+// Adds one alter's score quantities to the lane's accumulators, held as
+// packed pairs of quantities (quantities 2x and 2x+1 in H[x], L[x]):
+// quantity 0 the weight w = exp(f_j) relative to the "no change" alter
+// (whose predictor is 0), quantity 1+e the product w * d_e (not for the "no
+// change" alter). Every product is a Dekker product of the weight's pair with
+// d_e's pair, added with TwoSum, two quantities per instruction. LOMASK: bit
+// e set when d_e may have a double-float remainder (integer counts have none).
 template <int V, unsigned LOMASK>
-__device__ __forceinline__ void block_lse(float *rec, float wh, float wl, const float *d32,
-                                          const float *d32lo, bool weighted, int k, int lane) {
-  float h[V], l[V];
-  h[0] = wh;
-  l[0] = wl;
+__device__ __forceinline__ void lse_accumulate(float2 (&H)[(V + 1) / 2], float2 (&L)[(V + 1) / 2],
+                                               float wh, float wl, const float *d32,
+                                               const float *d32lo, bool weighted, int k) {
+  const float2 w2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
 #pragma unroll
-  for (int q = 1; q < V; ++q) {
-    h[q] = 0.f;
-    l[q] = 0.f;
-    if (weighted && q - 1 < k) {
-      const float dh = d32[q - 1];
-      const float p = __fmul_rn(wh, dh);
-      h[q] = p;
-      if ((LOMASK >> (q - 1)) & 1u)
-        l[q] = __fadd_rn(fmaf(wh, dh, -p), fmaf(wh, d32lo[q - 1], __fmul_rn(wl, dh)));
-      else
-        l[q] = fmaf(wl, dh, fmaf(wh, dh, -p));
+  for (int x = 0; x < (V + 1) / 2; ++x) {
+    const int qa = 2 * x, qb = 2 * x + 1;
+    // d of quantity q: 1 for the weight itself, d_{q-1} for a product, 0
+    // beyond the model's effects or for the "no change" alter
+    const bool ua = qa == 0 || (weighted && qa - 1 < k), ub = qb < V && weighted && qb - 1 < k;
+    const float da = qa == 0 ? 1.f : (ua ? d32[qa - 1] : 0.f);
+    const float db = ub ? d32[qb - 1] : 0.f;
+    const float2 d2 = make_float2(da, db);
+    const float2 p = __fmul2_rn(w2, d2);
+    float2 pl = __ffma2_rn(wl2, d2, __ffma2_rn(w2, d2, make_float2(-p.x, -p.y)));
+    const bool la = qa > 0 && ((LOMASK >> (qa - 1)) & 1u), lb = (LOMASK >> (qb - 1)) & 1u;
+    if (la || lb) {
+      const float2 dl2 =
+          make_float2(la && ua ? d32lo[qa - 1] : 0.f, lb && ub ? d32lo[qb - 1] : 0.f);
+      pl = __ffma2_rn(w2, dl2, pl);
     }
+    ff_add2(H[x], L[x], p, pl);
   }
-  const int q = warp_multi_sum_ff<V>(h, l, lane);
-  const bool writer = (V >= 32) || ((lane & ((32 / V) - 1)) == 0);
+}
+
+// The group sums of the warp's lanes reduced by the fixed recursive-halving
+// warp reduction; the lane holding quantity q stores it as the pair
+// rec[2q], rec[2q+1].
+template <int V>
+__device__ __forceinline__ void lse_store(float *rec, float (&h)[V], float (&l)[V], int k,
+                                          int lane) {
+  bool writer;
+  const int q = warp_multi_sum_ff<V>(h, l, lane, &writer);
   if (writer && q <= k) {
     rec[2 * q] = h[0];
     rec[2 * q + 1] = l[0];
   }
 }
 
-// The block records of one pass combined by one warp of the team: lane l adds
-// blocks l, l+32, ... in order (double-float), then a fixed butterfly adds the
+// The group records combined by one warp of the team: lane l adds groups l,
+// l+32, ... in order (double-float), then the fixed warp reduction adds the
 // lanes' partial sums. Quantity q lands in S.red[32G + q] as a double, past
-// the warp slots the team reductions use. The order of every addition depends
-// on the block index only, so the result is the same for every team size.
+// the warp slots the team reductions use.
 template <int V>
-__device__ __forceinline__ void combine_blocks(const Team &T, const Slice &S, int n, int k) {
-  const int nb = (n + 31) >> 5;
+__device__ __forceinline__ void combine_groups(const Team &T, const Slice &S, int nsb, int k) {
   float h[V], l[V];
 #pragma unroll
   for (int q = 0; q < V; ++q) {
     h[q] = 0.f;
     l[q] = 0.f;
   }
-  for (int b = T.lane; b < nb; b += 32) {
+  for (int b = T.lane; b < nsb; b += 32) {
     const float *rec = S.blk + (size_t)b * 2 * (k + 1);
 #pragma unroll
     for (int q = 0; q < V; ++q)
       if (q <= k) ff_add(h[q], l[q], rec[2 * q], rec[2 * q + 1]);
   }
-  const int q = warp_multi_sum_ff<V>(h, l, T.lane);
-  const bool writer = (V >= 32) || ((T.lane & ((32 / V) - 1)) == 0);
+  bool writer;
+  const int q = warp_multi_sum_ff<V>(h, l, T.lane, &writer);
   if (writer && q <= k) S.red[32 * T.G + q] = __dadd_rn((double)h[0], (double)l[0]);
 }
 
@@ -393,10 +416,11 @@ __device__ __forceinline__ double f64_of(const DevProblem &P, const Slice &S, co
 // not depend on the team size; results land in S.red[32G + q]. Used when a
 // predictor leaves the double-float exponential's range or is not finite,
 // and at every ministep under F_LSE64. Called by the whole team.
-template <bool MULTI, int V>
+template <bool MULTI, int VQ>
 static __device__ __noinline__ void lse_float64(const Team &T, const DevProblem &P,
                                                 const Slice &S, const StepCtx &X, double *d,
                                                 int net) {
+  constexpr int V = VQ <= 8 ? 8 : (VQ <= 16 ? 16 : 32);  // warp_multi_sum's power of two
   const int n = P.n, k = P.k, L = T.L, i = X.i;
   long long mk = dkey(0.0);
   for (int j = T.tl; j < n; j += L) {
@@ -445,14 +469,105 @@ static __device__ __noinline__ void lse_float64(const Team &T, const DevProblem 
   }
 }
 
-// Compile-time width of the score sums (k + 1 quantities, a power of two) and
-// the mask of effects whose change statistic can have a double-float remainder.
+// Compile-time width of the score sums (the k + 1 quantities in a specialised
+// build; the library build rounds k + 1 up to a power of two) and the mask of
+// effects whose change statistic can have a double-float remainder (LOMASK).
 #if defined(CUSNA_JIT_SPEC)
-#define CUSNA_LSE_V (CUSNA_JIT_K + 1 <= 8 ? 8 : (CUSNA_JIT_K + 1 <= 16 ? 16 : 32))
+#define CUSNA_LSE_V (CUSNA_JIT_K + 1)
 #define CUSNA_LSE_LOMASK CUSNA_JIT_LOMASK
 #else
 #define CUSNA_LSE_LOMASK 0xFFFFFFFFu
 #endif
+
+// The pass over the alters of one network ministep (see net_choice): per
+// alter the change statistics, the float32 Gumbel key with its error bound
+// (into *best and S.gbuf), the permitted-alter bits (S.okbits) and, when the
+// double-float score sums are wanted (fast_sums), the alter's score
+// quantities into its lane's group accumulators; each group's sums end in its
+// record in S.blk. Returns true on lanes that saw a predictor outside the
+// double-float exponential's range.
+template <bool MULTI, bool VALID, int V>
+__device__ __forceinline__ bool alter_pass(const Team &T, const DevProblem &P, const Slice &S,
+                                           const StepCtx &X, long long ms, uint32_t chain,
+                                           float *d32, float *d32lo, KeyTop &best, bool fast_sums,
+                                           int net) {
+  const int n = P.n, k = P.k, i = X.i;
+  (void)net;
+  const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
+  const int nb = (n + 31) >> 5, nsb = lse_groups(nb);
+#ifdef CUSNA_JIT_K
+  constexpr int KS = CUSNA_JIT_K;
+#else
+  const int KS = k;
+#endif
+  bool wide = false;
+  for (int g = T.warp; g < nsb; g += T.G) {
+    float2 AH[(V + 1) / 2], AL[(V + 1) / 2];
+#pragma unroll
+    for (int x = 0; x < (V + 1) / 2; ++x) {
+      AH[x] = make_float2(0.f, 0.f);
+      AL[x] = make_float2(0.f, 0.f);
+    }
+    for (int b = g; b < nb; b += nsb) {
+      const int j = (b << 5) + T.lane;
+      bool ok = false, stay = false;
+      float f = 0.f;
+      float2 fx = make_float2(0.f, 0.f);
+      if (j < n) {
+        const int aij = bit_of(S.rowsT, n, i, j);
+        float ub = -INFINITY;
+        stay = j == i;
+        ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
+        if (ok) {
+          float absf = 0.f;
+#if defined(CUSNA_JIT_SPEC)
+          // the effect plan compiled in (saom_jit.cu): the same float32 values
+          if (!stay)
+            f = jit_change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo, &absf,
+                                   &fx);
+#elif defined(CUSNA_JIT_MULTI)
+          if (!stay)
+            f = jit_change_stats32(net, P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo,
+                                   &absf, &fx);
+#else
+          if (!stay)
+            f = change_stats32<MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo,
+                                      &absf, &fx);
+#endif
+          const float gk = __fsub_rn(f, loglog_est(alter_word<VALID>(P, S, ms, chain, j)));
+          const float E = __fadd_rn(__fmul_rn(ecoef, absf), 6e-6f);
+          ub = __fadd_rn(gk, E);
+          keytop_add(best, gk, E, j);
+        }
+        S.gbuf[j] = ub;
+      }
+      const uint32_t okb = __ballot_sync(kFull, ok);
+      if (T.lane == 0) S.okbits[b] = okb;
+      if (fast_sums && ok) {
+        float wh = 1.f, wl = 0.f;  // the "no change" alter: exp(0)
+        if (!stay) {
+          if (fabsf(f) <= kFFExpMax) {
+            exp_ff(fx.x, fx.y, S.etab, wh, wl);
+          } else {  // also NaN
+            wide = true;
+            wh = 0.f;
+          }
+        }
+        lse_accumulate<V, CUSNA_LSE_LOMASK>(AH, AL, wh, wl, d32, d32lo, !stay, KS);
+      }
+    }
+    if (fast_sums) {
+      float ah[V], al[V];
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        ah[q] = (q & 1) ? AH[q >> 1].y : AH[q >> 1].x;
+        al[q] = (q & 1) ? AL[q >> 1].y : AL[q >> 1].x;
+      }
+      lse_store<V>(S.blk + (size_t)g * 2 * (k + 1), ah, al, KS, T.lane);
+    }
+  }
+  return wide;
+}
 
 // One network ministep of focal actor i on the network of slice S, up to the
 // choice: change statistics, float32 keys and the double-float score sums, the
@@ -486,8 +601,8 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     T.sync();
   }
 
-  // ---- one pass over the alters ------------------------------------------
-  // Lane by lane, alters in ascending j: integer change statistics, the
+  // ---- one pass over the alters (alter_pass) -------------------------------
+  // Lane by lane: integer change statistics, the
   // float32 predictor f32_j (change_stats32) and the float32 Gumbel key
   // g_j = f32_j - loglog_est(u_j) with u_j from the reference's counters
   // (msteps, chain, 1, j). The key is within
@@ -495,70 +610,31 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   // of the float64 key f_j - log(-log u_j): (k + 8) u absf_j for f32_j, 4e-6
   // for loglog_est and u (absf_j + 23) for the subtraction (|f32_j| <= absf_j,
   // |log(-log u)| < 23). gbuf[j] keeps the upper bound g_j + E_j.
-  // The score sums are formed per block of 32 alters (alter j on lane j mod
-  // 32, whatever the team size) in double-float arithmetic: the predictor as
-  // the pair f32_j + flo_j (within ~2^-47 absf_j of the reference's float64
-  // f_j), its exponential relative to the "no change" alter (exp_ff, relative
-  // error ~2e-14), and the weighted change statistics; the blocks are
-  // combined after the choice in an order fixed by the block index
-  // (combine_blocks), so the scores do not depend on the launch shape. A
+  // The score sums are formed per group of alters (lse_groups; the grouping
+  // and every order of addition depend on n and j only) in double-float
+  // arithmetic: the predictor as a double-float pair (within ~2^-47 absf_j of
+  // the reference's float64 f_j), its exponential relative to the "no change"
+  // alter (exp_ff, relative error ~2e-14), and the weighted change
+  // statistics; the groups are combined after the choice in group order
+  // (combine_groups), so the scores do not depend on the launch shape. A
   // predictor outside [-60, 60] (or not finite) sends the ministep's sums to
-  // the float64 path (lse_float64), as does F_LSE64.
+  // the float64 path (lse_float64), as does F_LSE64. Without requested scores
+  // (F_NO_SCORES) no sums are formed.
   KeyTop best{-INFINITY, 0.f, -INFINITY, 0x7FFFFFFF};
-  const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
-  const bool fast_sums = (P.flags & F_LSE64) == 0;
-  bool wide = false;
-  for (int jb = 32 * T.warp; jb < n; jb += L) {
-    const int j = jb + T.lane;
-    bool ok = false, stay = false;
-    float f = 0.f, flo = 0.f;
-    if (j < n) {
-      const int aij = bit_of(S.rowsT, n, i, j);
-      float ub = -INFINITY;
-      stay = j == i;
-      ok = stay || (bit_of(P.permT, n, i, j) && !(P.maxdeg > 0 && aij == 0 && X.od_i >= P.maxdeg));
-      if (ok) {
-        float absf = 0.f;
-#if defined(CUSNA_JIT_SPEC)
-        // the effect plan compiled in (saom_jit.cu): the same float32 values
-        if (!stay)
-          f = jit_change_stats32(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo, &absf, &flo);
-#elif defined(CUSNA_JIT_MULTI)
-        if (!stay)
-          f = jit_change_stats32(net, P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo, &absf,
-                                 &flo);
-#else
-        if (!stay)
-          f = change_stats32<MULTI>(P, S, X, j, aij, bit_of(S.colsT, n, i, j), d32, d32lo, &absf,
-                                    &flo);
-#endif
-        const float g = __fsub_rn(f, loglog_est(alter_word<VALID>(P, S, ms, chain, j)));
-        const float E = __fadd_rn(__fmul_rn(ecoef, absf), 6e-6f);
-        ub = __fadd_rn(g, E);
-        keytop_add(best, g, E, j);
-      }
-      S.gbuf[j] = ub;
-    }
-    const uint32_t okb = __ballot_sync(kFull, ok);
-    if (T.lane == 0) S.okbits[jb >> 5] = okb;
-    if (fast_sums) {
-      float wh = 0.f, wl = 0.f;
-      if (ok) {
-        if (stay) wh = 1.f;
-        else if (fabsf(f) <= kFFExpMax) exp_ff(f, flo, S.etab, wh, wl);
-        else wide = true;  // also NaN
-      }
-      float *rec = S.blk + (size_t)(jb >> 5) * 2 * (k + 1);
+  const bool want_sums = (P.flags & F_NO_SCORES) == 0;
+  const bool fast_sums = want_sums && (P.flags & F_LSE64) == 0;
 #ifdef CUSNA_LSE_V
-      block_lse<CUSNA_LSE_V, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, CUSNA_JIT_K,
-                                               T.lane);
+  const bool wide = alter_pass<MULTI, VALID, CUSNA_LSE_V>(T, P, S, X, ms, chain, d32, d32lo, best,
+                                                          fast_sums, net);
 #else
-      if (k + 1 <= 8) block_lse<8, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, k, T.lane);
-      else if (k + 1 <= 16) block_lse<16, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, k, T.lane);
-      else block_lse<32, CUSNA_LSE_LOMASK>(rec, wh, wl, d32, d32lo, ok && !stay, k, T.lane);
+  bool wide;
+  if (k + 1 <= 8)
+    wide = alter_pass<MULTI, VALID, 8>(T, P, S, X, ms, chain, d32, d32lo, best, fast_sums, net);
+  else if (k + 1 <= 16)
+    wide = alter_pass<MULTI, VALID, 16>(T, P, S, X, ms, chain, d32, d32lo, best, fast_sums, net);
+  else
+    wide = alter_pass<MULTI, VALID, 32>(T, P, S, X, ms, chain, d32, d32lo, best, fast_sums, net);
 #endif
-    }
-  }
   if (__any_sync(kFull, wide) && T.lane == 0) S.misc[12] = (int)ms;
   T.sync();
   const KeyTop top = team_keytop(T, best, S.red + 26 * T.G);
@@ -596,7 +672,7 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   // sum of weights, 1+e: weighted sum of d_e), by a warp other than the
   // chosen alter's owner, which meanwhile forms the chosen alter's float64
   // statistics; on the float64 path, the whole team
-  const bool sums64 = !fast_sums || S.misc[12] == (int)ms;
+  const bool sums64 = want_sums && (!fast_sums || S.misc[12] == (int)ms);
   if (sums64) {
 #ifdef CUSNA_LSE_V
     lse_float64<MULTI, CUSNA_LSE_V>(T, P, S, X, d, net);
@@ -605,21 +681,23 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     else if (k + 1 <= 16) lse_float64<MULTI, 16>(T, P, S, X, d, net);
     else lse_float64<MULTI, 32>(T, P, S, X, d, net);
 #endif
-  } else {
+  } else if (fast_sums) {
     const int owner_warp = (jstar % L) >> 5;
     if (T.warp == (T.G > 1 ? (owner_warp + 1) % T.G : 0)) {
+      const int nsb = lse_groups((n + 31) >> 5);
 #ifdef CUSNA_LSE_V
-      combine_blocks<CUSNA_LSE_V>(T, S, n, CUSNA_JIT_K);
+      combine_groups<CUSNA_LSE_V>(T, S, nsb, CUSNA_JIT_K);
 #else
-      if (k + 1 <= 8) combine_blocks<8>(T, S, n, k);
-      else if (k + 1 <= 16) combine_blocks<16>(T, S, n, k);
-      else combine_blocks<32>(T, S, n, k);
+      if (k + 1 <= 8) combine_groups<8>(T, S, nsb, k);
+      else if (k + 1 <= 16) combine_groups<16>(T, S, nsb, k);
+      else combine_groups<32>(T, S, nsb, k);
 #endif
     }
   }
 
-  // ---- the chosen alter's change statistics, in float64 as the reference adds them
-  if (T.tl == jstar % L) {
+  // ---- the chosen alter's change statistics, in float64 as the reference
+  // adds them (for the score update only)
+  if (want_sums && T.tl == jstar % L) {
     if (jstar == i) {
       for (int e = 0; e < k; ++e) S.dstar[e] = 0.0;
     } else {
@@ -722,7 +800,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
     const int jstar = net_choice<false, VALID>(T, P, S, i, ms, chain, d, d32, d32lo);
     const int aij_star = bit_of(S.rowsT, n, i, jstar);
     T.sync();
-    if (T.tl < k) {
+    if (!(P.flags & F_NO_SCORES) && T.tl < k) {
       const int e = T.tl;
       const double s0 = S.red[32 * T.G], se = S.red[32 * T.G + 1 + e];
       S.sc[e] = __dadd_rn(S.sc[e], __dsub_rn(S.dstar[e], __ddiv_rn(se, s0)));

@@ -42,6 +42,7 @@ enum : int {
   F_HAS_STEP = 1 << 14,    // some effect is constant within a ministep
   F_HAS_Z = 1 << 15,       // behaviour values are read (behaviour or dynamic covariates)
   F_LSE64 = 1 << 16,       // score log-sum-exp in float64 at every ministep (validation)
+  F_NO_SCORES = 1 << 17,   // no scores requested: the score sums are not formed
 };
 
 // How the change statistic d_e of toggling i -> j is formed (DevProblem::ekind).
@@ -114,8 +115,10 @@ struct DevProblem {
   // effect plan (k each) and its table pool
   const int *ekind, *ecfn, *eoffd, *eofft;
   const double *tab;
-  const float *tab32;    // float32 rounding of tab's lookup values (the float32 pass)
-  const float *tab32lo;  // tab - tab32, rounded to float32: tab32 + tab32lo is tab to ~2^-48
+  // tab's lookup values as double-float pairs: .x the float32 rounding (the
+  // float32 pass), .y the float32 rounding of the remainder (x + y is tab's
+  // value to ~2^-48, for the score sums); one 8-byte load per lookup
+  const float2 *tab2;
 
   // outputs (chain-major), any may be null
   double *stats, *ntim;
@@ -216,6 +219,21 @@ __device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl)
   two_sum(ah, bh, s, e);
   ah = s;
   al = __fadd_rn(__fadd_rn(al, bl), e);
+}
+
+// The same on two independent pairs at once with the packed float32x2
+// instructions of this architecture (__fadd2_rn, __ffma2_rn: each component
+// rounded as __fadd_rn / __fmaf_rn), which issue one instruction for two
+// operations. a - b is fma(b, -1, a), one rounding of the exact difference.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ void ff_add2(float2 &ah, float2 &al, float2 bh, float2 bl) {
+  const float2 s = __fadd2_rn(ah, bh);
+  const float2 bb = sub2(s, ah);
+  const float2 e = __fadd2_rn(sub2(ah, sub2(s, bb)), sub2(bh, bb));
+  ah = s;
+  al = __fadd2_rn(__fadd2_rn(al, bl), e);
 }
 
 // Largest |x| the double-float exponential accepts; the score sums fall back

@@ -111,13 +111,13 @@ void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi)
   // change statistics and of the predictor for the score sums
   g.put("__device__ __forceinline__ float jit_change_stats32%s(const DevProblem &P, const Slice &S,\n"
         "    const StepCtx &X, int j, int aij, int aji, float *d32, float *d32lo, float *absf,\n"
-        "    float *flo) {\n", x);
+        "    float2 *fx) {\n", x);
   g.s += "  const int i = X.i;\n";
   gen_shape(g, J);
   g.s += "  (void)n; (void)W; (void)i; (void)aji; (void)d32lo;\n";
   gen_pair_counts(g, fl);
-  g.s += "  const uint32_t sg = aij ? 0x80000000u : 0u;\n"
-         "  float f = 0.f, a = 0.f, fo = 0.f;\n";
+  g.put("  const uint32_t sg = aij ? 0x80000000u : 0u;\n"
+        "  float f = 0.f, a = 0.f, tt[%d], tl[%d];\n", k, k);
   for (int e = 0; e < k; ++e) {
     const int kind = J.kind[e], cfn = J.cfn[e], t = J.tid[e];
     g.put("  {  // effect %d: type %d, kind %d, function %d\n", e, t, kind, cfn);
@@ -132,10 +132,11 @@ void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi)
       if (cfn != 0 && cfn != 1) g.s += "    tlo = fmaf(th, v, -term);\n";
     } else if (kind == K_LOOK) {
       gen_index(g, cfn);
-      g.put("    v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[%d] + idx]) ^ sg);\n"
-            "    vlo = __uint_as_float(__float_as_uint(P.tab32lo[S.eoffd[%d] + idx]) ^ sg);\n"
+      g.put("    const float2 t2 = P.tab2[S.eoffd[%d] + idx];\n"
+            "    v = __uint_as_float(__float_as_uint(t2.x) ^ sg);\n"
+            "    vlo = __uint_as_float(__float_as_uint(t2.y) ^ sg);\n"
             "    term = __fmul_rn(th, v);\n"
-            "    tlo = fmaf(th, vlo, fmaf(th, v, -term));\n", e, e);
+            "    tlo = fmaf(th, vlo, fmaf(th, v, -term));\n", e);
     } else if (kind == K_STEP) {
       g.put("    const int q = 2 * aij + aji;\n"
             "    v = S.stepd32[%d + q];\n    vlo = S.stepdlo32[%d + q];\n"
@@ -175,11 +176,13 @@ void gen_functions(Gen &g, const JitPlan &J, const std::string &sfx, bool multi)
     if (J.ety[e] == 1) g.s += "    if (aij) { v = 0.f; vlo = 0.f; has_term = false; }\n";
     else if (J.ety[e] == 2) g.s += "    if (!aij) { v = 0.f; vlo = 0.f; has_term = false; }\n";
     g.put("    d32[%d] = v;\n    d32lo[%d] = vlo;\n", e, e);
-    g.s += "    if (has_term) {\n      float err;\n      two_sum(f, term, f, err);\n"
-           "      fo = __fadd_rn(fo, __fadd_rn(err, tlo));\n"
+    g.put("    tt[%d] = has_term ? term : 0.f;\n    tl[%d] = has_term ? tlo : 0.f;\n", e, e);
+    g.s += "    if (has_term) {\n      f = __fadd_rn(f, term);\n"
            "      a = __fadd_rn(a, fabsf(term));\n    }\n  }\n";
   }
-  g.s += "  *absf = a;\n  *flo = fo;\n  return f;\n}\n";
+  // the predictor as a double-float pair: the terms' pairs added in a fixed
+  // packed tree (f, the float32 sum in effect order, keys the choice)
+  g.put("  *absf = a;\n  *fx = ff_tree_sum<%d>(tt, tl);\n  return f;\n}\n", k);
   // float64 evaluation (change_stats): the chosen alter and uncertified choices
   g.put("template <bool TERMS>\n"
         "__device__ __forceinline__ double jit_change_stats%s(const DevProblem &P, const Slice &S,\n"
@@ -254,12 +257,12 @@ std::string jit_multi_spec_source(const std::vector<JitPlan> &nets) {
   // the chosen network's plan (warp-uniform per ministep)
   g.s += "__device__ __forceinline__ float jit_change_stats32(int net, const DevProblem &P,\n"
          "    const Slice &S, const StepCtx &X, int j, int aij, int aji, float *d32, float *d32lo,\n"
-         "    float *absf, float *flo) {\n"
+         "    float *absf, float2 *fx) {\n"
          "  switch (net) {\n";
   for (int d = 0; d < D; ++d)
-    g.put("    case %d: return jit_change_stats32_n%d(P, S, X, j, aij, aji, d32, d32lo, absf, flo);\n",
+    g.put("    case %d: return jit_change_stats32_n%d(P, S, X, j, aij, aji, d32, d32lo, absf, fx);\n",
           d, d);
-  g.s += "    default: *absf = 0.f; *flo = 0.f; return 0.f;\n  }\n}\n";
+  g.s += "    default: *absf = 0.f; *fx = make_float2(0.f, 0.f); return 0.f;\n  }\n}\n";
   g.s += "template <bool TERMS>\n"
          "__device__ __forceinline__ double jit_change_stats(int net, const DevProblem &P,\n"
          "    const Slice &S, const StepCtx &X, int j, int aij, int aji, double *d) {\n"
@@ -406,10 +409,11 @@ Compiled compile_spec(const std::string &spec) {
   }
   for (int q = 0; q < 2; ++q) N.add_name(prog, kNames[q]);
   // CUSNA_JIT_MINB: resident 256-thread CTAs per SM the register budget of
-  // the 256-thread instantiation allows (default 3: 85 registers; measured
-  // on the n=200, 4096-chain workload against 2, 75 vs 79 ms, and against 4,
-  // 62.4 vs 66.5 ms; equal to 2 at n=1000)
-  std::string minb = "-DCUSNA_MINB_256=3";
+  // the 256-thread instantiation allows (default 2: 128 registers). Measured
+  // on the n=200, 4096-chain workload: with the double-float score sums 2
+  // gives 90.3 ms against 92.9 for 3 (80 registers, which spill); the earlier
+  // float32 sums ran best with 3.
+  std::string minb = "-DCUSNA_MINB_256=2";
   if (const char *m = std::getenv("CUSNA_JIT_MINB")) minb = std::string("-DCUSNA_MINB_256=") + m;
   const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false",
                         "-default-device", "-DLIBCUSNA_BUILD", minb.c_str()};

@@ -224,37 +224,71 @@ __device__ __forceinline__ int warp_multi_sum(R (&v)[V], int lane) {
   return q;
 }
 
-// The same recursive halving over V double-float pairs (h[q], l[q]). ff_add is
-// symmetric in its operands (TwoSum's error term is exact), so the lanes that
-// share a quantity in the final stages agree.
+// Recursive halving over V double-float pairs (h[q], l[q]), any V <= 32: at
+// stage s (partner lane^(16>>s)) a lane holding c values keeps the lower
+// m = ceil(c/2) (bit clear) or the upper c - m, shifted down (bit set; an odd
+// c pads the upper half with a zero), and adds its partner's copies, so every
+// stage takes ceil(c/2) additions and V values need about V + 3 in all.
+// Afterwards the lane's h[0], l[0] is the warp total of quantity q (returned)
+// when *real is set; each quantity has exactly one such lane. ff_add is
+// symmetric in its operands (TwoSum's error term is exact).
 template <int V>
-__device__ __forceinline__ int warp_multi_sum_ff(float (&h)[V], float (&l)[V], int lane) {
-  int q = 0;
+__device__ __forceinline__ int warp_multi_sum_ff(float (&h)[V], float (&l)[V], int lane,
+                                                 bool *real) {
+  int q = 0, r = V;  // r: how many of the lane's values are real
+  int c = V;
 #pragma unroll
-  for (int s = 0; (1 << s) < V; ++s) {
+  for (int s = 0; s < 5; ++s) {
     const int o = 16 >> s;
-    const int half = V >> (s + 1);
+    const int m = (c + 1) >> 1;
     const bool up = (lane & o) != 0;
 #pragma unroll
-    for (int x = 0; x < half; ++x) {
-      const float sh = up ? h[x] : h[x + half], sl = up ? l[x] : l[x + half];
-      float kh = up ? h[x + half] : h[x], kl = up ? l[x + half] : l[x];
+    for (int x = 0; x < m; ++x) {
+      const bool pair = m + x < c;
+      const float vh = pair ? h[pair ? m + x : 0] : 0.f, vl = pair ? l[pair ? m + x : 0] : 0.f;
+      const float sh = up ? h[x] : vh, sl = up ? l[x] : vl;
+      float kh = up ? vh : h[x], kl = up ? vl : l[x];
       const float gh = __shfl_xor_sync(kFull, sh, o), gl = __shfl_xor_sync(kFull, sl, o);
       ff_add(kh, kl, gh, gl);
       h[x] = kh;
       l[x] = kl;
     }
-    if (up) q += half;
+    if (up) {
+      q += m;
+      r = r > m ? r - m : 0;
+    } else {
+      r = r < m ? r : m;
+    }
+    c = m;
   }
+  *real = r > 0;
+  return q;
+}
+
+// Sum of K double-float pairs (h[e], l[e]) in a fixed pairwise tree, two
+// additions per packed instruction: h[x] += h[x + m] for the upper half at
+// each level (an odd count leaves its middle element for the next level).
+template <int K>
+__device__ __forceinline__ float2 ff_tree_sum(float (&h)[K], float (&l)[K]) {
+  int c = K;
 #pragma unroll
   for (int s = 0; s < 5; ++s) {
-    const int o = 16 >> s;
-    if ((1 << s) >= V) {
-      const float gh = __shfl_xor_sync(kFull, h[0], o), gl = __shfl_xor_sync(kFull, l[0], o);
-      ff_add(h[0], l[0], gh, gl);
+    if (c > 1) {
+      const int m = (c + 1) >> 1, na = c - m;
+#pragma unroll
+      for (int x = 0; x + 1 < na; x += 2) {
+        float2 ah = make_float2(h[x], h[x + 1]), al = make_float2(l[x], l[x + 1]);
+        ff_add2(ah, al, make_float2(h[x + m], h[x + 1 + m]), make_float2(l[x + m], l[x + 1 + m]));
+        h[x] = ah.x;
+        h[x + 1] = ah.y;
+        l[x] = al.x;
+        l[x + 1] = al.y;
+      }
+      if (na & 1) ff_add(h[na - 1], l[na - 1], h[na - 1 + m], l[na - 1 + m]);
+      c = m;
     }
   }
-  return q;
+  return make_float2(h[0], l[0]);
 }
 
 __device__ __forceinline__ long long warp_max_ll(long long x) {
@@ -612,15 +646,16 @@ __device__ __forceinline__ double change_stats(const DevProblem &P, const Slice 
 //
 // The same pass carries the double-float images the score sums use:
 // d32lo[e] with d32[e] + d32lo[e] = d_e to about 2^-48 (0 for the integer
-// counts), and *flo with f32 + *flo = f to about 2^-47 absf: each term's
-// remainder (an exact Dekker product for integer counts; theta times the
-// table's float32 remainder for looked-up values) plus the exact TwoSum error
-// of each float32 addition.
+// counts), and the predictor as a double-float pair *fx, within about
+// 2^-47 absf of f: each term's remainder (an exact Dekker product for integer
+// counts; theta times the table's float32 remainder for looked-up values)
+// plus the exact TwoSum error of each float32 addition (fx->x = f32 here; the
+// specialised build adds the term pairs in a packed tree instead).
 template <bool MULTI>
 __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice &S,
                                                 const StepCtx &X, int j, int aij, int aji,
                                                 float *d32, float *d32lo, float *absf,
-                                                float *flo) {
+                                                float2 *fx) {
   const int n = P.n, W = P.W, k = P.k, i = X.i;
   const int fl = P.flags;
   int ri_cj = 0, ri_rj = 0, rj_ci = 0, ci_cj = 0, ci_rj = 0, ricirj = 0;
@@ -681,8 +716,9 @@ __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice
         case 14: idx = i * n + j; break;
         default: idx = (S.z[i] - P.zlo) * P.zR + (S.z[j] - P.zlo); break;  // 15
       }
-      v = __uint_as_float(__float_as_uint(P.tab32[S.eoffd[e] + idx]) ^ sg);
-      vlo = __uint_as_float(__float_as_uint(P.tab32lo[S.eoffd[e] + idx]) ^ sg);
+      const float2 t2 = P.tab2[S.eoffd[e] + idx];
+      v = __uint_as_float(__float_as_uint(t2.x) ^ sg);
+      vlo = __uint_as_float(__float_as_uint(t2.y) ^ sg);
       term = __fmul_rn(th, v);
       tlo = fmaf(th, vlo, fmaf(th, v, -term));
     } else if (kind == K_STEP) {
@@ -741,7 +777,7 @@ __device__ __forceinline__ float change_stats32(const DevProblem &P, const Slice
     }
   }
   *absf = a;
-  *flo = fo;
+  *fx = make_float2(f, fo);
   return f;
 }
 

@@ -190,6 +190,7 @@ extern "C" CUSNA_API cusna_status cusna_saom_simulate_period_static(
   }
   if (kb > 0 || has_dyn) fl |= F_HAS_Z;
   if (r->want_end_nets && r->a_ends) fl |= F_WANT_ENDS;
+  if (!r->scores) fl |= F_NO_SCORES;  // no score sums without scores
 
   // ---- launch shape (as the autotuned entry points choose it) ------------
   int dev = 0, sms = 0, smem_optin = 0;
@@ -331,8 +332,7 @@ extern "C" CUSNA_API cusna_status cusna_saom_simulate_period_static(
   D.prow = 1;
   D.ekind = I32(oKind); D.ecfn = I32(oCfn); D.eoffd = I32(oOffd); D.eofft = I32(oOffd);
   D.tab = F64(oTab);
-  D.tab32 = nullptr;  // no lookup tables in this plan
-  D.tab32lo = nullptr;
+  D.tab2 = nullptr;  // no lookup tables in this plan
   D.stats = r->stats; D.ntim = r->ntim; D.scores = r->scores; D.dist = r->dist;
   D.dist_stat = r->dist_stat; D.steps = r->steps;
   if (kb) { D.bdist = r->bdist; D.bscores = r->bscores; D.z_end = r->z_end; }
