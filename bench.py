@@ -22,11 +22,17 @@ the ranks' ministeps over the slowest rank's time.
   mom_fit  (1 GPU, unless --no-mom) the second metric: MoM fit wall time on
          the n=300 panel, plain GPU Robbins-Monro against the surrogate-assisted
          fit, with both fits' convergence t-ratios, their estimates' agreement
-         in SE units and the number of period simulations each needed
+         in SE units and the number of period simulations each needed; the
+         surrogate fit again with its network term off (what the network
+         adds), and both fits again from the reference's default start
+  c1_fit   (unless --no-mom) the conditional MoM fit of the n=50 panel on the
+         GPU and over the CPU engine
+  c4       (unless --no-c4) ministeps/s of the n=1000 co-evolution workload
+         (1024 chains) with its CPU baseline
   batching (1 GPU, unless --no-batching) one Robbins-Monro round of the
          512-group workload (1024 problems of n = 20..400) through one-shot
          batch calls, a replayable plan, and the plan replayed from a CUDA
-         graph; --c3-fit adds the joint conditional MoM fit
+         graph, and the joint conditional MoM fit (unless --no-c3-fit)
 
 --impl reference times the reference's CPU engine on the host cores on a
 bounded sample of the same workload (oracle/_ref where it was compiled from
@@ -284,34 +290,81 @@ def cpu_baseline(args, inp, M, seed, lam, theta, lamb, thetab):
             "sample": f"{sample} of the {M} chains ({st} ministeps, {dt:.1f} s)"}
 
 
-def mom_fit_comparison(n3_check=True):
+def note(msg):
+    """Progress of the bench's sections on stderr (the JSON line is stdout)."""
+    sys.stderr.write(f"[bench {time.strftime('%H:%M:%S')}] {msg}\n")
+    sys.stderr.flush()
+
+
+def _surrogate_summary(sf, plain):
+    """What one surrogate-assisted fit did, beside the plain fit it is judged
+    against."""
+    fs = sf.fit
+    return {
+        "wall_s": fs.wall_time,
+        "max_abs_tconv": float(np.abs(fs.tconv).max()),
+        "max_abs_theta_diff_over_se": float(np.max(np.abs(fs.theta - plain.theta) / plain.se)),
+        "period_simulations": int(sf.n_period_sims),
+        "takeovers": sf.takeovers,
+        "plain_takeover_before_phase3": sf.fallback,
+        "judge_passed_first": bool(sf.judge[0]["passed"]) if sf.judge else None,
+        "surrogate_max_error_sd": float(np.max(sf.judge[0]["error"])) if sf.judge else None,
+        "phase_times_s": fs.phase_times,
+        "stages": [{"gate": np.round(st["gate"], 3).tolist(),
+                    "heldout_mse_surface": (None if st.get("val_surface") is None
+                                            else np.round(st["val_surface"], 4).tolist()),
+                    "heldout_mse_with_network": (None if st.get("val_net") is None
+                                                 else np.round(st["val_net"], 4).tolist()),
+                    "pilot_steps_se": [round(x, 3) for x in st.get("pilot_steps", [])]}
+                   for st in sf.stages],
+    }
+
+
+def mom_fit_comparison():
     """MoM fit wall time on the n=300 surrogate panel: plain GPU Robbins-Monro
-    (phases 1-3 of R/mom.R) against the surrogate-assisted fit, both started
+    (phases 1-3 of R/mom.R, rounds replayed from CUDA graphs, the phase-2
+    rounds without score sums) against the surrogate-assisted fit, both started
     from the same prior estimate (the data-generating theta, which the
-    surrogate's first training design is centred on). Both paths are warmed up
-    first (simulator, network kernels, graph capture); each fit is timed once
-    on the host clock."""
+    surrogate's first training design is centred on); the surrogate fit once
+    more with its network term off (the response surface alone), which shows
+    what the network adds; and both fits once more from the reference's default
+    start (R/mom.R:199-211). Everything is warmed up first (simulator, network
+    kernels, graph capture); each fit is timed once on the host clock."""
     from cusna_gb300 import data as D
     from cusna_gb300 import mom
     from cusna_gb300 import surrogate as S
-    eng = mom.GpuEngine()
-    waves, cov = WL.c5_panel(eng)
+    eng = mom.PlanEngine(use_graph=True)
+    waves, cov = WL.c5_panel(mom.GpuEngine())
     est = mom.mom_estimator(D.build_saom_data(waves), WL.c5_effects(cov), None, None, False,
                             dict(mom.DEFAULT_CONTROL), engine=eng)
     centre = WL.c5_theta_true()
-    # warm-up: one small simulation round and a tiny network fit
+    # warm-up: simulation rounds (the specialised kernel of this model) and a
+    # tiny network fit
     for _ in range(3):
-        mom.mom_simulate(est, centre, 256, np.random.default_rng(0), eng)
+        mom.mom_simulate(est, centre, 256, np.random.default_rng(0), mom.GpuEngine())
     from cusna_gb300 import sim as G
-    G.specialise_wait(900.0)   # the specialised period kernel of this model
+    G.specialise_wait(900.0)
     r = np.random.default_rng(0)
     S.MlpSurrogate(S.N_IN, est.k + 1, S.HIDDEN).fit(r.standard_normal((2048, S.N_IN)),
                                                       r.standard_normal((2048, est.k + 1)),
                                                       epochs=2, n_group=S.N_IN - est.k - 1)
+    note("c5: warm-up plain fit")
+    mom.mom_run(est, theta0=centre, engine=eng)          # plans and graphs of the plain fit
+    note("c5: surrogate fit")
     sf = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng)
+    note(f"c5: surrogate fit {sf.fit.wall_time:.1f} s; plain fit")
     plain = mom.mom_run(est, theta0=centre, engine=eng)
-    fs = sf.fit
+    note(f"c5: plain fit {plain.wall_time:.1f} s; surrogate fit without the network")
+    sf_off = S.mom_run_surrogate(est, centre, S.SurrogateControl(network=False), eng)
+    theta0 = mom.default_theta0(est)
+    note(f"c5: without network {sf_off.fit.wall_time:.1f} s; plain fit from the default start")
+    plain_cold = mom.mom_run(est, theta0=theta0, engine=eng)
+    note(f"c5: plain from default {plain_cold.wall_time:.1f} s; surrogate from the default start")
+    sf_cold = S.mom_run_surrogate(est, theta0, S.SurrogateControl(), eng)
+    note(f"c5: surrogate from default {sf_cold.fit.wall_time:.1f} s")
+    eng.close()
     ctl = est.control
+    fs = sf.fit
     return {
         "workload": "c5: n=300, 3 waves (wave 1 Bernoulli(0.03), waves 2-3 simulated at rate 7 "
                     "and theta_true), 7 evaluation effects + 2 rates, unconditional MoM",
@@ -324,12 +377,107 @@ def mom_fit_comparison(n3_check=True):
         "period_simulations": {"plain": int(plain.n_sims * est.P),
                                "surrogate": int(sf.n_period_sims)},
         "takeovers": sf.takeovers,
-        "surrogate_max_error_sd": float(np.max(sf.judge[0]["error"])),
+        "surrogate_max_error_sd": (float(np.max(sf.judge[0]["error"])) if sf.judge else None),
         "phase_times_s": {"plain": plain.phase_times, "surrogate": fs.phase_times},
         "training_pairs": int(sum(s["n_theta"] for s in sf.stages) * est.P),
+        "surrogate": _surrogate_summary(sf, plain),
+        "surrogate_without_network": _surrogate_summary(sf_off, plain),
+        "from_default_start": {
+            "theta0": np.round(theta0, 4).tolist(),
+            "plain_s": plain_cold.wall_time,
+            "plain_max_abs_tconv": float(np.abs(plain_cold.tconv).max()),
+            "plain_max_abs_theta_diff_over_se": float(np.max(np.abs(plain_cold.theta - plain.theta)
+                                                             / plain.se)),
+            "surrogate": _surrogate_summary(sf_cold, plain),
+        },
         "control": {"n1": ctl["n1"], "nsub": ctl["nsub"], "n2": list(ctl["n2"]),
                     "batch2": ctl["batch2"], "nD": ctl["nD"], "n3": ctl["n3"]},
+        "engine": "replayable plans (CUDA graphs); phase-2 rounds without score sums",
     }
+
+
+def c1_fit_comparison(args):
+    """C1: the conditional MoM fit of the n=50, 3-wave panel (density, recip,
+    transTrip; R/mom.R defaults with n3 = 1000), from the reference's default
+    start, through the GPU plan engine and through the same estimator over the
+    CPU engine (the oracle's restatement of the reference engine, all host
+    threads), host wall clock, one fit each."""
+    from cusna_gb300 import data as D
+    from cusna_gb300 import effects as E
+    from cusna_gb300 import mom
+    waves = WL.c1_panel(mom.GpuEngine())
+    effs = [E.make_effect_spec(x) for x in ("density", "recip", "transTrip")]
+    ctl = dict(mom.DEFAULT_CONTROL)
+    ctl["n3"] = 1000
+    eng = mom.PlanEngine(use_graph=True)
+    est = mom.mom_estimator(D.build_saom_data(waves), effs, None, None, True, ctl, engine=eng)
+    from cusna_gb300 import sim as G
+    for _ in range(3):
+        mom.mom_simulate(est, mom.default_theta0(est), 64, np.random.default_rng(0), mom.GpuEngine())
+    G.specialise_wait(900.0)
+    note("c1: warm-up fit")
+    mom.mom_run(est, engine=eng)        # plans, graphs and tuning of this model
+    fit = mom.mom_run(est, engine=eng)
+    note(f"c1: GPU fit {fit.wall_time:.1f} s")
+    eng.close()
+    out = {"workload": "c1: n=50, 3 waves (wave 1 Bernoulli(0.05), waves 2-3 simulated at rate 6, "
+                       "density -2.5, recip 2.0, transTrip 0.4); conditional MoM, R/mom.R "
+                       "defaults with n3=1000, from the default start",
+           "metric": "MoM fit wall time", "unit": "s", "higher_is_better": False,
+           "gpu_s": fit.wall_time, "theta": np.round(fit.theta, 4).tolist(),
+           "se": np.round(fit.se, 4).tolist(),
+           "max_abs_tconv": float(np.abs(fit.tconv).max()),
+           "phase_times_s": fit.phase_times, "simulations": int(fit.n_sims) * est.P}
+    if not args.no_cpu_baseline:
+        import oracle
+        port = oracle.Oracle("port")
+        est_c = mom.mom_estimator(D.build_saom_data(waves), effs, None, None, True, ctl,
+                                  engine=port)
+        cf = mom.mom_run(est_c, engine=port)
+        note(f"c1: CPU fit {cf.wall_time:.1f} s")
+        out["cpu_baseline"] = {
+            "value": cf.wall_time, "unit": "s", "cores": port.max_threads(), "kind": "port",
+            "sample": "the whole fit, the same estimator over the CPU engine",
+            "max_abs_tconv": float(np.abs(cf.tconv).max()),
+            "max_abs_theta_diff_over_se": float(np.max(np.abs(cf.theta - fit.theta) / fit.se))}
+        out["speedup_vs_cpu"] = cf.wall_time / fit.wall_time
+    return out
+
+
+def c4_throughput(args, torch, dev, stream):
+    """C4: batched network-behaviour co-evolution, n=1000, 1024 chains, through
+    the device-pointer entry point: the specialised kernel after the tuner
+    settles, mean of 3 calls' device time, beside the CPU engine on 8 chains."""
+    from cusna_gb300 import sim as G
+    inp, M, seed, lam, theta, lamb, thetab = workload("c4", 1024)
+    m = marshal_period(inp, M, seed, lam, theta, lamb=lamb, thetab=thetab)
+    device_copy(m, torch, dev)
+    opts = lambda: G.options(device_ptrs=True, stream=stream.cuda_stream)  # noqa: E731
+    for _ in range(3):
+        G.simulate_ex(m, opts())
+    G.specialise_wait(900.0)
+    for _ in range(10):
+        G.simulate_ex(m, opts())
+    kms, spec = [], []
+    for _ in range(3):
+        o = opts()
+        G.simulate_ex(m, o)
+        kms.append(o.elapsed_ms)
+        spec.append(o.specialised)
+        shape = (o.warps_per_chain, o.chains_per_cta)
+    torch.cuda.synchronize()
+    m_h = marshal_period(inp, M, seed, lam, theta, lamb=lamb, thetab=thetab)
+    steps = int(G.simulate(m_h)["steps"].sum())
+    res = {"workload": f"c4: {WORKLOADS['c4']}; M={M}", "metric": "ministeps/s",
+           "unit": "ministeps/s", "value": steps / (float(np.mean(kms)) / 1e3),
+           "kernel_ms": float(np.mean(kms)), "ministeps_per_call": steps,
+           "launch_shape": {"warps_per_chain": shape[0], "chains_per_cta": shape[1]},
+           "period_kernel": "specialised" if all(spec) else "library"}
+    if not args.no_cpu_baseline:
+        args2 = argparse.Namespace(**vars(args))
+        args2.workload, args2.cpu_chains = "c4", 8
+        res["cpu_baseline"] = cpu_baseline(args2, inp, M, seed, lam, theta, lamb, thetab)
+    return res
 
 
 def batching_comparison(full_fit=False):
@@ -375,9 +523,11 @@ def batching_comparison(full_fit=False):
            "round_ms": rounds, "chains_per_round": est.P,
            "plan_shape": {"warps_per_chain": shape[0], "chains_per_cta": shape[1],
                           "ctas": shape[2]}}
+    note(f"c3: rounds {rounds}")
     if full_fit:
         eng = mom.PlanEngine(use_graph=True)
         fit = mom.mom_run(est, engine=eng)
+        note(f"c3: fit {fit.wall_time:.1f} s")
         out["fit"] = {"wall_s": fit.wall_time, "phase_times_s": fit.phase_times,
                       "theta": fit.theta.tolist(), "se": fit.se.tolist(),
                       "tconv": fit.tconv.tolist(),
@@ -535,8 +685,10 @@ def main():
                     help="skip the multi-network simulator and estimator measurement")
     ap.add_argument("--no-batching", action="store_true",
                     help="skip the multi-group round timing (batch calls vs replayed plans)")
-    ap.add_argument("--c3-fit", action="store_true",
-                    help="also run the joint conditional MoM fit of the 512-group workload")
+    ap.add_argument("--no-c3-fit", action="store_true",
+                    help="skip the joint conditional MoM fit of the 512-group workload")
+    ap.add_argument("--no-c4", action="store_true",
+                    help="skip the n=1000 co-evolution throughput line")
     args = ap.parse_args()
     if args.chains == 0:
         args.chains = 4096 if args.workload == "c2" else 1024
@@ -635,6 +787,7 @@ def main():
     kern_avg_ms = float(np.mean(kernel_ms))
 
     # ---- end to end through the reference-facing C ABI ---------------------
+    note("timed steps done; end-to-end calls")
     e2e = None
     if not args.no_e2e:
         m_h = marshal_period(inp, M, seed, lam, theta, lamb=lamb, thetab=thetab)
@@ -655,35 +808,54 @@ def main():
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": 1e3 * float(np.mean(walls))}
 
+    note("CPU baseline")
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         cpu = cpu_baseline(args, inp, M, seed, lam, theta, lamb, thetab)
 
+    note("c3 batching")
     batching = None
     if not args.no_batching and ws == 1:
         try:
-            batching = batching_comparison(args.c3_fit)
+            batching = batching_comparison(not args.no_c3_fit)
         except Exception as exc:   # the simulator line is reported regardless
             batching = {"error": f"{type(exc).__name__}: {exc}"}
 
+    note("fran")
     fran = None
     if not args.no_multi and ws == 1:
         try:
             fran = fran_latency(args)
         except Exception as exc:  # reported, never fatal to the headline line
             fran = {"error": f"{type(exc).__name__}: {exc}"}
+    note("multi-network")
     multi = None
     if not args.no_multi and ws == 1:
         try:
             multi = multi_comparison(args)
         except Exception as exc:  # reported, never fatal to the headline line
             multi = {"error": f"{type(exc).__name__}: {exc}"}
+    note("c5 MoM fits")
     mom_fit = None
     if not args.no_mom and ws == 1:
         try:
             mom_fit = mom_fit_comparison()
         except Exception as exc:   # the simulator line is reported regardless
             mom_fit = {"error": f"{type(exc).__name__}: {exc}"}
+    note("c1 fit")
+    c1_fit = None
+    if not args.no_mom and ws == 1:
+        try:
+            c1_fit = c1_fit_comparison(args)
+        except Exception as exc:   # reported, never fatal to the headline line
+            c1_fit = {"error": f"{type(exc).__name__}: {exc}"}
+    note("c4 throughput")
+    c4 = None
+    if not args.no_c4 and ws == 1 and args.workload == "c2":
+        try:
+            c4 = c4_throughput(args, torch, dev, stream)
+        except Exception as exc:   # reported, never fatal to the headline line
+            c4 = {"error": f"{type(exc).__name__}: {exc}"}
 
     clk = clocks.summary(local)
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -707,6 +879,8 @@ def main():
         "gpu_launches": int(sum(launches)), "clocks": clk,
         "wall_s_timed_region": t_wall,
         "mom_fit": mom_fit,
+        "c1_fit": c1_fit,
+        "c4": c4,
         "batching": batching,
         "multi": multi,
         "fran": fran,

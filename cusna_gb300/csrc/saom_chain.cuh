@@ -308,14 +308,14 @@ __device__ __forceinline__ bool is_nan64(double x) {
 
 // The score sums are formed per alter group: the 32-alter blocks b (alter j
 // in block j >> 5, on lane j & 31) fall into nsb groups, block b into group
-// b mod nsb, with nsb fixed by n alone (about two blocks per group, an even
-// count where there are several, so a team of G warps, which takes groups
-// g, g+G, ..., shares them evenly for G up to nsb). A lane adds its alters of
-// a group in ascending block order into double-float accumulators, one warp
-// reduction per group follows, and the group records are combined in group
-// order: every sum's order depends on n and j only, never on the team size.
+// b mod nsb, with nsb fixed by n alone (a multiple of 4 with up to two blocks
+// per group, so a team of G warps, which takes groups g, g+G, ..., shares
+// them evenly for G up to 4, and up to nsb). A lane adds its alters of a group
+// in ascending block order into double-float accumulators, one warp reduction
+// per group follows, and the group records are combined in group order: every
+// sum's order depends on n and j only, never on the team size.
 __host__ __device__ __forceinline__ int lse_groups(int nb) {
-  const int g = 2 * ((nb + 3) / 4);
+  const int g = 4 * ((nb + 7) / 8);
   return g < nb ? g : nb;
 }
 
@@ -501,14 +501,16 @@ __device__ __forceinline__ bool alter_pass(const Team &T, const DevProblem &P, c
   const int KS = k;
 #endif
   bool wide = false;
-  for (int g = T.warp; g < nsb; g += T.G) {
+  // without score sums the blocks are simply dealt to the warps in turn
+  const int ng = fast_sums ? nsb : nb;
+  for (int g = T.warp; g < ng; g += T.G) {
     float2 AH[(V + 1) / 2], AL[(V + 1) / 2];
 #pragma unroll
     for (int x = 0; x < (V + 1) / 2; ++x) {
       AH[x] = make_float2(0.f, 0.f);
       AL[x] = make_float2(0.f, 0.f);
     }
-    for (int b = g; b < nb; b += nsb) {
+    for (int b = g; b < nb; b += ng) {
       const int j = (b << 5) + T.lane;
       bool ok = false, stay = false;
       float f = 0.f;

@@ -87,6 +87,12 @@ class Marshalled:
     def out(self, name):
         return self.keep.get("out_" + name)
 
+    def drop_outputs(self, names):
+        """Stop requesting the named outputs (their result pointers become NULL)."""
+        for name in names:
+            if self.keep.pop("out_" + name, None) is not None:
+                setattr(self.result, name, None)
+
 
 def _c(a, dt):
     return np.ascontiguousarray(np.asarray(a, dtype=dt))

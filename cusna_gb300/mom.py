@@ -58,15 +58,21 @@ class PlanEngine(GpuEngine):
         self.use_graph = use_graph
         self._plans = {}
 
-    def simulate_round(self, est, theta, M: int, rng) -> list:
+    def simulate_round(self, est, theta, M: int, rng, scores: bool = True) -> list:
+        """scores=False: a plan whose results leave the scores out, so the
+        simulator forms no score sums (the Robbins-Monro steps of phase 2 read
+        only the statistics)."""
         from . import sim
         lam, th, lamb, thb, _ = split_theta(est, theta)
-        key = (id(est), int(M))
+        key = (id(est), int(M), bool(scores))
         plan = self._plans.get(key)
         if plan is None:
             ms = [marshal_period(d["inp"], M, int(rng.integers(1, np.iinfo(np.int32).max)), lam[q], th,
                                  lamb=lamb[q], thetab=thb if est.kb else None)
                   for q, d in enumerate(est.per)]
+            if not scores:
+                for m in ms:
+                    m.drop_outputs(("scores", "bscores"))
             plan = sim.SimPlan(ms, use_graph=self.use_graph)
             self._plans[key] = plan
         else:
@@ -218,14 +224,17 @@ class SimRound:
 
 
 def mom_simulate(est: Estimator, theta, M: int, rng, engine, keep_nets=False,
-                 theta_rows=None) -> SimRound:
+                 theta_rows=None, scores=True) -> SimRound:
     """All periods of one round in one batch launch (R/mom.R:129-170).
     theta_rows: optional (M, p) per-chain parameters (the simulator honours
-    per-chain theta; used to generate surrogate training data)."""
+    per-chain theta; used to generate surrogate training data). scores=False:
+    only the statistics are wanted (a plan engine then has the simulator skip
+    the score sums, and the pieces' score columns are zero)."""
     P, p, k, kb = est.P, est.p, est.k, est.kb
     lam, th, lamb, thb, off = split_theta(est, theta)
     if theta_rows is None and not keep_nets and hasattr(engine, "simulate_round"):
-        outs = engine.simulate_round(est, theta, M, rng)
+        outs = (engine.simulate_round(est, theta, M, rng) if scores
+                else engine.simulate_round(est, theta, M, rng, scores=False))
     else:
         ms = []
         for q in range(P):
@@ -239,8 +248,11 @@ def mom_simulate(est: Estimator, theta, M: int, rng, engine, keep_nets=False,
                 thb_arg = tr[:, off + k:p] if kb else None
             else:
                 lam_arg, th_arg, lamb_arg, thb_arg = lam[q], th, lamb[q], (thb if kb else None)
-            ms.append(marshal_period(d["inp"], M, seed, lam_arg, th_arg, lamb=lamb_arg,
-                                     thetab=thb_arg, want_ends=keep_nets))
+            m = marshal_period(d["inp"], M, seed, lam_arg, th_arg, lamb=lamb_arg,
+                               thetab=thb_arg, want_ends=keep_nets)
+            if not scores:
+                m.drop_outputs(("scores", "bscores"))
+            ms.append(m)
         outs = engine.simulate_batch(ms)
     stats_acc = np.zeros((M, p))
     pieces, nets, z_ends = [], ([] if keep_nets else None), ([] if keep_nets and est.coevol else None)
@@ -248,7 +260,9 @@ def mom_simulate(est: Estimator, theta, M: int, rng, engine, keep_nets=False,
     for q, r in enumerate(outs):
         sp = np.zeros((M, p))
         scp = np.zeros((M, p))
-        scores = r["scores"].astype(np.float64)
+        scores = (r["scores"].astype(np.float64) if "scores" in r
+                  else np.zeros((M, k + 1)))
+        bscores = r["bscores"] if "bscores" in r else np.zeros((M, kb + 1))
         if not est.conditional:
             sp[:, q] = r["dist_stat"] + est.rate_consts[q]
             scp[:, q] = scores[:, 0]
@@ -258,9 +272,9 @@ def mom_simulate(est: Estimator, theta, M: int, rng, engine, keep_nets=False,
                                            est.data.beh.overall_mean, est.data.beh.range,
                                            est.data.beh.sim_mean)
             sp[:, P + q] = r["bdist"]
-            scp[:, P + q] = r["bscores"][:, 0]
+            scp[:, P + q] = bscores[:, 0]
             sp[:, off + k:p] = bstats
-            scp[:, off + k:p] = r["bscores"][:, 1:kb + 1]
+            scp[:, off + k:p] = bscores[:, 1:kb + 1]
             if keep_nets:
                 z_ends.append(r["z_end"])
         sp[:, off:off + k] = r["stats"]
@@ -380,7 +394,7 @@ def mom_run(est: Estimator, theta0=None, engine=None, verbose=False, return_nets
         dinv = mom_dinv(mom_derivative(s.pieces), ctl["diagonalize"])
         thav = np.zeros(est.p)
         for _ in range(int(n2[sub])):
-            s = mom_simulate(est, theta, ctl["batch2"], rng, engine)
+            s = mom_simulate(est, theta, ctl["batch2"], rng, engine, scores=False)
             dev = s.stats.mean(axis=0) - est.targets
             theta = theta - guard_step(est, theta, gain * (dinv @ dev))
             thav += theta

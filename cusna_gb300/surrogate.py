@@ -23,12 +23,17 @@ that share one budget of training pairs (default 65,536):
      inside the stage's trust region (the box of its training thetas);
   4. between stages a plain pilot simulation at the estimate corrects it (a
      Newton step with the surrogate's Jacobian) and measures the covariance
-     that scales the next stage's design;
+     that scales the next stage's design (drawn within the previous stage's
+     trust region widened by its width on each side); when the pilots' steps
+     do not fall below a standard error, the surrogate is not trusted and
+     plain simulation takes over (the Robbins-Monro phases of R/mom.R from
+     the last pilot's point);
   5. phase 3 (R/mom.R:250-258) simulates as in the plain fit and judges the
      surrogate: its error is |simulated mean - surrogate mean| / simulated SD
      per statistic. When that error, or a convergence t-ratio, reaches the
      bound (0.1), plain simulation takes over: a Newton step with the phase-3
-     derivative and another phase 3, until the t-ratios are within the bound.
+     derivative and another phase 3, until the t-ratios are within the bound,
+     and the plain Robbins-Monro phases when a few such steps do not get there.
 """
 from __future__ import annotations
 
@@ -256,9 +261,17 @@ class MlpSurrogate:
             Rv = ys[val]
             self.alpha = np.clip((net * Rv).sum(axis=0) / np.maximum((net * net).sum(axis=0), 1e-30),
                                  0.0, 1.0)
+            # what the network adds: held-out mean squared error per output, in
+            # units of the response surface's residual SD, of the response
+            # surface alone (the residual itself) and with the gated network
+            val_surface = (Rv * Rv).mean(axis=0)
+            val_net = ((Rv - self.alpha * net) ** 2).mean(axis=0)
+        else:
+            val_surface = val_net = None
         torch.cuda.synchronize(self.dev)
         return dict(history=self.history, seconds=time.perf_counter() - t0, steps=steps * epochs,
-                    batch=batch, n_train=len(tr), n_val=n_val, best_val=best)
+                    batch=batch, n_train=len(tr), n_val=n_val, best_val=best,
+                    val_surface=val_surface, val_net=val_net)
 
     def _std_mse(self, Xs, Ys) -> float:
         y = self._forward_std(Xs)
@@ -377,6 +390,7 @@ class SurrogateControl:
     max_pilots: int = 4           # pilots between two stages at most
     pilot_tol: float = 1.0        # stop piloting once a step is below this many SEs
     seed: int = 4321
+    network: bool = True          # False: the response surface alone (no network term)
 
 
 @dataclass
@@ -387,6 +401,7 @@ class SurrogateFit:
     stages: list = field(default_factory=list)    # per stage: design, estimate, training
     theta_surrogate: np.ndarray | None = None
     n_period_sims: int = 0
+    fallback: str | None = None     # why plain simulation took over before phase 3
 
 
 class PanelSurrogate:
@@ -422,13 +437,17 @@ class PanelSurrogate:
         return mean
 
 
-def draw_thetas(est: mom.Estimator, centre, n_theta, rng, design, spread, chol=None):
+def draw_thetas(est: mom.Estimator, centre, n_theta, rng, design, spread, chol=None,
+                limit=None):
     """Training parameter vectors: centre + spread * z (design "iso") or
-    centre + spread * chol z (design "se"); rates are kept positive."""
+    centre + spread * chol z (design "se"); rates are kept positive, and every
+    coordinate within `limit` (lo, hi) when given."""
     p = est.p
     z = rng.standard_normal((n_theta, p))
     centre = np.asarray(centre, dtype=np.float64)
     theta = centre[None, :] + spread * (z if design == "iso" else z @ chol.T)
+    if limit is not None:
+        theta = np.clip(theta, limit[0], limit[1])
     n_rates = 0 if est.conditional else (2 * est.P if est.coevol else est.P)
     if n_rates:
         theta[:, :n_rates] = np.maximum(theta[:, :n_rates], 0.05 * np.abs(centre[:n_rates]) + 1e-3)
@@ -441,7 +460,7 @@ def training_pairs(est: mom.Estimator, theta, rng, engine, feats):
     after period: (P * rows, N_IN) and (P * rows, d)."""
     blocks = period_blocks(est)
     n_theta = theta.shape[0]
-    s = mom.mom_simulate(est, theta[0], n_theta, rng, engine, theta_rows=theta)
+    s = mom.mom_simulate(est, theta[0], n_theta, rng, engine, theta_rows=theta, scores=False)
     X, Y = [], []
     for q, (sp, _) in enumerate(s.pieces):
         b = blocks[q]
@@ -527,18 +546,23 @@ def mom_run_surrogate(est: mom.Estimator, centre, scontrol: SurrogateControl | N
         raise ValueError(f"{d} parameters per period exceed the surrogate input width {N_IN}")
     feats = period_features(est, engine, n_feat)
     stages, sur, chol, n_theta_total, n_pilot = [], None, None, 0, 0
+    limit, fallback = None, None
     for i, stg in enumerate(sc.stages):
         n_theta = max(16, -(-int(round(stg.frac * sc.n_pairs)) // est.P))
         design = stg.design if (stg.design == "iso" or chol is not None) else "iso"
         ta = time.perf_counter()
-        th = draw_thetas(est, theta, n_theta, rng, design, stg.spread, chol)
+        th = draw_thetas(est, theta, n_theta, rng, design, stg.spread, chol, limit)
         X, Y = training_pairs(est, th, rng, engine, feats)
         times["simulate_training"] += time.perf_counter() - ta
         n_theta_total += n_theta
         ta = time.perf_counter()
         net = MlpSurrogate(N_IN, d, sc.hidden, seed=sc.seed + i)
-        info = net.fit(X, Y, epochs=stg.epochs, batch=sc.batch, lr=sc.lr, seed=sc.seed + i,
-                       n_group=n_feat)
+        # without the network the fit trains no epochs: the untrained network
+        # predicts zero, so its gated term is zero and the surface stands alone
+        info = net.fit(X, Y, epochs=stg.epochs if sc.network else 0, batch=sc.batch, lr=sc.lr,
+                       seed=sc.seed + i, n_group=n_feat)
+        if not sc.network:
+            net.alpha = np.zeros(net.n_out)
         times["train"] += time.perf_counter() - ta
         sur = PanelSurrogate(est, net, feats)
         ta = time.perf_counter()
@@ -547,12 +571,14 @@ def mom_run_surrogate(est: mom.Estimator, centre, scontrol: SurrogateControl | N
         times["surrogate_rm"] += time.perf_counter() - ta
         rec = dict(design=design, spread=stg.spread, n_theta=n_theta, theta=theta.copy(),
                    train_seconds=info["seconds"], val=info.get("best_val"),
-                   gate=net.alpha.copy())
+                   gate=net.alpha.copy(), val_surface=info.get("val_surface"),
+                   val_net=info.get("val_net"))
         if i + 1 < len(sc.stages):
             # plain pilots with the surrogate's Jacobian (quasi-Newton) until
             # the step is below pilot_tol standard errors in every coordinate
             ta = time.perf_counter()
             rec["pilot_steps"] = []
+            step_se = np.inf
             for _ in range(sc.max_pilots):
                 prev = theta
                 theta, chol, pmean, psd = pilot_correction(est, sur, theta, sc.pilot, rng, engine, box)
@@ -565,15 +591,46 @@ def mom_run_surrogate(est: mom.Estimator, centre, scontrol: SurrogateControl | N
                     break
             times["pilot"] = times.get("pilot", 0.0) + time.perf_counter() - ta
             rec["theta_corrected"] = theta.copy()
+            # the next stage's draws stay inside this stage's trust region
+            # widened by its own width on each side, as the pilots do
+            limit = (box[0] - (box[1] - box[0]), box[1] + (box[1] - box[0]))
+            if step_se >= sc.pilot_tol:
+                # the surrogate's estimate did not hold up under the plain
+                # pilots: the surrogate is not trusted further, and plain
+                # simulation takes over (the Robbins-Monro phases of R/mom.R
+                # from the last pilot's point)
+                fallback = "pilot steps did not fall below pilot_tol standard errors"
         stages.append(rec)
         if verbose:
             print(f"[surrogate stage {i + 1}: {design} x{stg.spread}] theta =", np.round(rec["theta"], 4),
                   "corrected =", np.round(theta, 4))
+        if fallback:
+            break
+    def plain_takeover(theta, judge, takeovers, n_before):
+        # plain simulation takes over: the Robbins-Monro phases of R/mom.R
+        # from theta (a fit that does not depend on the surrogate any more)
+        ta = time.perf_counter()
+        plain = mom.mom_run(est, theta0=theta, engine=engine, verbose=verbose)
+        times["plain_takeover"] = time.perf_counter() - ta
+        n_sims = n_before + plain.n_sims
+        fit = mom.MomFit(plain.theta, plain.se, plain.tconv, plain.tconv_max, est.param_names,
+                         est.targets, plain.sim_means, plain.D, plain.msf, est.conditional,
+                         plain.rate_est, plain.rate_sd, int(n_sims), time.perf_counter() - t0,
+                         "gpu+surrogate (plain takeover)", None, None, times)
+        return SurrogateFit(fit, judge, takeovers + 1, stages, theta_sur, n_sims * est.P, fallback)
+
     theta_sur = theta.copy()
+    if fallback:
+        return plain_takeover(theta, [], 0, n_theta_total + n_pilot)
     ta = time.perf_counter()
     theta, p3, judge, takeovers = judge_and_take_over(est, sur, theta, engine, rng, ctl["n3"],
                                                       sc.bound, sc.max_takeovers, verbose)
     times["phase3"] = time.perf_counter() - ta
+    if not judge[-1]["passed"]:
+        # the judge's Newton steps did not reach the bound either
+        fallback = "phase-3 Newton takeovers did not bring the t-ratios within the bound"
+        return plain_takeover(theta, judge, takeovers,
+                              n_theta_total + n_pilot + ctl["n3"] * len(judge))
     s, Dm, msf, dev, tconv, tconv_max, se = p3
     rate_est = s.ntim.mean(axis=0) if est.conditional else None
     rate_sd = s.ntim.std(axis=0, ddof=1) if est.conditional else None

@@ -6,7 +6,8 @@ the surrogate's Robbins-Monro, the response-surface Jacobian, and the judge
 with plain-simulation takeover (a surrogate that is wrong on purpose).
 GPU: on the n=300 panel, the surrogate-assisted fit reaches the plain GPU
 fit's estimates (within 0.1 SE, all |t-conv| < 0.1) with fewer simulations and
-in less wall time -- what the trained network gains over the plain method."""
+in less wall time; and the same fit with the network's term off (the response
+surface alone) shows what the trained network adds."""
 import numpy as np
 import pytest
 
@@ -135,27 +136,37 @@ def test_judge_rejects_a_wrong_surrogate_and_plain_simulation_takes_over(c1_est,
 
 
 # ---- GPU ---------------------------------------------------------------------
-@pytest.mark.gpu
-def test_gpu_surrogate_fit_matches_plain_fit_with_fewer_simulations():
-    eng = mom.GpuEngine()
-    waves, cov = WL.c5_panel(eng)
+@pytest.fixture(scope="module")
+def c5_gpu():
+    """The n=300 panel's estimator on the GPU plan engine, warmed up (the
+    period kernel specialised to this model, the network's kernels and
+    training graphs, the plain fit's plans and graphs), and its plain fit
+    from the data-generating theta."""
+    eng = mom.PlanEngine(use_graph=True)
+    waves, cov = WL.c5_panel(mom.GpuEngine())
     est = mom.mom_estimator(D.build_saom_data(waves), WL.c5_effects(cov), None, None, False,
                             dict(mom.DEFAULT_CONTROL), engine=eng)
     centre = WL.c5_theta_true()
-    # both fits run the period kernel specialised to this model: compiled
-    # first (the library compiles it in the background after a few uses)
     from cusna_gb300 import sim
     for _ in range(3):
-        mom.mom_simulate(est, centre, 64, np.random.default_rng(0), eng)
+        mom.mom_simulate(est, centre, 64, np.random.default_rng(0), mom.GpuEngine())
     sim.specialise_wait(900.0)
-    # and the network's kernels and training graphs are warm (a tiny fit)
     r = np.random.default_rng(0)
     S.MlpSurrogate(S.N_IN, est.k + 1, S.HIDDEN).fit(r.standard_normal((2048, S.N_IN)),
                                                       r.standard_normal((2048, est.k + 1)),
                                                       epochs=2, n_group=S.N_IN - est.k - 1)
-    sf = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng)
+    mom.mom_run(est, theta0=centre, engine=eng)
     plain = mom.mom_run(est, theta0=centre, engine=eng)
+    yield est, eng, centre, plain
+    eng.close()
+
+
+@pytest.mark.gpu
+def test_gpu_surrogate_fit_matches_plain_fit_with_fewer_simulations(c5_gpu):
+    est, eng, centre, plain = c5_gpu
+    sf = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng)
     fs = sf.fit
+    assert sf.fallback is None
     assert np.abs(fs.tconv).max() < 0.1 and np.abs(plain.tconv).max() < 0.1
     assert (np.abs(fs.theta - plain.theta) < 0.1 * plain.se).all(), \
         np.abs(fs.theta - plain.theta) / plain.se
@@ -164,3 +175,27 @@ def test_gpu_surrogate_fit_matches_plain_fit_with_fewer_simulations():
     assert fs.wall_time < plain.wall_time, (fs.wall_time, plain.wall_time)
     # the surrogate alone (before any takeover) was judged: its error is recorded
     assert np.isfinite(sf.judge[0]["error"]).all()
+
+
+@pytest.mark.gpu
+def test_gpu_what_the_network_adds_over_the_response_surface(c5_gpu):
+    """The same fit with the network's term off (the response surface alone)
+    against the fit with it. On the first stage's held-out training pairs the
+    network removes most of the surface's residual error; the first stage's
+    surrogate estimate then lies far closer to the plain fit's, the plain
+    pilots accept it, and the fit finishes on the surrogate. The surface alone
+    leads the pilots astray, plain simulation takes over, and the fit needs
+    more simulations and more time."""
+    est, eng, centre, plain = c5_gpu
+    on = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng)
+    off = S.mom_run_surrogate(est, centre, S.SurrogateControl(network=False), eng)
+    st_on, st_off = on.stages[0], off.stages[0]
+    assert np.all(st_off["gate"] == 0) and np.any(st_on["gate"] > 0)
+    assert np.mean(st_on["val_net"]) < 0.5 * np.mean(st_on["val_surface"]), \
+        (st_on["val_net"], st_on["val_surface"])
+    dist_on = np.max(np.abs(st_on["theta"] - plain.theta) / plain.se)
+    dist_off = np.max(np.abs(st_off["theta"] - plain.theta) / plain.se)
+    assert dist_on < dist_off, (dist_on, dist_off)
+    assert on.fallback is None and off.fallback is not None
+    assert off.n_period_sims > on.n_period_sims
+    assert off.fit.wall_time > on.fit.wall_time
