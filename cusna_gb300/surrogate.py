@@ -27,13 +27,14 @@ that share one budget of training pairs (default 65,536):
      trust region widened by its width on each side); when the pilots' steps
      do not fall below a standard error, the surrogate is not trusted and
      plain simulation takes over (the Robbins-Monro phases of R/mom.R from
-     the last pilot's point);
+     the fit's start);
   5. phase 3 (R/mom.R:250-258) simulates as in the plain fit and judges the
      surrogate: its error is |simulated mean - surrogate mean| / simulated SD
      per statistic. When that error, or a convergence t-ratio, reaches the
      bound (0.1), plain simulation takes over: a Newton step with the phase-3
      derivative and another phase 3, until the t-ratios are within the bound,
-     and the plain Robbins-Monro phases when a few such steps do not get there.
+     and the plain Robbins-Monro phases when a few such steps do not get there
+     (from the last point when it is near the targets, else from the start).
 """
 from __future__ import annotations
 
@@ -620,16 +621,21 @@ def mom_run_surrogate(est: mom.Estimator, centre, scontrol: SurrogateControl | N
         return SurrogateFit(fit, judge, takeovers + 1, stages, theta_sur, n_sims * est.P, fallback)
 
     theta_sur = theta.copy()
+    start = np.asarray(centre, dtype=np.float64).copy()
     if fallback:
-        return plain_takeover(theta, [], 0, n_theta_total + n_pilot)
+        # the pilots wandered: the plain phases start again from the fit's start
+        return plain_takeover(start, [], 0, n_theta_total + n_pilot)
     ta = time.perf_counter()
     theta, p3, judge, takeovers = judge_and_take_over(est, sur, theta, engine, rng, ctl["n3"],
                                                       sc.bound, sc.max_takeovers, verbose)
     times["phase3"] = time.perf_counter() - ta
     if not judge[-1]["passed"]:
-        # the judge's Newton steps did not reach the bound either
+        # the judge's Newton steps did not reach the bound either: the plain
+        # phases continue from the last phase-3 point when it is near the
+        # targets (every |t-conv| below 3), else start again from the start
         fallback = "phase-3 Newton takeovers did not bring the t-ratios within the bound"
-        return plain_takeover(theta, judge, takeovers,
+        near = bool(np.max(np.abs(judge[-1]["tconv"])) < 3.0)
+        return plain_takeover(theta if near else start, judge, takeovers,
                               n_theta_total + n_pilot + ctl["n3"] * len(judge))
     s, Dm, msf, dev, tconv, tconv_max, se = p3
     rate_est = s.ntim.mean(axis=0) if est.conditional else None
