@@ -93,15 +93,17 @@ def smem_bytes_per_network_ministep(n, W):
 
 
 # Warp-instructions the period kernel executes per network ministep, from ncu
-# captures of the bench's own timed launch (smsp__inst_executed.sum over the
+# captures of the bench's own launches (smsp__inst_executed.sum over the
 # launch's 6,557,430 network ministeps; n=200, k=8, 4096 chains, autotuned
-# shape): the kernel specialised to the effect plan and the library kernel.
-INST_PER_MINISTEP = {("c2", True): 5813.0, ("c2", False): 10100.0}
-# DRAM bytes of one period-kernel launch per chain (the problem and the
-# outputs), from the full ncu capture of the specialised kernel at 1024 chains
-# (1.478 MB read + 0.209 MB written); a launch of M chains moves at most M times
-# this (the problem's share does not grow with M).
-DRAM_BYTES_PER_CHAIN = {"c2": (1478400.0 + 208640.0) / 1024}
+# shape): the kernel specialised to the effect plan and the library kernel;
+# and per ministep (network and behaviour, 6,146,609 a launch) of the n=1000
+# co-evolution workload's specialised kernel.
+INST_PER_MINISTEP = {("c2", True): 7704.0, ("c2", False): 14212.0, ("c4", True): 30523.0}
+# DRAM bytes of one period-kernel launch per chain (the problem, its tables and
+# the outputs), from the full ncu capture of the specialised kernel at 1024
+# chains (1.980 MB read + 0.995 MB written); a launch of M chains moves at
+# most M times this (the problem's share does not grow with M).
+DRAM_BYTES_PER_CHAIN = {"c2": (1980160.0 + 995328.0) / 1024}
 
 
 def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, specialised=True,
@@ -468,11 +470,20 @@ def c4_throughput(args, torch, dev, stream):
     torch.cuda.synchronize()
     m_h = marshal_period(inp, M, seed, lam, theta, lamb=lamb, thetab=thetab)
     steps = int(G.simulate(m_h)["steps"].sum())
+    rate = steps / (float(np.mean(kms)) / 1e3)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    ipm = INST_PER_MINISTEP.get(("c4", True)) if all(spec) else None
+    peak = 4.0 * sms * 2070e6 / 1e9
     res = {"workload": f"c4: {WORKLOADS['c4']}; M={M}", "metric": "ministeps/s",
-           "unit": "ministeps/s", "value": steps / (float(np.mean(kms)) / 1e3),
+           "unit": "ministeps/s", "value": rate,
            "kernel_ms": float(np.mean(kms)), "ministeps_per_call": steps,
            "launch_shape": {"warps_per_chain": shape[0], "chains_per_cta": shape[1]},
-           "period_kernel": "specialised" if all(spec) else "library"}
+           "period_kernel": "specialised" if all(spec) else "library",
+           "roofline": {"bound": "issue", "unit": "G warp-instructions/s",
+                        "achieved": rate * ipm / 1e9 if ipm else None, "peak": peak,
+                        "frac": rate * ipm / 1e9 / peak if ipm else None,
+                        "inst_per_ministep": ipm,
+                        "peak_source": "4 warp-instructions per cycle per SM x SMs x 2070 MHz"}}
     if not args.no_cpu_baseline:
         args2 = argparse.Namespace(**vars(args))
         args2.workload, args2.cpu_chains = "c4", 8

@@ -303,11 +303,15 @@ CUSNA_API cusna_status cusna_behavior_stats_gpu(
  * before returning and copies a few small host arrays. Every problem
  * and result pointer must be a device pointer (as with device_ptrs in
  * cusna_gpu_options), and the work runs on `stream` (a cudaStream_t; NULL for
- * the default stream). The call returns once the results are written.
+ * the default stream); the few descriptor arrays the host reads are copied
+ * on that stream, after the caller's own work there. The call returns once
+ * the results are written.
  * Its scratch is one fixed 16 MiB array in device memory. Every GPU that loads
  * the library holds that array until the process exits. A problem that needs
  * more scratch is refused with CUSNA_ERR_UNSUPPORTED and the size in
- * cusna_last_error(). The first call on each device looks up the array's
+ * cusna_last_error(); so is a problem whose chain out-rows do not fit one
+ * CTA's shared memory (n beyond about 1,200-1,300 actors, depending on the
+ * model). The first call on each device looks up the array's
  * device address (once). All calls share the array: calls whose GPU work
  * overlaps, from two streams
  * or two threads, race on it and must be serialised by the caller. */
