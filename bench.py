@@ -24,7 +24,8 @@ the ranks' ministeps over the slowest rank's time.
          fit, with both fits' convergence t-ratios, their estimates' agreement
          in SE units and the number of period simulations each needed; the
          surrogate fit again with its network term off (what the network
-         adds), and both fits again from the reference's default start
+         adds), both fits again from the reference's default start, and each
+         fit once more in a fresh process without warm-up (fresh_process)
   c1_fit   (unless --no-mom) the conditional MoM fit of the n=50 panel on the
          GPU and over the CPU engine
   c4       (unless --no-c4) ministeps/s of the n=1000 co-evolution workload
@@ -365,6 +366,8 @@ def mom_fit_comparison():
     sf_cold = S.mom_run_surrogate(est, theta0, S.SurrogateControl(), eng)
     note(f"c5: surrogate from default {sf_cold.fit.wall_time:.1f} s")
     eng.close()
+    fresh = cold_fits()
+    note(f"c5: fresh processes {fresh}")
     ctl = est.control
     fs = sf.fit
     return {
@@ -392,10 +395,47 @@ def mom_fit_comparison():
                                                              / plain.se)),
             "surrogate": _surrogate_summary(sf_cold, plain),
         },
+        "fresh_process": fresh,
         "control": {"n1": ctl["n1"], "nsub": ctl["nsub"], "n2": list(ctl["n2"]),
                     "batch2": ctl["batch2"], "nD": ctl["nD"], "n3": ctl["n3"]},
         "engine": "replayable plans (CUDA graphs); phase-2 rounds without score sums",
     }
+
+
+def cold_fit_child(which):
+    """--cold-fit plain|surrogate: one C5 fit in this fresh process, without any
+    warm-up (the period kernel comes from the on-disk cache of specialised
+    kernels when an earlier process compiled it); prints one JSON line."""
+    t_proc = time.perf_counter()
+    from cusna_gb300 import data as D
+    from cusna_gb300 import mom
+    from cusna_gb300 import surrogate as S
+    eng = mom.PlanEngine(use_graph=True)
+    waves, cov = WL.c5_panel(mom.GpuEngine())
+    est = mom.mom_estimator(D.build_saom_data(waves), WL.c5_effects(cov), None, None, False,
+                            dict(mom.DEFAULT_CONTROL), engine=eng)
+    centre = WL.c5_theta_true()
+    t0 = time.perf_counter()
+    if which == "plain":
+        fit = mom.mom_run(est, theta0=centre, engine=eng)
+    else:
+        fit = S.mom_run_surrogate(est, centre, S.SurrogateControl(), eng).fit
+    wall = time.perf_counter() - t0
+    print(json.dumps({"fit_s": wall, "fit_wall_time": fit.wall_time,
+                      "since_process_start_s": time.perf_counter() - t_proc,
+                      "max_abs_tconv": float(np.abs(fit.tconv).max())}), flush=True)
+
+
+def cold_fits():
+    """The C5 fits each in a fresh process (cold_fit_child), with the on-disk
+    cache of specialised kernels as the earlier fits of this run left it."""
+    out = {}
+    for which in ("plain", "surrogate"):
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cold-fit", which],
+                           capture_output=True, text=True, timeout=600)
+        lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+        out[which] = json.loads(lines[-1]) if lines else {"error": r.stderr[-500:]}
+    return out
 
 
 def c1_fit_comparison(args):
@@ -700,7 +740,11 @@ def main():
                     help="skip the joint conditional MoM fit of the 512-group workload")
     ap.add_argument("--no-c4", action="store_true",
                     help="skip the n=1000 co-evolution throughput line")
+    ap.add_argument("--cold-fit", choices=["plain", "surrogate"], default=None,
+                    help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.cold_fit:
+        return cold_fit_child(args.cold_fit)
     if args.chains == 0:
         args.chains = 4096 if args.workload == "c2" else 1024
     if args.impl == "reference":

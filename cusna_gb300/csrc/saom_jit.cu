@@ -3,6 +3,8 @@
 // loading and launch through driver entry points. See saom_jit.h.
 #include <cuda.h>
 #include <dlfcn.h>
+#include <unistd.h>
+#include <sys/stat.h>
 #include <nvrtc.h>
 
 #include <atomic>
@@ -287,6 +289,7 @@ struct Nvrtc {
   decltype(&nvrtcGetCUBIN) get_cubin = nullptr;
   decltype(&nvrtcGetLoweredName) lowered = nullptr;
   decltype(&nvrtcDestroyProgram) destroy = nullptr;
+  decltype(&nvrtcVersion) version = nullptr;  // optional (the cache key)
 };
 
 Nvrtc load_nvrtc() {
@@ -311,6 +314,7 @@ Nvrtc load_nvrtc() {
   sym(N.get_cubin, "nvrtcGetCUBIN");
   sym(N.lowered, "nvrtcGetLoweredName");
   sym(N.destroy, "nvrtcDestroyProgram");
+  N.version = reinterpret_cast<decltype(&nvrtcVersion)>(dlsym(h, "nvrtcVersion"));
   N.ok = ok;
   return N;
 }
@@ -377,18 +381,137 @@ struct Compiled {
   double seconds = 0.0;
 };
 
+// ---- on-disk cache of compiled specialisations -------------------------------
+// A compiled plan is written to CUSNA_JIT_CACHE_DIR (default
+// $XDG_CACHE_HOME/cusna_gb300, else ~/.cache/cusna_gb300; CUSNA_JIT_CACHE=0
+// turns the cache off) under a 128-bit hash of everything the compilation
+// depends on: the generated source, the text of every device header it
+// includes, the compiler options and the NVRTC version. A later process then
+// loads the cubin instead of compiling (milliseconds instead of seconds), and
+// a plan found in the cache is used from its first call. Files are written to
+// a temporary name and renamed, so a reader never sees a partial file.
+struct CacheKey {
+  uint64_t a = 1469598103934665603ull, b = 1099511628211ull * 31;
+  void add(const void *p, size_t n) {
+    const unsigned char *c = (const unsigned char *)p;
+    for (size_t i = 0; i < n; ++i) {
+      a = (a ^ c[i]) * 1099511628211ull;                 // FNV-1a
+      b = (b + c[i] + 1) * 0x9E3779B97F4A7C15ull ^ (b >> 29);
+    }
+  }
+  void add(const std::string &s) { add(s.data(), s.size()); add("\0", 1); }
+};
+
+std::string cache_dir() {
+  const char *off = std::getenv("CUSNA_JIT_CACHE");
+  if (off && off[0] == '0') return "";
+  if (const char *d = std::getenv("CUSNA_JIT_CACHE_DIR")) return d;
+  if (const char *x = std::getenv("XDG_CACHE_HOME")) return std::string(x) + "/cusna_gb300";
+  if (const char *h = std::getenv("HOME")) return std::string(h) + "/.cache/cusna_gb300";
+  return "";
+}
+
+std::string compile_options_text() {
+  std::string minb = "-DCUSNA_MINB_256=2";
+  if (const char *m = std::getenv("CUSNA_JIT_MINB")) minb = std::string("-DCUSNA_MINB_256=") + m;
+  return minb;
+}
+
+// the cache file of a generated source ("" when the cache is off)
+std::string cache_path(const std::string &src) {
+  const std::string dir = cache_dir();
+  if (dir.empty()) return "";
+  static const std::string headers = [] {
+    std::string h;
+    for (int q = 0; q < kJitHeaderCount; ++q) h += std::string(kJitHeaderNames[q]) + kJitHeaderSources[q];
+    return h;
+  }();
+  CacheKey k;
+  k.add(src);
+  k.add(headers);
+  k.add(compile_options_text());
+  int major = 0, minor = 0;
+  if (nvrtc().version) nvrtc().version(&major, &minor);
+  k.add(&major, sizeof major);
+  k.add(&minor, sizeof minor);
+  char name[80];
+  std::snprintf(name, sizeof name, "/jit_%016llx%016llx.bin", (unsigned long long)k.a,
+                (unsigned long long)k.b);
+  return dir + name;
+}
+
+bool cache_read(const std::string &path, Compiled &C) {
+  if (path.empty()) return false;
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  char magic[8] = {};
+  uint64_t len[3] = {};
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "CUSNAJC1", 8) == 0 &&
+            std::fread(len, sizeof len[0], 3, f) == 3 && len[0] < 4096 && len[1] < 4096 &&
+            len[2] > 0 && len[2] < ((uint64_t)1 << 30);
+  if (ok) {
+    C.lowered[0].resize(len[0]);
+    C.lowered[1].resize(len[1]);
+    C.cubin.resize(len[2]);
+    ok = std::fread(&C.lowered[0][0], 1, len[0], f) == len[0] &&
+         std::fread(&C.lowered[1][0], 1, len[1], f) == len[1] &&
+         std::fread(C.cubin.data(), 1, len[2], f) == len[2];
+  }
+  std::fclose(f);
+  if (ok) C.status = 0;
+  return ok;
+}
+
+void cache_write(const std::string &path, const Compiled &C) {
+  if (path.empty() || C.status != 0) return;
+  const std::string dir = path.substr(0, path.rfind('/'));
+  // create the directory and its parent (~/.cache) when missing
+  const std::string parent = dir.substr(0, dir.rfind('/'));
+  if (!parent.empty()) mkdir(parent.c_str(), 0755);
+  mkdir(dir.c_str(), 0755);
+  const std::string tmp = path + ".tmp" + std::to_string((long long)getpid());
+  FILE *f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return;
+  const uint64_t len[3] = {C.lowered[0].size(), C.lowered[1].size(), C.cubin.size()};
+  bool ok = std::fwrite("CUSNAJC1", 1, 8, f) == 8 && std::fwrite(len, sizeof len[0], 3, f) == 3 &&
+            std::fwrite(C.lowered[0].data(), 1, len[0], f) == len[0] &&
+            std::fwrite(C.lowered[1].data(), 1, len[1], f) == len[1] &&
+            std::fwrite(C.cubin.data(), 1, len[2], f) == len[2];
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
+}
+
+std::string full_source(const std::string &spec) {
+  return std::string("#include \"saom_kernel.cuh\"\n") + spec +
+         (is_multi(spec) ? "#include \"saom_multi_kernel.cuh\"\n" : "#include \"saom_period.cuh\"\n");
+}
+
+// true when the plan's compiled kernel is in the on-disk cache
+bool cached(const std::string &spec) {
+  const std::string path = cache_path(full_source(spec));
+  return !path.empty() && access(path.c_str(), R_OK) == 0;
+}
+
 Compiled compile_spec(const std::string &spec) {
   Compiled C;
+  const bool multi = is_multi(spec);
+  const char *const *kNames = multi ? kMultiNames : kPeriodNames;
+  const std::string src = full_source(spec);
+  const std::string cpath = cache_path(src);
+  {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (cache_read(cpath, C)) {
+      C.log = "loaded from the on-disk cache " + cpath;
+      C.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      return C;
+    }
+    C = Compiled();
+  }
   const Nvrtc &N = nvrtc();
   if (!N.ok) {
     C.log = "NVRTC is not available";
     return C;
   }
-  const bool multi = is_multi(spec);
-  const char *const *kNames = multi ? kMultiNames : kPeriodNames;
-  const std::string src = std::string("#include \"saom_kernel.cuh\"\n") + spec +
-                          (multi ? "#include \"saom_multi_kernel.cuh\"\n"
-                                 : "#include \"saom_period.cuh\"\n");
   // CUSNA_JIT_SOURCE_DIR: also write the generated translation unit there (a
   // file per plan, named by a hash of its text), so it can be read, or
   // compiled offline with nvcc against csrc/ for its register report
@@ -413,8 +536,7 @@ Compiled compile_spec(const std::string &spec) {
   // on the n=200, 4096-chain workload: with the double-float score sums 2
   // gives 90.3 ms against 92.9 for 3 (80 registers, which spill); the earlier
   // float32 sums ran best with 3.
-  std::string minb = "-DCUSNA_MINB_256=2";
-  if (const char *m = std::getenv("CUSNA_JIT_MINB")) minb = std::string("-DCUSNA_MINB_256=") + m;
+  const std::string minb = compile_options_text();
   const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false",
                         "-default-device", "-DLIBCUSNA_BUILD", minb.c_str()};
   const nvrtcResult r = N.compile(prog, (int)(sizeof opts / sizeof opts[0]), opts);
@@ -439,6 +561,7 @@ Compiled compile_spec(const std::string &spec) {
   }
   N.destroy(&prog);
   C.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  cache_write(cpath, C);
   return C;
 }
 
@@ -568,6 +691,8 @@ bool jit_get(const std::string &spec, JitKernel *out, bool now) {
     }
     if (E->state == S_FAILED) return false;
     ++E->uses;
+    // a plan in the on-disk cache loads in milliseconds: take it now
+    if (E->state == S_IDLE && !now && E->uses == 1 && cached(spec)) now = true;
     if (E->state == S_IDLE && (now || E->uses >= uses_before_compile())) {
       if (now) {
         E->state = S_QUEUED;

@@ -2,7 +2,8 @@
 NVRTC; csrc/saom_jit.cu).
 
 CPU: the generated source of every parity case's effect plan compiles (no
-device needed). GPU (`-m gpu`): every output of the specialised kernel is
+device needed), and a compiled plan is written to the on-disk cache and read
+back by a fresh process. GPU (`-m gpu`): every output of the specialised kernel is
 bit-identical to the library kernel's on every parity case and at the word
 edges, and a replayable plan switches to the specialised kernel once it is
 compiled without changing any output.
@@ -22,14 +23,51 @@ def marshal(c, **kw):
                           thetab=c["thetab"], **kw)
 
 
-def test_specialised_source_compiles_for_every_parity_case(built_lib):
+def test_specialised_source_compiles_for_every_parity_case(built_lib, monkeypatch):
     from cusna_gb300 import sim
+    monkeypatch.setenv("CUSNA_JIT_CACHE", "0")     # compile, whatever a cache holds
     cases = [WL.parity_case(kind, seed=0) for kind in WL.PARITY_KINDS]
     ms = [marshal(c) for c in cases]
     # NVRTC releases the interpreter while it compiles: one thread per case
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         secs = list(ex.map(sim.specialise_check, ms))
     assert all(s > 0 for s in secs)
+
+
+_CHILD = """
+import sys, json
+sys.path.insert(0, {root!r})
+from cusna_gb300 import sim, workloads as WL
+from cusna_gb300.glue import marshal_period
+c = WL.parity_case("covariate", seed=0)
+m = marshal_period(c["inp"], c["M"], c["seed"], c["lam"], c["theta"])
+print(json.dumps(sim.specialise_check(m)))
+"""
+
+
+def test_compiled_plans_are_cached_on_disk_for_the_next_process(built_lib, tmp_path):
+    """The first process compiles the plan (seconds) and writes it under
+    CUSNA_JIT_CACHE_DIR; a second, fresh process finds it and loads it in
+    milliseconds; CUSNA_JIT_CACHE=0 compiles again."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from tests.conftest import ROOT
+    env = dict(os.environ, CUSNA_JIT_CACHE_DIR=str(tmp_path))
+    env.pop("CUSNA_JIT_CACHE", None)
+
+    def run(e):
+        r = subprocess.run([sys.executable, "-c", _CHILD.format(root=ROOT)], env=e,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    first = run(env)
+    files = list(tmp_path.glob("jit_*.bin"))
+    assert len(files) == 1 and files[0].stat().st_size > 10000
+    second = run(env)
+    assert first > 1.0 and second < 0.5 * first and second < 1.0, (first, second)
+    assert run(dict(env, CUSNA_JIT_CACHE="0")) > 1.0
 
 
 class Engine:
