@@ -100,11 +100,11 @@ def smem_bytes_per_network_ministep(n, W):
 # and per ministep (network and behaviour, 6,146,609 a launch) of the n=1000
 # co-evolution workload's specialised kernel.
 INST_PER_MINISTEP = {("c2", True): 7704.0, ("c2", False): 14212.0, ("c4", True): 30523.0}
-# DRAM bytes of one period-kernel launch per chain (the problem, its tables and
-# the outputs), from the full ncu capture of the specialised kernel at 1024
-# chains (1.980 MB read + 0.995 MB written); a launch of M chains moves at
-# most M times this (the problem's share does not grow with M).
-DRAM_BYTES_PER_CHAIN = {"c2": (1980160.0 + 995328.0) / 1024}
+# DRAM bytes of one period-kernel launch of the bench workload (the problem, its
+# tables and the outputs), measured by ncu on the bench's own timed launch
+# (dram__bytes_read.sum 2,669,056 + dram__bytes_write.sum 2,578,944 at 4096
+# chains, specialised kernel).
+DRAM_BYTES_PER_LAUNCH = {("c2", 4096): 2669056.0 + 2578944.0}
 
 
 def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, specialised=True,
@@ -126,8 +126,7 @@ def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, spec
     fp32_peak = 256.0 * sm_count * hz / 1e12          # TFLOP/s, 128 FMA per cycle per SM
     smem = smem_bytes_per_network_ministep(n, W) * rate / 1e12
     flops = flops_per_network_ministep(n, k) * rate / 1e12
-    traffic = (DRAM_BYTES_PER_CHAIN[workload] * chains
-               if workload in DRAM_BYTES_PER_CHAIN and chains else None)
+    traffic = DRAM_BYTES_PER_LAUNCH.get((workload, int(chains))) if specialised else None
     hbm_peak, hbm_src = measured_hbm_gbs()
     dram = None
     if traffic is not None:
@@ -137,8 +136,8 @@ def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, spec
     return {"bound": "issue", "achieved": achieved, "peak": peak,
             "unit": "G warp-instructions/s", "frac": achieved / peak if achieved else None,
             "traffic": traffic,
-            "traffic_source": "ncu dram__bytes_read+write per chain at 1024 chains, times the "
-                              "launch's chains (an upper bound)",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the bench's "
+                              "timed launch (4096 chains)",
             "kernel_ms": kernel_ms, "network_ministeps_per_s": rate,
             "inst_per_ministep": ipm, "sm_mhz": mhz,
             "peak_source": "4 warp-instructions per cycle per SM x SMs x sampled SM clock",
