@@ -461,6 +461,11 @@ def c1_fit_comparison(args):
     fit = mom.mom_run(est, engine=eng)
     note(f"c1: GPU fit {fit.wall_time:.1f} s")
     eng.close()
+    # the same fit through the library's C entry point (cusna_mom_estimate:
+    # the Robbins-Monro loop in C++ over its own plans), warmed up once
+    mom.mom_run_native(est)
+    nat = mom.mom_run_native(est)
+    note(f"c1: C-ABI fit {nat.wall_time:.2f} s")
     out = {"workload": "c1: n=50, 3 waves (wave 1 Bernoulli(0.05), waves 2-3 simulated at rate 6, "
                        "density -2.5, recip 2.0, transTrip 0.4); conditional MoM, R/mom.R "
                        "defaults with n3=1000, from the default start",
@@ -468,7 +473,12 @@ def c1_fit_comparison(args):
            "gpu_s": fit.wall_time, "theta": np.round(fit.theta, 4).tolist(),
            "se": np.round(fit.se, 4).tolist(),
            "max_abs_tconv": float(np.abs(fit.tconv).max()),
-           "phase_times_s": fit.phase_times, "simulations": int(fit.n_sims) * est.P}
+           "phase_times_s": fit.phase_times, "simulations": int(fit.n_sims) * est.P,
+           "c_abi_fit": {"entry": "cusna_mom_estimate", "gpu_s": nat.wall_time,
+                         "phase_times_s": nat.phase_times,
+                         "max_abs_tconv": float(np.abs(nat.tconv).max()),
+                         "max_abs_theta_diff_over_se":
+                             float(np.max(np.abs(nat.theta - fit.theta) / fit.se))}}
     if not args.no_cpu_baseline:
         import oracle
         port = oracle.Oracle("port")

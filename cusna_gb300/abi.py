@@ -104,6 +104,27 @@ class ValidationOptions(C.Structure):
     ]
 
 
+class MomOptions(C.Structure):
+    """cusna_mom_options (include/libcusna.h): 0 in a field means its default."""
+    _fields_ = [
+        ("struct_version", C.c_int32), ("conditional", C.c_int32), ("firstg", C.c_double),
+        ("nsub", C.c_int32), ("n2", _p), ("batch2", C.c_int32), ("n1", C.c_int32),
+        ("nD", C.c_int32), ("n3", C.c_int32), ("diagonalize", C.c_double), ("seed", C.c_uint64),
+        ("rate_consts", _p), ("use_graph", C.c_int32), ("verbose", C.c_int32),
+    ]
+
+
+class MomResult(C.Structure):
+    """cusna_mom_result (include/libcusna.h): caller-owned output arrays."""
+    _fields_ = [
+        ("struct_version", C.c_int32), ("use_start", C.c_int32), ("theta", _p), ("se", _p),
+        ("tconv", _p), ("sim_means", _p), ("D", _p), ("msf", _p), ("rate_est", _p),
+        ("rate_sd", _p), ("tconv_max", C.c_double),
+        ("n_sims", C.c_int64), ("wall_seconds", C.c_double),
+        ("phase_seconds", C.c_double * 3),
+    ]
+
+
 def _here() -> str:
     return os.path.dirname(os.path.abspath(__file__))
 
@@ -162,6 +183,8 @@ def load_library(path: str | None = None):
     lib.cusna_saom_plan_shape.restype = i32
     lib.cusna_saom_plan_destroy.argtypes = [_p]
     lib.cusna_saom_plan_destroy.restype = None
+    lib.cusna_mom_estimate.argtypes = [P(SaomProblem), i32, _p, i32, P(MomOptions), P(MomResult)]
+    lib.cusna_mom_estimate.restype = i32
     sz, f32 = C.c_size_t, C.c_float
     lib.cusna_mlp_param_count.argtypes = [i32, i32, i32]
     lib.cusna_mlp_param_count.restype = sz
@@ -215,7 +238,7 @@ EXPORTED_SYMBOLS = [
     "cusna_network_stats_gpu", "cusna_behavior_stats_gpu",
     "cusna_saom_simulate_period_static", "cusna_saom_simulate_period_validate",
     "cusna_saom_plan_create", "cusna_saom_plan_launch", "cusna_saom_plan_set_epoch",
-    "cusna_saom_plan_shape", "cusna_saom_plan_destroy",
+    "cusna_saom_plan_shape", "cusna_saom_plan_destroy", "cusna_mom_estimate",
     "cusna_mlp_param_count", "cusna_mlp_workspace_bytes", "cusna_mlp_init", "cusna_mlp_forward",
     "cusna_mlp_grad", "cusna_mlp_train_step", "cusna_mlp_train_steps", "cusna_mlp_jacobian",
     "cusna_saom_simulate_multi", "cusna_cross_stats", "cusna_typed_stats",

@@ -593,8 +593,11 @@ Registry &reg() {
   return *R;
 }
 
+void stop_worker_at_exit();
+
 void worker_loop() {
   Registry &R = reg();
+  bool first = true;
   for (;;) {
     std::pair<std::string, Entry *> job;
     {
@@ -606,6 +609,11 @@ void worker_loop() {
       R.busy = true;
     }
     Compiled c = compile_spec(job.first);
+    // what the compiler built lazily during its first full compilation is
+    // destroyed at exit before the handlers registered earlier: register the
+    // stop handler once more, after it
+    if (first) std::atexit(stop_worker_at_exit);
+    first = false;
     {
       std::lock_guard<std::mutex> lk(R.mu);
       job.second->comp = std::move(c);
@@ -615,6 +623,24 @@ void worker_loop() {
     }
     R.cv.notify_all();
   }
+}
+
+// One tiny compilation with the plans' options in the calling thread, before
+// the stop handler is first registered: the compiler library constructs its
+// lazily built state here, so at exit (handlers and static destructors run in
+// the reverse order of their registration) the handler's wait for a
+// compilation in flight comes before that state is destroyed.
+void warm_up_compiler() {
+  const Nvrtc &N = nvrtc();
+  if (!N.ok) return;
+  nvrtcProgram prog = nullptr;
+  const char *src = "extern \"C\" __global__ void cusna_warm_up(float *x) { x[threadIdx.x] += 1.0f; }\n";
+  if (N.create(&prog, src, "cusna_warm_up.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) return;
+  const std::string minb = compile_options_text();
+  const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false",
+                        "-default-device", "-DLIBCUSNA_BUILD", minb.c_str()};
+  N.compile(prog, (int)(sizeof opts / sizeof opts[0]), opts);
+  N.destroy(&prog);
 }
 
 // At process exit: drop queued compilations and wait for the one in flight,
@@ -702,9 +728,9 @@ bool jit_get(const std::string &spec, JitKernel *out, bool now) {
         R.queue.emplace_back(spec, E);
         if (!R.worker) {
           R.worker = true;
-          // the compiler library is loaded first, so this handler runs before
-          // its static destructors at exit (handlers run in reverse order)
-          (void)nvrtc();
+          // the compiler library is loaded and has compiled once first, so
+          // this handler runs before its static destructors at exit
+          warm_up_compiler();
           std::atexit(stop_worker_at_exit);
           std::thread(worker_loop).detach();
         }

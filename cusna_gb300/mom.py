@@ -413,6 +413,53 @@ def mom_run(est: Estimator, theta0=None, engine=None, verbose=False, return_nets
                   int(n_sims), time.perf_counter() - t0, backend, s.nets, s.z_ends, times)
 
 
+def native_problems(est: Estimator):
+    """The periods as the C estimator takes them: one marshalled problem per
+    period (host arrays; M, seed, theta and lam are placeholders the estimator
+    overwrites)."""
+    if est.kb or est.coevol or any(d["inp"].nrate for d in est.per):
+        raise ValueError("cusna_mom_estimate fits network effects only (no behaviour or rate effects)")
+    return [marshal_period(d["inp"], 1, 1, 1.0, np.zeros(est.k)) for d in est.per]
+
+
+def mom_run_native(est: Estimator, theta0=None, use_graph: bool = True) -> MomFit:
+    """The Robbins-Monro fit through the library's C entry point
+    cusna_mom_estimate (the same phases as mom_run, run in C++ over replayable
+    plans, with no Python between rounds). Network-effect models only."""
+    import ctypes as C
+    from . import abi
+    lib = abi.load_library()
+    ms = native_problems(est)
+    probs = (abi.SaomProblem * est.P)(*[m.problem for m in ms])
+    ctl = est.control
+    n2 = np.ascontiguousarray(ctl["n2"], dtype=np.int32)
+    rc = np.ascontiguousarray(est.rate_consts, dtype=np.float64)
+    tg = np.ascontiguousarray(est.targets, dtype=np.float64)
+    o = abi.MomOptions(struct_version=abi.ABI_VERSION, conditional=int(est.conditional),
+                       firstg=float(ctl["firstg"]), nsub=int(ctl["nsub"]), n2=n2.ctypes.data,
+                       batch2=int(ctl["batch2"]), n1=int(ctl["n1"]), nD=int(ctl["nD"]),
+                       n3=int(ctl["n3"]), diagonalize=float(ctl["diagonalize"]) or -1.0,
+                       seed=int(ctl["seed"]) or 1234, rate_consts=rc.ctypes.data,
+                       use_graph=1 if use_graph else -1)
+    p, P = est.p, est.P
+    out = {x: np.zeros(p) for x in ("theta", "se", "tconv", "sim_means")}
+    out["D"], out["msf"] = np.zeros((p, p)), np.zeros((p, p))
+    out["rate_est"], out["rate_sd"] = np.zeros(P), np.zeros(P)
+    if theta0 is not None:
+        out["theta"][:] = theta0
+    r = abi.MomResult(struct_version=abi.ABI_VERSION, use_start=int(theta0 is not None),
+                      **{x: a.ctypes.data for x, a in out.items()})
+    st = lib.cusna_mom_estimate(probs, P, tg.ctypes.data, p, C.byref(o), C.byref(r))
+    if st != 0:
+        raise RuntimeError(f"cusna_mom_estimate failed ({st}): {lib.cusna_last_error().decode()}")
+    times = dict(zip(("phase1", "phase2", "phase3"), r.phase_seconds))
+    return MomFit(out["theta"], out["se"], out["tconv"], float(r.tconv_max), est.param_names,
+                  est.targets, out["sim_means"], out["D"], out["msf"], est.conditional,
+                  out["rate_est"] if est.conditional else None,
+                  out["rate_sd"] if est.conditional else None, int(r.n_sims),
+                  float(r.wall_seconds), "gpu-native", phase_times=times)
+
+
 def mom_control(firstg=0.4, nsub=4, n2=(40, 40, 60, 80), batch2=256, n1=1000, n3=4000,
                 nD=1000, diagonalize=0.2, seed=1234) -> dict:
     """Control settings (R/estimate.R:21-28)."""

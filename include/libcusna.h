@@ -354,6 +354,68 @@ CUSNA_API cusna_status cusna_saom_plan_shape(const cusna_saom_plan *plan,
 /* Waits for the device, then frees the plan and its device memory. */
 CUSNA_API void cusna_saom_plan_destroy(cusna_saom_plan *plan);
 
+/* ---- Method-of-Moments estimator (src/libcusna.h:532-542 reserves the opaque
+ * cusna_mom_options / cusna_mom_result for it; this defines them) ------------
+ * The Robbins-Monro MoM fit of R/mom.R:129-269 (phases 1-3: derivative,
+ * diagonalised inverse, guarded steps, averaged phase-2 iterates, phase-3
+ * standard errors and convergence t-ratios) in C++ over replayable plans:
+ * every period (or group-period) of the model is prepared once on the device,
+ * and each round only rewrites the parameters and replays the plan's CUDA
+ * graph; the phase-2 rounds ask for the statistics alone (no score sums).
+ *
+ * periods[0..P): one cusna_saom_problem per period as the glue fills it for
+ * the CPU engine (host pointers; x0/sim start networks, descriptors,
+ * conditional and target_dist). Their M, seed, theta and lam are ignored (the
+ * estimator sets them). Network effects only: kb and nrate must be 0.
+ * targets[0..p): the observed moments in the estimator's layout
+ * (R/targets.R:99-126): unconditional p = P + k, the P observed distances then
+ * the k effect statistics summed over periods; conditional p = k.
+ * result->theta[0..p): the start when use_start is set (else the reference's
+ * default start, R/mom.R:199-211: rates 1.5 d/n + 1, density -1, others 0);
+ * the estimate on return. The other output arrays may be NULL.
+ * Every option left 0 takes the reference's default (mom_control(),
+ * R/estimate.R:21-28), so a zeroed struct is the reference's control;
+ * diagonalize < 0 asks for weight 0 (no diagonalisation). */
+typedef struct cusna_mom_options {
+    int32_t  struct_version;  /* CUSNA_ABI_VERSION                             */
+    int32_t  conditional;     /* 1: conditional MoM (periods stop at target_dist) */
+    double   firstg;          /* initial gain (0: 0.4)                          */
+    int32_t  nsub;            /* phase-2 subphases (0: 4)                       */
+    const int32_t *n2;        /* [nsub] iterations per subphase (NULL: 40, 40, 60, 80, then 80) */
+    int32_t  batch2;          /* chains per phase-2 iteration (0: 256)          */
+    int32_t  n1;              /* phase-1 chains (0: 1000)                       */
+    int32_t  nD;              /* chains per subphase derivative (0: 1000)       */
+    int32_t  n3;              /* phase-3 chains (0: 4000)                       */
+    double   diagonalize;     /* weight of diag(D) in the inverse (0: 0.2; < 0: weight 0, the full D) */
+    uint64_t seed;            /* seeds of the periods' Philox streams (0: 1234) */
+    const double *rate_consts;/* [opt] P constants added to the distance statistics
+                                 (composition changes, R/mom.R:160)           */
+    int32_t  use_graph;       /* 1 (default, 0 = 1): replay rounds from CUDA graphs; -1 plain launches */
+    int32_t  verbose;         /* 1: the estimate after each phase on stderr (R/mom.R:230, :245-246) */
+} cusna_mom_options;
+
+typedef struct cusna_mom_result {
+    int32_t  struct_version;
+    int32_t  use_start;       /* in: 1 = start from theta                       */
+    double  *theta;           /* [p] in/out                                     */
+    double  *se;              /* [opt] [p] standard errors                      */
+    double  *tconv;           /* [opt] [p] convergence t-ratios                 */
+    double  *sim_means;       /* [opt] [p] phase-3 simulated means              */
+    double  *D;               /* [opt] [p*p] phase-3 score-function derivative  */
+    double  *msf;             /* [opt] [p*p] phase-3 covariance of the statistics */
+    double  *rate_est;        /* [opt] [P] conditional: mean simulated time per period */
+    double  *rate_sd;         /* [opt] [P] conditional: its standard deviation  */
+    double   tconv_max;       /* out: overall maximum convergence ratio         */
+    int64_t  n_sims;          /* out: chains simulated per period               */
+    double   wall_seconds;    /* out                                            */
+    double   phase_seconds[3];/* out: phases 1, 2, 3                            */
+} cusna_mom_result;
+
+CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *periods, int32_t P,
+                                          const double *targets, int32_t p,
+                                          const cusna_mom_options *opts,
+                                          cusna_mom_result *result);
+
 /* ---- multi-network co-evolution (src/libcusna.h:219-291) --------------------
  * D one-mode networks (2..CUSNA_MAXNET) on one actor set. Each ministep picks a
  * network with probability proportional to its rate, then one actor of it
