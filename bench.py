@@ -540,14 +540,18 @@ def c4_throughput(args, torch, dev, stream):
     return res
 
 
-def batching_comparison(full_fit=False):
+def batching_comparison(full_fit=False, restart=False):
     """One Robbins-Monro round of the uneven multi-group workload (512 groups,
     n ~ U{20..400}, 2 periods each: 1024 problems, one chain each): through
     one-shot batch calls that marshal and upload every problem each round,
     through a replayable plan (prepared once; a round writes theta and launches),
     and through the same plan replayed from a CUDA graph. Host wall clock per
     round, median of 5 after one warm-up round. With full_fit, the joint
-    conditional MoM fit through the graph-replayed plans as well."""
+    conditional MoM fit through the graph-replayed plans as well; with
+    restart, a second fit started from the first fit's estimate with 16
+    chains per unit in each phase-2 round (the schedule's noise and the
+    distance of the default start, not the simulator, hold the first fit's
+    t-ratios above 0.1)."""
     from cusna_gb300 import data as D
     from cusna_gb300 import mom
     eng = mom.GpuEngine()
@@ -592,6 +596,16 @@ def batching_comparison(full_fit=False):
                       "theta": fit.theta.tolist(), "se": fit.se.tolist(),
                       "tconv": fit.tconv.tolist(),
                       "control": {"n1": 50, "nD": 50, "batch2": 1, "n3": 500}}
+        if restart:
+            est.control = dict(ctl, batch2=16)
+            fit2 = mom.mom_run(est, theta0=fit.theta, engine=eng)
+            note(f"c3: restart fit {fit2.wall_time:.1f} s")
+            out["fit_restart"] = {
+                "wall_s": fit2.wall_time, "phase_times_s": fit2.phase_times,
+                "theta": fit2.theta.tolist(), "se": fit2.se.tolist(),
+                "tconv": fit2.tconv.tolist(),
+                "start": "the first fit's estimate",
+                "control": {"n1": 50, "nD": 50, "batch2": 16, "n3": 500}}
         eng.close()
     return out
 
@@ -747,6 +761,9 @@ def main():
                     help="skip the multi-group round timing (batch calls vs replayed plans)")
     ap.add_argument("--no-c3-fit", action="store_true",
                     help="skip the joint conditional MoM fit of the 512-group workload")
+    ap.add_argument("--c3-restart", action="store_true",
+                    help="after the C3 fit, a second fit from its estimate with 16 chains per "
+                         "unit in each phase-2 round (about 90 s more)")
     ap.add_argument("--no-c4", action="store_true",
                     help="skip the n=1000 co-evolution throughput line")
     ap.add_argument("--cold-fit", choices=["plain", "surrogate"], default=None,
@@ -881,7 +898,7 @@ def main():
     batching = None
     if not args.no_batching and ws == 1:
         try:
-            batching = batching_comparison(not args.no_c3_fit)
+            batching = batching_comparison(not args.no_c3_fit, args.c3_restart)
         except Exception as exc:   # the simulator line is reported regardless
             batching = {"error": f"{type(exc).__name__}: {exc}"}
 

@@ -643,6 +643,7 @@ CUSNA_API cusna_status cusna_mlp_train_steps(float *params, float *grad, float *
   a.B = batch; a.n_steps = n_steps; a.hyper = hyper; a.losses = losses; a.work = work;
   a.work_bytes = work_bytes; a.n_in = n_in; a.H = hidden; a.n_out = n_out;
   cudaStream_t st = (cudaStream_t)stream;
+  NvtxRange r("cusna_mlp_train_steps");
   return use_graph ? replay_train_graph(a, st) : train_steps_impl(a, st);
 }
 

@@ -532,6 +532,7 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
   Round R;
   // phase 1 (R/mom.R:224-229)
   double t0 = now_s();
+  std::unique_ptr<NvtxRange> range(new NvtxRange("mom phase 1"));
   if ((s = round(n1, true, R)) != CUSNA_OK) return s;
   {
     const Mat di = dinv_of(derivative(R, p), p, diag_w);
@@ -544,6 +545,8 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
   if (opts->verbose) print_theta("[phase 1]", theta);
   // phase 2 (R/mom.R:233-248)
   t0 = now_s();
+  range.reset();  // ranges nest: the old one ends before the next begins
+  range.reset(new NvtxRange("mom phase 2"));
   for (int sub = 0; sub < nsub; ++sub) {
     const double gain = firstg * std::pow(0.5, sub);
     if ((s = round(nD, true, R)) != CUSNA_OK) return s;
@@ -569,6 +572,8 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
   result->phase_seconds[1] = now_s() - t0;
   // phase 3 (R/mom.R:250-258)
   t0 = now_s();
+  range.reset();
+  range.reset(new NvtxRange("mom phase 3"));
   if ((s = round(n3, true, R)) != CUSNA_OK) return s;
   const Mat D = derivative(R, p);
   const Mat dinv = safe_solve(D, p);
@@ -594,6 +599,7 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
     for (int b = 0; b < p; ++b)
       for (int c = 0; c < p; ++c) cov[(size_t)a * p + b] += tmp[(size_t)a * p + c] * dinv[(size_t)b * p + c];
   result->phase_seconds[2] = now_s() - t0;
+  range.reset();
 
   for (int j = 0; j < p; ++j) {
     result->theta[j] = theta[j];

@@ -1560,6 +1560,7 @@ CUSNA_API cusna_status cusna_saom_simulate_period(const cusna_saom_problem *prob
                                                   cusna_saom_result *result) {
   g_err.clear();
   if (!problem || !result) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
+  NvtxRange r("cusna_saom_simulate_period");
   return simulate(problem, result, 1, nullptr);
 }
 
@@ -1568,6 +1569,7 @@ CUSNA_API cusna_status cusna_saom_simulate_period_ex(const cusna_saom_problem *p
                                                      cusna_gpu_options *opts) {
   g_err.clear();
   if (!problem || !result) { set_err("problem or result is NULL"); return CUSNA_ERR_NULL_ARG; }
+  NvtxRange r("cusna_saom_simulate_period_ex");
   return simulate(problem, result, 1, opts);
 }
 
@@ -1606,6 +1608,7 @@ CUSNA_API cusna_status cusna_saom_simulate_batch(const cusna_saom_problem *probl
                                                  cusna_saom_result *results, int32_t count,
                                                  cusna_gpu_options *opts) {
   g_err.clear();
+  NvtxRange r("cusna_saom_simulate_batch");
   return simulate(problems, results, count, opts);
 }
 
@@ -1668,6 +1671,7 @@ CUSNA_API cusna_status cusna_saom_specialise_wait(double seconds, int32_t *compi
 CUSNA_API cusna_status cusna_saom_simulate_multi(const cusna_saom_multi_problem *problem,
                                                  cusna_saom_multi_result *result) {
   g_err.clear();
+  NvtxRange r("cusna_saom_simulate_multi");
   return simulate_multi(problem, result);
 }
 
@@ -1675,12 +1679,14 @@ CUSNA_API cusna_status cusna_saom_plan_create(const cusna_saom_problem *problems
                                              cusna_saom_result *results, int32_t count,
                                              int32_t shared_params, cusna_saom_plan **plan) {
   g_err.clear();
+  NvtxRange r("cusna_saom_plan_create");
   return plan_create(problems, results, count, shared_params, plan);
 }
 
 CUSNA_API cusna_status cusna_saom_plan_launch(cusna_saom_plan *plan, void *stream,
                                              int32_t use_graph) {
   g_err.clear();
+  NvtxRange r("cusna_saom_plan_launch");
   return plan_launch(plan, (cudaStream_t)stream, use_graph != 0);
 }
 

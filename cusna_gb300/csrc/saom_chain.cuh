@@ -308,13 +308,21 @@ __device__ __forceinline__ bool is_nan64(double x) {
 
 // The score sums are formed per alter group: the 32-alter blocks b (alter j
 // in block j >> 5, on lane j & 31) fall into nsb groups, block b into group
-// b mod nsb, with nsb fixed by n alone (a multiple of 4 with up to two blocks
-// per group, so a team of G warps, which takes groups g, g+G, ..., shares
-// them evenly for G up to 4, and up to nsb). A lane adds its alters of a group
-// in ascending block order into double-float accumulators, one warp reduction
-// per group follows, and the group records are combined in group order: every
-// sum's order depends on n and j only, never on the team size.
+// b mod nsb, with nsb fixed by n alone. A team of G warps takes groups g,
+// g+G, ...; each group costs one warp reduction, so small networks (up to 16
+// blocks) use few large groups (about four blocks each, at least two), and
+// larger ones a multiple of 4 with up to two blocks per group (shared evenly
+// by teams of up to 16 warps). A lane adds its alters of a group in ascending
+// block order into double-float accumulators, one warp reduction per group
+// follows, and the group records are combined in group order: every sum's
+// order depends on n and j only, never on the team size.
 __host__ __device__ __forceinline__ int lse_groups(int nb) {
+  // up to 16 blocks: about four blocks per group, at least two groups (so a
+  // team of two warps shares the pass); beyond: about two blocks per group
+  if (nb <= 16) {
+    const int g = (nb + 3) / 4;
+    return nb < 2 ? nb : (g < 2 ? 2 : g);
+  }
   const int g = 4 * ((nb + 7) / 8);
   return g < nb ? g : nb;
 }
@@ -326,10 +334,14 @@ __host__ __device__ __forceinline__ int lse_groups(int nb) {
 // change" alter). Every product is a Dekker product of the weight's pair with
 // d_e's pair, added with TwoSum, two quantities per instruction. LOMASK: bit
 // e set when d_e may have a double-float remainder (integer counts have none).
+// first (uniform over the warp): the accumulators are still zero, so the
+// products are stored as they are (what TwoSum onto zero would give, bit for
+// bit).
 template <int V, unsigned LOMASK>
 __device__ __forceinline__ void lse_accumulate(float2 (&H)[(V + 1) / 2], float2 (&L)[(V + 1) / 2],
                                                float wh, float wl, const float *d32,
-                                               const float *d32lo, bool weighted, int k) {
+                                               const float *d32lo, bool weighted, int k,
+                                               bool first) {
   const float2 w2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
 #pragma unroll
   for (int x = 0; x < (V + 1) / 2; ++x) {
@@ -348,7 +360,12 @@ __device__ __forceinline__ void lse_accumulate(float2 (&H)[(V + 1) / 2], float2 
           make_float2(la && ua ? d32lo[qa - 1] : 0.f, lb && ub ? d32lo[qb - 1] : 0.f);
       pl = __ffma2_rn(w2, dl2, pl);
     }
-    ff_add2(H[x], L[x], p, pl);
+    if (first) {
+      H[x] = p;
+      L[x] = pl;
+    } else {
+      ff_add2(H[x], L[x], p, pl);
+    }
   }
 }
 
@@ -366,27 +383,17 @@ __device__ __forceinline__ void lse_store(float *rec, float (&h)[V], float (&l)[
   }
 }
 
-// The group records combined by one warp of the team: lane l adds groups l,
-// l+32, ... in order (double-float), then the fixed warp reduction adds the
-// lanes' partial sums. Quantity q lands in S.red[32G + q] as a double, past
-// the warp slots the team reductions use.
-template <int V>
+// The group records combined by one warp of the team: lane q adds quantity
+// q's records in group order (double-float). Quantity q lands in
+// S.red[32G + q] as a double, past the warp slots the team reductions use.
 __device__ __forceinline__ void combine_groups(const Team &T, const Slice &S, int nsb, int k) {
-  float h[V], l[V];
-#pragma unroll
-  for (int q = 0; q < V; ++q) {
-    h[q] = 0.f;
-    l[q] = 0.f;
-  }
-  for (int b = T.lane; b < nsb; b += 32) {
-    const float *rec = S.blk + (size_t)b * 2 * (k + 1);
-#pragma unroll
-    for (int q = 0; q < V; ++q)
-      if (q <= k) ff_add(h[q], l[q], rec[2 * q], rec[2 * q + 1]);
-  }
-  bool writer;
-  const int q = warp_multi_sum_ff<V>(h, l, T.lane, &writer);
-  if (writer && q <= k) S.red[32 * T.G + q] = __dadd_rn((double)h[0], (double)l[0]);
+  const int q = T.lane;
+  if (q > k) return;
+  const float *rec = S.blk + 2 * q;
+  const size_t stride = 2 * (size_t)(k + 1);
+  float h = rec[0], l = rec[1];
+  for (int g = 1; g < nsb; ++g) ff_add(h, l, rec[g * stride], rec[g * stride + 1]);
+  S.red[32 * T.G + q] = __dadd_rn((double)h, (double)l);
 }
 
 // The float64 predictor f_j of alter j (and its change statistics in d): the
@@ -479,6 +486,14 @@ static __device__ __noinline__ void lse_float64(const Team &T, const DevProblem 
 #define CUSNA_LSE_LOMASK 0xFFFFFFFFu
 #endif
 
+// Per-thread scratch of one alter's change statistics in the pass over the
+// alters: the model's k in the specialised build, the capacity otherwise.
+#if defined(CUSNA_JIT_K)
+constexpr int kScratchK = CUSNA_JIT_K;
+#else
+constexpr int kScratchK = kMaxEff;
+#endif
+
 // The pass over the alters of one network ministep (see net_choice): per
 // alter the change statistics, the float32 Gumbel key with its error bound
 // (into *best and S.gbuf), the permitted-alter bits (S.okbits) and, when the
@@ -489,8 +504,7 @@ static __device__ __noinline__ void lse_float64(const Team &T, const DevProblem 
 template <bool MULTI, bool VALID, int V>
 __device__ __forceinline__ bool alter_pass(const Team &T, const DevProblem &P, const Slice &S,
                                            const StepCtx &X, long long ms, uint32_t chain,
-                                           float *d32, float *d32lo, KeyTop &best, bool fast_sums,
-                                           int net) {
+                                           KeyTop &best, bool fast_sums, int net) {
   const int n = P.n, k = P.k, i = X.i;
   (void)net;
   const float ecoef = (float)(k + 10) * 5.9604644775390625e-8f;
@@ -512,6 +526,10 @@ __device__ __forceinline__ bool alter_pass(const Team &T, const DevProblem &P, c
     }
     for (int b = g; b < nb; b += ng) {
       const int j = (b << 5) + T.lane;
+      // the alter's float32 change statistics and their double-float
+      // remainders: in the specialised build every index is a constant, so
+      // these stay in registers
+      float d32[kScratchK], d32lo[kScratchK];
       bool ok = false, stay = false;
       float f = 0.f;
       float2 fx = make_float2(0.f, 0.f);
@@ -545,9 +563,13 @@ __device__ __forceinline__ bool alter_pass(const Team &T, const DevProblem &P, c
       }
       const uint32_t okb = __ballot_sync(kFull, ok);
       if (T.lane == 0) S.okbits[b] = okb;
-      if (fast_sums && ok) {
-        float wh = 1.f, wl = 0.f;  // the "no change" alter: exp(0)
-        if (!stay) {
+      // the group's first block initialises every lane's accumulators (a lane
+      // without a permitted alter there stores zeros); later blocks add the
+      // permitted alters
+      const bool first = b == g;
+      if (fast_sums && (ok || first)) {
+        float wh = ok ? 1.f : 0.f, wl = 0.f;  // the "no change" alter: exp(0)
+        if (ok && !stay) {
           if (fabsf(f) <= kFFExpMax) {
             exp_ff(fx.x, fx.y, S.etab, wh, wl);
           } else {  // also NaN
@@ -555,7 +577,7 @@ __device__ __forceinline__ bool alter_pass(const Team &T, const DevProblem &P, c
             wh = 0.f;
           }
         }
-        lse_accumulate<V, CUSNA_LSE_LOMASK>(AH, AL, wh, wl, d32, d32lo, !stay, KS);
+        lse_accumulate<V, CUSNA_LSE_LOMASK>(AH, AL, wh, wl, d32, d32lo, ok && !stay, KS, first);
       }
     }
     if (fast_sums) {
@@ -575,15 +597,15 @@ __device__ __forceinline__ bool alter_pass(const Team &T, const DevProblem &P, c
 // choice: change statistics, float32 keys and the double-float score sums, the
 // certified or exact float64 choice, and the chosen alter's float64 change
 // statistics in S.dstar. Returns j*. The score sums are left in S.red[32G + q]
-// (float64) for the score update. d (float64), d32 and d32lo are per-thread
-// scratch of k values.
+// (float64) for the score update. d (float64) is per-thread scratch of k
+// values.
 // MULTI: the network is one of a multi-network problem's, whose network w has
 // its rows at rows0 + w*net_stride words (cross effects read them).
 // VALID: validation mode (caller-supplied words in place of Philox).
 template <bool MULTI, bool VALID = false>
 __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, const Slice &S,
                                           int i, long long ms, uint32_t chain, double *d,
-                                          float *d32, float *d32lo, const uint32_t *rows0 = nullptr,
+                                          const uint32_t *rows0 = nullptr,
                                           size_t net_stride = 0, int net = 0) {
   const int n = P.n, W = P.W, k = P.k, L = T.L;
   (void)net;
@@ -626,16 +648,16 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
   const bool want_sums = (P.flags & F_NO_SCORES) == 0;
   const bool fast_sums = want_sums && (P.flags & F_LSE64) == 0;
 #ifdef CUSNA_LSE_V
-  const bool wide = alter_pass<MULTI, VALID, CUSNA_LSE_V>(T, P, S, X, ms, chain, d32, d32lo, best,
+  const bool wide = alter_pass<MULTI, VALID, CUSNA_LSE_V>(T, P, S, X, ms, chain, best,
                                                           fast_sums, net);
 #else
   bool wide;
   if (k + 1 <= 8)
-    wide = alter_pass<MULTI, VALID, 8>(T, P, S, X, ms, chain, d32, d32lo, best, fast_sums, net);
+    wide = alter_pass<MULTI, VALID, 8>(T, P, S, X, ms, chain, best, fast_sums, net);
   else if (k + 1 <= 16)
-    wide = alter_pass<MULTI, VALID, 16>(T, P, S, X, ms, chain, d32, d32lo, best, fast_sums, net);
+    wide = alter_pass<MULTI, VALID, 16>(T, P, S, X, ms, chain, best, fast_sums, net);
   else
-    wide = alter_pass<MULTI, VALID, 32>(T, P, S, X, ms, chain, d32, d32lo, best, fast_sums, net);
+    wide = alter_pass<MULTI, VALID, 32>(T, P, S, X, ms, chain, best, fast_sums, net);
 #endif
   if (__any_sync(kFull, wide) && T.lane == 0) S.misc[12] = (int)ms;
   T.sync();
@@ -687,12 +709,10 @@ __device__ __forceinline__ int net_choice(const Team &T, const DevProblem &P, co
     const int owner_warp = (jstar % L) >> 5;
     if (T.warp == (T.G > 1 ? (owner_warp + 1) % T.G : 0)) {
       const int nsb = lse_groups((n + 31) >> 5);
-#ifdef CUSNA_LSE_V
-      combine_groups<CUSNA_LSE_V>(T, S, nsb, CUSNA_JIT_K);
+#ifdef CUSNA_JIT_K
+      combine_groups(T, S, nsb, CUSNA_JIT_K);
 #else
-      if (k + 1 <= 8) combine_groups<8>(T, S, nsb, k);
-      else if (k + 1 <= 16) combine_groups<16>(T, S, nsb, k);
-      else combine_groups<32>(T, S, nsb, k);
+      combine_groups(T, S, nsb, k);
 #endif
     }
   }
@@ -747,7 +767,6 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
   long long dist = 0, bdist = 0, ms = 0, msb = 0;
   double t = 0.0, rho = 0.0;
   double d[kMaxEff];
-  float d32[kMaxEff], d32lo[kMaxEff];
 
   for (;;) {
     int i;
@@ -799,7 +818,7 @@ static __device__ void run_chain(const Team &T, const DevProblem &P, const Slice
       continue;
     }
 
-    const int jstar = net_choice<false, VALID>(T, P, S, i, ms, chain, d, d32, d32lo);
+    const int jstar = net_choice<false, VALID>(T, P, S, i, ms, chain, d);
     const int aij_star = bit_of(S.rowsT, n, i, jstar);
     T.sync();
     if (!(P.flags & F_NO_SCORES) && T.tl < k) {

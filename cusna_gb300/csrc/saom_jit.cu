@@ -6,6 +6,7 @@
 #include <unistd.h>
 #include <sys/stat.h>
 #include <nvrtc.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <chrono>
@@ -524,6 +525,10 @@ Compiled compile_spec(const std::string &spec) {
     }
   }
   const auto t0 = std::chrono::steady_clock::now();
+  nvtxRangePushA("specialise: NVRTC compile");
+  struct PopRange {
+    ~PopRange() { nvtxRangePop(); }
+  } pop_range;
   nvrtcProgram prog = nullptr;
   if (N.create(&prog, src.c_str(), "cusna_period_jit.cu", kJitHeaderCount, kJitHeaderSources,
                kJitHeaderNames) != NVRTC_SUCCESS) {
@@ -706,9 +711,18 @@ bool jit_get(const std::string &spec, JitKernel *out, bool now) {
   Registry &R = reg();
   Entry *E = nullptr;
   bool compile_now = false;
+  // a loaded module belongs to the device (context) it was loaded on, so the
+  // registry holds one entry per device and plan; a second device compiles
+  // its own copy (from the on-disk cache when that is on)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
+  }
+  const std::string key = std::to_string(dev) + '\n' + spec;
   {
     std::lock_guard<std::mutex> lk(R.mu);
-    auto &slot = R.map[spec];
+    auto &slot = R.map[key];
     if (!slot) slot.reset(new Entry());
     E = slot.get();
     if (E->state == S_LOADED) {

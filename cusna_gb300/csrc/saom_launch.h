@@ -1,6 +1,7 @@
 // saom_launch.h -- launch wrappers shared by the kernels (saom_sim.cu) and the
 // host code (saom_api.cu).
 #pragma once
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "saom_common.cuh"
@@ -74,6 +75,15 @@ void note_launch();           // counts a launch made outside the wrappers here
 // least `bytes`; never lowers it (see saom_sim.cu).
 cudaError_t raise_dyn_smem(const void *func, size_t bytes);
 void set_last_error(const char *msg);  // text of cusna_last_error() for this thread
+
+// A named range on the calling thread's timeline for profilers (NVTX, header
+// only: without an attached tool each push and pop is a call that returns).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 cudaError_t launch_netstats(const uint8_t *a, int M, const StatDesc &D, double *out, int sms,
                             cudaStream_t st);
 cudaError_t launch_behstats(const int *z, int n, int M, int kb, const int *bty, const uint8_t *xnet,

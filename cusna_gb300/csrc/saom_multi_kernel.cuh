@@ -40,7 +40,6 @@ static __device__ void run_chain_multi(const Team &T, const DevProblem *nets, co
   long long ms = 0, msd[kMaxNet] = {};
   double t = 0.0;
   double dbuf[kMaxEff];
-  float d32[kMaxEff], d32lo[kMaxEff];
   const Slice S0 = multi_slice(base, lay, 0, cols_g, rows_g, cols_words);
   // network w's rows: rows0 + w*net_stride words (in shared memory the slices
   // follow one another; in global scratch each network has cols_words)
@@ -72,7 +71,7 @@ static __device__ void run_chain_multi(const Team &T, const DevProblem *nets, co
     const int d = S0.rnet[slot], i = S0.rfocal[slot];
     const DevProblem &P = nets[d];
     const Slice S = multi_slice(base, lay, d, cols_g, rows_g, cols_words);
-    const int jstar = net_choice<true>(T, P, S, i, ms, chain, dbuf, d32, d32lo, rows0, net_stride, d);
+    const int jstar = net_choice<true>(T, P, S, i, ms, chain, dbuf, rows0, net_stride, d);
     const int aij_star = bit_of(S.rowsT, n, i, jstar);
     T.sync();
     if (T.tl < P.k) {
