@@ -3,15 +3,17 @@
 //
 // Parameters live in one float32 buffer (the master copy Adam updates):
 //   [W1 (H x n_in) | b1 (H) | W2 (H x H) | b2 (H) | W3 (n_out x H) | b3 (n_out)]
-// Every matrix product runs on the tensor cores with bfloat16 operands and
-// float32 accumulation (mma.sync m16n8k16): weights are rounded to bfloat16
-// copies at the start of each call, activations are rounded when they feed the
-// next product, and everything else (pre-activations, losses, gradients of the
-// biases, Adam) stays float32. n_in and H must be multiples of 16; the output
-// layer is padded to 16 rows internally.
+// Every matrix product runs on the fifth-generation tensor cores (tcgen05.mma,
+// kind::f16) with bfloat16 operands and a float32 accumulator in tensor memory:
+// weights are rounded to bfloat16 copies at the start of each call,
+// activations are rounded when they feed the next product, and everything else
+// (pre-activations, losses, gradients of the biases, Adam) stays float32. n_in
+// and H must be multiples of 16; the output layer is padded to 16 rows
+// internally.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -24,8 +26,6 @@
 namespace cusna {
 namespace {
 
-constexpr int kTile = 64;   // CTA tile (M and N)
-constexpr int kPadK = 24;   // shared-memory row stride in bf16 (16 + 8 pad: no bank conflicts)
 
 enum Epi : int {
   EPI_STORE = 0,     // C (fp32) = acc
@@ -43,111 +43,283 @@ __device__ __forceinline__ float gelu_grad(float z) {
   return cdf + z * pdf;
 }
 
-__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16 *p) {
-  return *reinterpret_cast<const uint32_t *>(p);
+// ---- fifth-generation tensor cores (tcgen05) ---------------------------------
+// One CTA of 128 threads computes a 128 x BN tile of C = A . B^T: the operand
+// tiles are staged in shared memory in the canonical no-swizzle layout (8 x 16-
+// byte core matrices), one thread issues tcgen05.mma (kind::f16, bf16 inputs,
+// M = 128, N = BN, K = 16 per instruction) with the accumulator in tensor
+// memory, tcgen05.commit signals an mbarrier when a K chunk's products are done,
+// and the four warps read their 32 accumulator rows back with tcgen05.ld for
+// the epilogue. Either operand may be K-major (row r at ptr + r * ld, its K
+// elements contiguous) or MN-major (K row k at ptr + k * ld, the M or N
+// elements contiguous), so the backward products read the forward activations
+// and weights in place, with no transposed copies.
+
+constexpr int kBM = 128;        // rows of a CTA tile (the MMA's M)
+constexpr int kKC = 64;         // K elements per staged chunk (4 MMAs)
+constexpr int kStages = 6;      // shared-memory stages of K chunks
+constexpr int kAhead = 3;       // chunks in flight ahead of the one multiplied
+// Spare shared memory past the last stage: every core matrix an MMA of a
+// 128-row tile can address, with the leading and stride offsets either way
+// round, stays inside the allocation.
+constexpr int kSlack = 32 * 1024;
+constexpr long long kWaitLimit = 1ll << 22;   // mbarrier polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// C[M x N] = A[M x K] . B[N x K]^T with bf16 A, B (row-major, leading dims lda,
-// ldb in elements, both multiples of 8) and fp32 accumulation on the tensor
-// cores. Requirements (checked by the host): K % 16 == 0. M and N are bounded by
-// predicated loads and stores. 128 threads: four warps, each a 32 x 32 sub-tile.
-template <int EPI>
-__global__ void __launch_bounds__(128) gemm_bf16_tc(
-    const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__restrict__ B, int ldb,
-    int M, int N, int K, const float *__restrict__ bias, const float *__restrict__ Zin,
-    float *__restrict__ Cf, __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Zout, int ldc) {
-  __shared__ __align__(16) __nv_bfloat16 As[kTile][kPadK];
-  __shared__ __align__(16) __nv_bfloat16 Bs[kTile][kPadK];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 1, wn = warp & 1, g = lane >> 2, t4 = lane & 3;
-  const int bm = blockIdx.y * kTile, bn = blockIdx.x * kTile;
-  float acc[2][4][4];
-#pragma unroll
-  for (int a = 0; a < 2; ++a)
-#pragma unroll
-    for (int b = 0; b < 4; ++b)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-  const int lrow = tid >> 1, lcol = (tid & 1) * 8;
-  for (int k0 = 0; k0 < K; k0 += 16) {
-    uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
-    if (bm + lrow < M) va = *reinterpret_cast<const uint4 *>(A + (size_t)(bm + lrow) * lda + k0 + lcol);
-    if (bn + lrow < N) vb = *reinterpret_cast<const uint4 *>(B + (size_t)(bn + lrow) * ldb + k0 + lcol);
-    *reinterpret_cast<uint4 *>(&As[lrow][lcol]) = va;
-    *reinterpret_cast<uint4 *>(&Bs[lrow][lcol]) = vb;
-    __syncthreads();
-    uint32_t af[2][4], bf[4][2];
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi) {
-      const int r = wm * 32 + mi * 16 + g;
-      af[mi][0] = ld_pair(&As[r][2 * t4]);
-      af[mi][1] = ld_pair(&As[r + 8][2 * t4]);
-      af[mi][2] = ld_pair(&As[r][2 * t4 + 8]);
-      af[mi][3] = ld_pair(&As[r + 8][2 * t4 + 8]);
-    }
-#pragma unroll
-    for (int ni = 0; ni < 4; ++ni) {
-      const int c = wn * 32 + ni * 8 + g;
-      bf[ni][0] = ld_pair(&Bs[c][2 * t4]);
-      bf[ni][1] = ld_pair(&Bs[c][2 * t4 + 8]);
-    }
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-      for (int ni = 0; ni < 4; ++ni) {
-        float *d = acc[mi][ni];
-        asm volatile(
-            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-            "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-            : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-            : "r"(af[mi][0]), "r"(af[mi][1]), "r"(af[mi][2]), "r"(af[mi][3]), "r"(bf[ni][0]),
-              "r"(bf[ni][1]));
+// Shared-memory matrix descriptor, no swizzle: start address, the byte offset
+// between core matrices adjacent in K (leading) and in M or N (stride), and
+// the fixed 0b001 at bits 46-48.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: f32 accumulator (bits 4-5 = 1), bf16 A
+// and B (bits 7-9, 10-12 = 1), A and B major-ness (bits 15, 16: 1 = MN-major),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+__device__ __forceinline__ uint32_t mma_idesc(int M, int N, bool a_mn, bool b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) |
+         ((b_mn ? 1u : 0u) << 16) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the mbarrier's phase of the given parity; false after kWaitLimit
+// polls (the caller records the failure and stops issuing work).
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (long long it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(mbar, parity)) return true;
+  return false;
+}
+
+// Issues the asynchronous copies of rows [r0, r0 + R) x K chunk [k0, k0 + kKC)
+// of an operand into the core-matrix layout at dst (zero-filled outside rows <
+// nrows, k < K). K-major: core matrix (row group g, K group c) at (g * 8 + c) *
+// 128 bytes; MN-major: core matrix (K group c, row group g) at (c * R/8 + g) *
+// 128 bytes. Each copy moves a 16-byte piece (8 consecutive elements). Eight
+// consecutive lanes fill the eight rows of one core matrix (one 128-byte
+// shared-memory wavefront, no bank conflict), and the next eight lanes the
+// neighbouring 16 bytes of the same eight rows (whole 32-byte sectors).
+template <bool MN>
+__device__ __forceinline__ void stage_tile(const __nv_bfloat16 *__restrict__ src, int ld, int r0,
+                                           int nrows, int k0, int K, int R, uint32_t dst) {
+  const int pieces = R * (kKC / 8);
+  for (int p = threadIdx.x; p < pieces; p += blockDim.x) {
+    const __nv_bfloat16 *g = src;
+    uint32_t off, bytes = 0;
+    const int q = p & 7, v = p >> 3;   // row within the core matrix, core slot
+    if (!MN) {
+      const int c = v & 7, r = (v >> 3) * 8 + q, k = k0 + c * 8;
+      if (r0 + r < nrows && k < K) {
+        g = src + (size_t)(r0 + r) * ld + k;
+        bytes = 16;
       }
-    __syncthreads();
+      off = (uint32_t)(((r >> 3) * 8 + c) * 128 + q * 16);
+    } else {
+      const int ng = R / 8, gi = v % ng, kk = (v / ng) * 8 + q, k = k0 + kk, r = r0 + gi * 8;
+      if (k < K && r < nrows) {
+        g = src + (size_t)k * ld + r;
+        bytes = 16;
+      }
+      off = (uint32_t)(((kk >> 3) * ng + gi) * 128 + q * 16);
+    }
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst + off), "l"(g),
+                 "r"(bytes)
+                 : "memory");
   }
+}
+
+// Descriptor of the MMA step s (K elements 16 s .. 16 s + 15 of the chunk) of a
+// staged tile with R rows.
+template <bool MN>
+__device__ __forceinline__ uint64_t step_desc(uint32_t base, int R, int s) {
+  if (!MN) return smem_desc(base + (uint32_t)s * 256u, 128u, 1024u);
+  return smem_desc(base + (uint32_t)(s * R * 32), (uint32_t)(R * 16), 128u);
+}
+
+template <int EPI>
+__device__ __forceinline__ void epilogue_store(int m, int n, float v, int ldc,
+                                               const float *__restrict__ bias,
+                                               const float *__restrict__ Zin, float *__restrict__ Cf,
+                                               __nv_bfloat16 *__restrict__ Cb,
+                                               float *__restrict__ Zout) {
+  const size_t o = (size_t)m * ldc + n;
+  if (EPI == EPI_STORE) {
+    Cf[o] = v;
+  } else if (EPI == EPI_BIAS) {
+    Cf[o] = v + bias[n];
+  } else if (EPI == EPI_BIAS_GELU) {
+    v += bias[n];
+    Zout[o] = v;
+    Cb[o] = __float2bfloat16_rn(gelu(v));
+  } else {  // EPI_GELU_BWD
+    const float dz = v * gelu_grad(Zin[o]);
+    Cf[o] = dz;
+    Cb[o] = __float2bfloat16_rn(dz);
+  }
+}
+
+// C[M x N] = A[M x K] . B[N x K]^T (bf16 operands, fp32 accumulation), a CTA
+// per 128 x BN tile (BN = 16..256, a multiple of 16), 128 threads. The K
+// chunks stream through kStages shared-memory stages with cp.async: chunk c +
+// kStages - 1 is in flight while the tensor cores multiply chunk c. The host
+// checks K % 16 == 0, 16-byte aligned operand rows and BN. *err receives 1 if
+// an mbarrier wait gave up.
+template <int EPI, bool A_MN, bool B_MN>
+__global__ void __launch_bounds__(128) gemm_tc05(
+    const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__restrict__ B, int ldb,
+    int M, int N, int K, int BN, const float *__restrict__ bias, const float *__restrict__ Zin,
+    float *__restrict__ Cf, __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Zout, int ldc,
+    int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char dsm[];
+  __shared__ __align__(8) unsigned long long mbar[kStages];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
+  const uint32_t a_bytes = kBM * kKC * 2, b_bytes = (uint32_t)BN * kKC * 2;
+  const uint32_t stage_bytes = a_bytes + b_bytes, sbase = smem_u32(dsm);
+  // tensor memory: a power of two of at least 32 columns, one f32 column per
+  // output column
+  uint32_t ncols = 32;
+  while ((int)ncols < BN) ncols <<= 1;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int q = 0; q < kStages; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[q])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = mma_idesc(kBM, BN, A_MN, B_MN);
+  const int nchunks = (K + kKC - 1) / kKC;
+  auto issue = [&](int c) {
+    const uint32_t sa = sbase + (uint32_t)(c % kStages) * stage_bytes;
+    stage_tile<A_MN>(A, lda, m0, M, c * kKC, K, kBM, sa);
+    stage_tile<B_MN>(B, ldb, n0, N, c * kKC, K, BN, sa + a_bytes);
+  };
+  // the first kAhead chunks in flight
+  for (int c = 0; c < kAhead; ++c) {
+    if (c < nchunks) issue(c);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  bool ok = true;
+  for (int c = 0; c < nchunks; ++c) {
+    // chunk c has landed (this thread's copies), then everyone's
+    asm volatile("cp.async.wait_group %0;" ::"n"(kAhead - 1) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = sbase + (uint32_t)(c % kStages) * stage_bytes, sb = sa + a_bytes;
+      const int steps = (K - c * kKC) >= kKC ? 4 : (K - c * kKC) / 16;
+      for (int s = 0; s < steps; ++s) {
+        const uint64_t da = step_desc<A_MN>(sa, kBM, s);
+        const uint64_t db = step_desc<B_MN>(sb, BN, s);
+        const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&mbar[c % kStages]))
+          : "memory");
+    }
+    // chunk c + kAhead goes to the stage of chunk c + kAhead - kStages, whose
+    // products were issued kStages - kAhead chunks ago
+    const int nc = c + kAhead, old = nc - kStages;
+    if (nc < nchunks) {
+      if (old >= 0 && ok)
+        ok = mbar_wait(smem_u32(&mbar[old % kStages]), (uint32_t)((old / kStages) & 1));
+      if (ok) issue(nc);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  // the last chunk's commit follows every earlier product
+  if (ok && nchunks > 0)
+    ok = mbar_wait(smem_u32(&mbar[(nchunks - 1) % kStages]),
+                   (uint32_t)(((nchunks - 1) / kStages) & 1));
+  ok = __syncthreads_and(ok) != 0;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (!ok) {
+    if (lane == 0) atomicExch(err, 1);
+  } else {
+    // accumulator rows to the warp's 32 x 33 staging area in shared memory (the
+    // stages are free now), then out a row at a time, lane = column
+    float *stg = reinterpret_cast<float *>(dsm) + warp * 32 * 33;
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      const int w = BN - c0 >= 32 ? 32 : 16;   // columns in this pass
+      for (int h = 0; h < w; h += 16) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c0 + h);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+            "%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+              "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int mi = 0; mi < 2; ++mi)
+        for (int j = 0; j < 16; ++j) stg[lane * 33 + h + j] = __uint_as_float(r[j]);
+      }
+      __syncwarp();
+      const int n = n0 + c0 + lane;
+      if (EPI == EPI_GELU_BWD) {
+        // the 32 rows' pre-activations loaded together (independent loads)
+        float z[32];
 #pragma unroll
-    for (int ni = 0; ni < 4; ++ni)
+        for (int rr = 0; rr < 32; ++rr) {
+          const int m = m0 + warp * 32 + rr;
+          z[rr] = (m < M && lane < w && n < N) ? Zin[(size_t)m * ldc + n] : 0.f;
+        }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int r = bm + wm * 32 + mi * 16 + g + (q >= 2 ? 8 : 0);
-        const int c = bn + wn * 32 + ni * 8 + 2 * t4 + (q & 1);
-        if (r >= M || c >= N) continue;
-        const size_t o = (size_t)r * ldc + c;
-        float v = acc[mi][ni][q];
-        if (EPI == EPI_STORE) {
-          Cf[o] = v;
-        } else if (EPI == EPI_BIAS) {
-          Cf[o] = v + bias[c];
-        } else if (EPI == EPI_BIAS_GELU) {
-          v += bias[c];
-          Zout[o] = v;
-          const float h = gelu(v);
-          Cb[o] = __float2bfloat16_rn(h);
-        } else {  // EPI_GELU_BWD
-          const float dz = v * gelu_grad(Zin[o]);
-          Cf[o] = dz;
-          Cb[o] = __float2bfloat16_rn(dz);
+        for (int rr = 0; rr < 32; ++rr) {
+          const int m = m0 + warp * 32 + rr;
+          if (m >= M || lane >= w || n >= N) continue;
+          const float dz = stg[rr * 33 + lane] * gelu_grad(z[rr]);
+          Cf[(size_t)m * ldc + n] = dz;
+          Cb[(size_t)m * ldc + n] = __float2bfloat16_rn(dz);
+        }
+      } else {
+        for (int rr = 0; rr < 32; ++rr) {
+          const int m = m0 + warp * 32 + rr;
+          if (m >= M || lane >= w || n >= N) continue;
+          epilogue_store<EPI>(m, n, stg[rr * 33 + lane], ldc, bias, Zin, Cf, Cb, Zout);
         }
       }
-}
-
-// out (cols x rows, bf16) = transpose of in (rows x cols); in may be fp32 or bf16.
-template <class T>
-__global__ void transpose_bf16(const T *__restrict__ in, int rows, int cols, int ldi,
-                               __nv_bfloat16 *__restrict__ out, int ldo) {
-  __shared__ float tile[32][33];
-  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int r = by + y, c = bx + threadIdx.x;
-    tile[y][threadIdx.x] = (r < rows && c < cols) ? (float)in[(size_t)r * ldi + c] : 0.f;
+      __syncwarp();
+    }
   }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int c = bx + y, r = by + threadIdx.x;
-    if (c < cols && r < rows) out[(size_t)c * ldo + r] = __float2bfloat16_rn(tile[threadIdx.x][y]);
-  }
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols)
+                 : "memory");
 }
 
 __global__ void to_bf16(const float *__restrict__ in, size_t n, __nv_bfloat16 *__restrict__ out) {
@@ -245,17 +417,29 @@ __global__ void adam_bump(cusna_adam_hyper *h) {
   h->c2 = 1.f - powf(h->beta2, (float)step);
 }
 
+// Adam with the device-side bias corrections; with w1b non-null it also
+// writes the updated weights' bfloat16 copies (W1, W2 and the real rows of the
+// padded W3), so the next training step needs no separate refresh.
 __global__ void adam_step_dev(float *__restrict__ p, const float *__restrict__ g,
                               float *__restrict__ m, float *__restrict__ v, size_t n,
-                              const cusna_adam_hyper *__restrict__ h) {
+                              const cusna_adam_hyper *__restrict__ h,
+                              __nv_bfloat16 *__restrict__ w1b, __nv_bfloat16 *__restrict__ w2b,
+                              __nv_bfloat16 *__restrict__ w3b, int n_in, int H, int n_out) {
   const float lr = h->lr, b1 = h->beta1, b2 = h->beta2, eps = h->eps, c1 = h->c1, c2 = h->c2;
+  const size_t o2 = (size_t)H * n_in + H, o3 = o2 + (size_t)H * H + H;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.f - b1) * gi;
     const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
     m[i] = mi;
     v[i] = vi;
-    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    const float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    p[i] = pi;
+    if (w1b) {
+      if (i < (size_t)H * n_in) w1b[i] = __float2bfloat16_rn(pi);
+      else if (i >= o2 && i < o2 + (size_t)H * H) w2b[i - o2] = __float2bfloat16_rn(pi);
+      else if (i >= o3 && i < o3 + (size_t)n_out * H) w3b[i - o3] = __float2bfloat16_rn(pi);
+    }
   }
 }
 
@@ -302,12 +486,15 @@ __global__ void jacobian_fwd(const float *__restrict__ P, const float *__restric
 
 // ---- workspace layout ------------------------------------------------------
 struct Ws {
-  __nv_bfloat16 *w1b, *w2b, *w3b, *w2t, *w3t, *xb, *xt, *h1b, *h1t, *h2b, *h2t, *dyb, *dyt,
-      *dz2b, *dz2t, *dz1b, *dz1t;
+  __nv_bfloat16 *w1b, *w2b, *w3b, *xb, *h1b, *h2b, *dyb, *dz2b, *dz1b;
   float *z1, *z2, *y, *dy, *dz2, *dz1, *loss;
+  int *err;       // a tensor-core wait gave up
 };
 
 constexpr int kOutPad = 16;
+// N columns of a CTA tile: 64 for wide products (more CTAs share the
+// epilogue), else N rounded up to a multiple of 16
+int tile_n(int N) { return N >= 64 ? 64 : (N + 15) / 16 * 16; }
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -325,16 +512,13 @@ size_t ws_layout(int n_in, int H, int B, unsigned char *base, Ws *w) {
   Ws d{};
   Ws &x = w ? *w : d;
   bf(&x.w1b, (size_t)H * n_in); bf(&x.w2b, (size_t)H * H); bf(&x.w3b, (size_t)O * H);
-  bf(&x.w2t, (size_t)H * H); bf(&x.w3t, (size_t)H * O);
-  bf(&x.xb, (size_t)B * n_in); bf(&x.xt, (size_t)n_in * B);
-  bf(&x.h1b, (size_t)B * H); bf(&x.h1t, (size_t)H * B);
-  bf(&x.h2b, (size_t)B * H); bf(&x.h2t, (size_t)H * B);
-  bf(&x.dyb, (size_t)B * O); bf(&x.dyt, (size_t)O * B);
-  bf(&x.dz2b, (size_t)B * H); bf(&x.dz2t, (size_t)H * B);
-  bf(&x.dz1b, (size_t)B * H); bf(&x.dz1t, (size_t)H * B);
+  bf(&x.xb, (size_t)B * n_in); bf(&x.h1b, (size_t)B * H); bf(&x.h2b, (size_t)B * H);
+  bf(&x.dyb, (size_t)B * O); bf(&x.dz2b, (size_t)B * H); bf(&x.dz1b, (size_t)B * H);
   f32(&x.z1, (size_t)B * H); f32(&x.z2, (size_t)B * H); f32(&x.y, (size_t)B * O);
   f32(&x.dy, (size_t)B * O); f32(&x.dz2, (size_t)B * H); f32(&x.dz1, (size_t)B * H);
   f32(&x.loss, 4);
+  if (base) x.err = (int *)(base + off);
+  off = align256(off + 4);
   return off;
 }
 
@@ -343,20 +527,22 @@ int blocks_for(size_t n) {
   return (int)(b < 1 ? 1 : (b > 2048 ? 2048 : b));
 }
 
-template <int EPI>
+// C = A . B^T on the tensor cores (gemm_tc05); A_MN / B_MN: the operand is
+// MN-major (element (row, k) at ptr + k * ld + row).
+template <int EPI, bool A_MN, bool B_MN>
 cudaError_t gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N,
                  int K, const float *bias, const float *Zin, float *Cf, __nv_bfloat16 *Cb,
-                 float *Zout, int ldc, cudaStream_t st) {
-  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
-  gemm_bf16_tc<EPI><<<grid, 128, 0, st>>>(A, lda, B, ldb, M, N, K, bias, Zin, Cf, Cb, Zout, ldc);
-  return cudaGetLastError();
-}
-
-template <class T>
-cudaError_t transpose(const T *in, int rows, int cols, int ldi, __nv_bfloat16 *out, int ldo,
-                      cudaStream_t st) {
-  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
-  transpose_bf16<T><<<grid, block, 0, st>>>(in, rows, cols, ldi, out, ldo);
+                 float *Zout, int ldc, const Ws &w, cudaStream_t st) {
+  // the allocation has kSlack spare bytes past the stages
+  const int BN = tile_n(N);
+  const size_t smem =
+      (size_t)kStages * ((size_t)kBM * kKC * 2 + (size_t)BN * kKC * 2) + (size_t)kSlack;
+  const void *fn = (const void *)gemm_tc05<EPI, A_MN, B_MN>;
+  cudaError_t e = raise_dyn_smem(fn, smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((N + BN - 1) / BN, (M + kBM - 1) / kBM);
+  gemm_tc05<EPI, A_MN, B_MN><<<grid, 128, smem, st>>>(A, lda, B, ldb, M, N, K, BN, bias, Zin, Cf,
+                                                      Cb, Zout, ldc, w.err);
   return cudaGetLastError();
 }
 
@@ -390,15 +576,14 @@ cusna_status check_call(int n_in, int H, int n_out, int B, bool training, size_t
   return CUSNA_OK;
 }
 
-// bf16 weight copies (and the transposed W2, W3 the backward pass reads)
+// bf16 weight copies (W3 padded to 16 rows of zeros)
 cusna_status refresh_weights(const float *P, int n_in, int H, int n_out, const Ws &w, cudaStream_t st) {
   const float *W1 = P, *W2 = P + (size_t)H * n_in + H, *W3 = W2 + (size_t)H * H + H;
   to_bf16<<<blocks_for((size_t)H * n_in), 256, 0, st>>>(W1, (size_t)H * n_in, w.w1b);
   to_bf16<<<blocks_for((size_t)H * H), 256, 0, st>>>(W2, (size_t)H * H, w.w2b);
   pad_bf16<<<blocks_for((size_t)kOutPad * H), 256, 0, st>>>(W3, n_out, H, H, kOutPad, H, w.w3b);
   MCU(cudaGetLastError());
-  MCU(transpose(W2, H, H, H, w.w2t, H, st));
-  MCU(transpose(w.w3b, kOutPad, H, H, w.w3t, kOutPad, st));
+  MCU(cudaMemsetAsync(w.err, 0, sizeof(int), st));
   return CUSNA_OK;
 }
 
@@ -407,9 +592,12 @@ cusna_status forward(const float *P, const float *X, const int32_t *sel, int n_i
   const float *b1 = P + (size_t)H * n_in, *b2 = b1 + H + (size_t)H * H, *b3 = b2 + H + (size_t)n_out * H;
   gather_bf16<<<blocks_for((size_t)B * n_in), 256, 0, st>>>(X, sel, B, n_in, w.xb);
   MCU(cudaGetLastError());
-  MCU(gemm<EPI_BIAS_GELU>(w.xb, n_in, w.w1b, n_in, B, H, n_in, b1, nullptr, nullptr, w.h1b, w.z1, H, st));
-  MCU(gemm<EPI_BIAS_GELU>(w.h1b, H, w.w2b, H, B, H, H, b2, nullptr, nullptr, w.h2b, w.z2, H, st));
-  MCU(gemm<EPI_BIAS>(w.h2b, H, w.w3b, H, B, n_out, H, b3, nullptr, w.y, nullptr, nullptr, kOutPad, st));
+  MCU((gemm<EPI_BIAS_GELU, false, false>(w.xb, n_in, w.w1b, n_in, B, H, n_in, b1, nullptr, nullptr,
+                                         w.h1b, w.z1, H, w, st)));
+  MCU((gemm<EPI_BIAS_GELU, false, false>(w.h1b, H, w.w2b, H, B, H, H, b2, nullptr, nullptr,
+                                         w.h2b, w.z2, H, w, st)));
+  MCU((gemm<EPI_BIAS, false, false>(w.h2b, H, w.w3b, H, B, n_out, H, b3, nullptr, w.y, nullptr,
+                                    nullptr, kOutPad, w, st)));
   return CUSNA_OK;
 }
 
@@ -424,36 +612,38 @@ cusna_status backward(const float *T, const int32_t *sel, int n_in, int H, int n
   MCU(cudaMemsetAsync(w.loss, 0, sizeof(float), st));
   mse_grad<<<blocks_for((size_t)B * O), 256, 0, st>>>(w.y, O, T, sel, B, n_out, w.dy, w.dyb, w.loss);
   MCU(cudaGetLastError());
-  // layer 3: gW3 = dY^T H2 (n_out x H), dZ2 = (dY W3) * gelu'(Z2)
-  MCU(transpose(w.dyb, B, O, O, w.dyt, B, st));
-  MCU(transpose(w.h2b, B, H, H, w.h2t, B, st));
-  MCU(gemm<EPI_STORE>(w.dyt, B, w.h2t, B, n_out, H, B, nullptr, nullptr, gW3, nullptr, nullptr, H, st));
+  // layer 3: gW3 = dY^T H2 (n_out x H), dZ2 = (dY W3) * gelu'(Z2); the batch
+  // is the reduction dimension, so dY and H2 enter MN-major, as stored
+  MCU((gemm<EPI_STORE, true, true>(w.dyb, O, w.h2b, H, n_out, H, B, nullptr, nullptr, gW3, nullptr,
+                                   nullptr, H, w, st)));
   col_sum<<<(n_out + 31) / 32, cs, 0, st>>>(w.dy, B, n_out, O, gb3);
-  MCU(gemm<EPI_GELU_BWD>(w.dyb, O, w.w3t, O, B, H, O, nullptr, w.z2, w.dz2, w.dz2b, nullptr, H, st));
+  MCU((gemm<EPI_GELU_BWD, false, true>(w.dyb, O, w.w3b, H, B, H, O, nullptr, w.z2, w.dz2, w.dz2b,
+                                       nullptr, H, w, st)));
   // layer 2: gW2 = dZ2^T H1, dZ1 = (dZ2 W2) * gelu'(Z1)
-  MCU(transpose(w.dz2b, B, H, H, w.dz2t, B, st));
-  MCU(transpose(w.h1b, B, H, H, w.h1t, B, st));
-  MCU(gemm<EPI_STORE>(w.dz2t, B, w.h1t, B, H, H, B, nullptr, nullptr, gW2, nullptr, nullptr, H, st));
+  MCU((gemm<EPI_STORE, true, true>(w.dz2b, H, w.h1b, H, H, H, B, nullptr, nullptr, gW2, nullptr,
+                                   nullptr, H, w, st)));
   col_sum<<<(H + 31) / 32, cs, 0, st>>>(w.dz2, B, H, H, gb2);
-  MCU(gemm<EPI_GELU_BWD>(w.dz2b, H, w.w2t, H, B, H, H, nullptr, w.z1, w.dz1, w.dz1b, nullptr, H, st));
+  MCU((gemm<EPI_GELU_BWD, false, true>(w.dz2b, H, w.w2b, H, B, H, H, nullptr, w.z1, w.dz1, w.dz1b,
+                                       nullptr, H, w, st)));
   // layer 1: gW1 = dZ1^T X
-  MCU(transpose(w.dz1b, B, H, H, w.dz1t, B, st));
-  MCU(transpose(w.xb, B, n_in, n_in, w.xt, B, st));
-  MCU(gemm<EPI_STORE>(w.dz1t, B, w.xt, B, H, n_in, B, nullptr, nullptr, gW1, nullptr, nullptr, n_in, st));
+  MCU((gemm<EPI_STORE, true, true>(w.dz1b, H, w.xb, n_in, H, n_in, B, nullptr, nullptr, gW1,
+                                   nullptr, nullptr, n_in, w, st)));
   col_sum<<<(H + 31) / 32, cs, 0, st>>>(w.dz1, B, H, H, gb1);
   MCU(cudaGetLastError());
   return CUSNA_OK;
 }
 
+// refresh: make the bfloat16 weight copies from params first (false when the
+// previous training step's Adam already wrote them)
 cusna_status grad_impl(const float *params, const float *x, const float *t, const int32_t *sel,
                        int B, float *grad, float *loss, void *work, size_t work_bytes, int n_in,
-                       int H, int n_out, cudaStream_t st) {
+                       int H, int n_out, cudaStream_t st, bool refresh = true) {
   if (!params || !x || !t || !grad || !work) return CUSNA_ERR_NULL_ARG;
   cusna_status s = check_call(n_in, H, n_out, B, true, work_bytes);
   if (s != CUSNA_OK) return s;
   Ws w{};
   ws_layout(n_in, H, B, (unsigned char *)work, &w);
-  if ((s = refresh_weights(params, n_in, H, n_out, w, st)) != CUSNA_OK) return s;
+  if (refresh && (s = refresh_weights(params, n_in, H, n_out, w, st)) != CUSNA_OK) return s;
   if ((s = forward(params, x, sel, n_in, H, n_out, B, w, st)) != CUSNA_OK) return s;
   if ((s = backward(t, sel, n_in, H, n_out, B, grad, w, st)) != CUSNA_OK) return s;
   if (loss) MCU(cudaMemcpyAsync(loss, w.loss, sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -477,13 +667,16 @@ struct TrainArgs {
 // 0..B every step), then Adam with the device-side step counter.
 cusna_status train_steps_impl(const TrainArgs &a, cudaStream_t st) {
   const size_t n = (size_t)a.H * a.n_in + a.H + (size_t)a.H * a.H + a.H + (size_t)a.n_out * a.H + a.n_out;
+  Ws w{};
+  ws_layout(a.n_in, a.H, a.B, (unsigned char *)a.work, &w);
   for (int s = 0; s < a.n_steps; ++s) {
     cusna_status r = grad_impl(a.params, a.x, a.t, a.rows ? a.rows + (size_t)s * a.B : nullptr, a.B,
                                a.grad, a.losses ? a.losses + s : nullptr, a.work, a.work_bytes,
-                               a.n_in, a.H, a.n_out, st);
+                               a.n_in, a.H, a.n_out, st, s == 0);
     if (r != CUSNA_OK) return r;
     adam_bump<<<1, 1, 0, st>>>(a.hyper);
-    adam_step_dev<<<blocks_for(n), 256, 0, st>>>(a.params, a.grad, a.m, a.v, n, a.hyper);
+    adam_step_dev<<<blocks_for(n), 256, 0, st>>>(a.params, a.grad, a.m, a.v, n, a.hyper, w.w1b,
+                                                  w.w2b, w.w3b, a.n_in, a.H, a.n_out);
     MCU(cudaGetLastError());
   }
   return CUSNA_OK;

@@ -146,6 +146,34 @@ def test_gpu_gradient_matches_oracle(dims):
 
 
 @pytest.mark.gpu
+def test_gpu_gradient_with_split_k_matches_oracle_and_repeats_exactly():
+    """A batch of 1024 splits the K of the products whose reduction runs over
+    the batch (and of the 256-wide hidden products) across CTAs; the partial
+    tiles are added in a fixed order by the last CTA of each tile, so two calls
+    agree bit for bit, and the gradient matches the oracle's."""
+    n_in, hidden, n_out = 16, 256, 8
+    g = _Gpu(n_in, hidden, n_out)
+    B = 1024
+    p, X, T = _problem(seed=21, B=B, n_in=n_in, hidden=hidden, n_out=n_out)
+    w, nb = g.work(B)
+    grads = []
+    for _ in range(2):
+        grad = g.torch.zeros(len(p), device=g.dev)
+        st = g.lib.cusna_mlp_grad(g.t(p).data_ptr(), g.t(X).data_ptr(), g.t(T).data_ptr(), None,
+                                  B, grad.data_ptr(), None, w.data_ptr(), nb, n_in, hidden,
+                                  n_out, None)
+        assert st == 0
+        grads.append(grad.double().cpu().numpy())
+    np.testing.assert_array_equal(grads[0], grads[1])
+    _, g_bf = OM.loss_grad(p, X, T, n_in, hidden, n_out, bf16=True)
+    assert _rel(grads[0], g_bf) < 2e-3, _rel(grads[0], g_bf)
+    o = 0
+    for sz in (hidden * n_in, hidden, hidden * hidden, hidden, n_out * hidden, n_out):
+        assert _rel(grads[0][o:o + sz], g_bf[o:o + sz]) < 5e-3
+        o += sz
+
+
+@pytest.mark.gpu
 def test_gpu_gradient_with_row_selection():
     g = _Gpu()
     p, X, T = _problem(seed=5, B=96)
