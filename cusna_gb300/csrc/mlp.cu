@@ -113,29 +113,31 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
 // consecutive lanes fill the eight rows of one core matrix (one 128-byte
 // shared-memory wavefront, no bank conflict), and the next eight lanes the
 // neighbouring 16 bytes of the same eight rows (whole 32-byte sectors).
+// R is a power of two (lg_ng = log2(R / 8)), so every index is a shift.
 template <bool MN>
 __device__ __forceinline__ void stage_tile(const __nv_bfloat16 *__restrict__ src, int ld, int r0,
-                                           int nrows, int k0, int K, int R, uint32_t dst) {
-  const int pieces = R * (kKC / 8);
+                                           int nrows, int k0, int K, int lg_ng, uint32_t dst) {
+  const int pieces = 64 << lg_ng;   // R rows x kKC / 8 pieces
   for (int p = threadIdx.x; p < pieces; p += blockDim.x) {
     const __nv_bfloat16 *g = src;
-    uint32_t off, bytes = 0;
+    uint32_t bytes = 0;
     const int q = p & 7, v = p >> 3;   // row within the core matrix, core slot
     if (!MN) {
-      const int c = v & 7, r = (v >> 3) * 8 + q, k = k0 + c * 8;
+      const int c = v & 7, r = ((v >> 3) << 3) + q, k = k0 + (c << 3);
       if (r0 + r < nrows && k < K) {
         g = src + (size_t)(r0 + r) * ld + k;
         bytes = 16;
       }
-      off = (uint32_t)(((r >> 3) * 8 + c) * 128 + q * 16);
     } else {
-      const int ng = R / 8, gi = v % ng, kk = (v / ng) * 8 + q, k = k0 + kk, r = r0 + gi * 8;
+      const int gi = v & ((1 << lg_ng) - 1), kk = ((v >> lg_ng) << 3) + q, k = k0 + kk;
+      const int r = r0 + (gi << 3);
       if (k < K && r < nrows) {
         g = src + (size_t)k * ld + r;
         bytes = 16;
       }
-      off = (uint32_t)(((kk >> 3) * ng + gi) * 128 + q * 16);
     }
+    // both layouts: core slot v holds 128 bytes, its row q at q * 16
+    const uint32_t off = (uint32_t)((v << 7) + (q << 4));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst + off), "l"(g),
                  "r"(bytes)
                  : "memory");
@@ -173,7 +175,7 @@ __device__ __forceinline__ void epilogue_store(int m, int n, float v, int ldc,
 }
 
 // C[M x N] = A[M x K] . B[N x K]^T (bf16 operands, fp32 accumulation), a CTA
-// per 128 x BN tile (BN = 16..256, a multiple of 16), 128 threads. The K
+// per 128 x BN tile (BN = 16, 32 or 64), 128 threads. The K
 // chunks stream through kStages shared-memory stages with cp.async: chunk c +
 // kStages - 1 is in flight while the tensor cores multiply chunk c. The host
 // checks K % 16 == 0, 16-byte aligned operand rows and BN. *err receives 1 if
@@ -213,10 +215,11 @@ __global__ void __launch_bounds__(128) gemm_tc05(
   const uint32_t tmem = tmem_slot;
   const uint32_t idesc = mma_idesc(kBM, BN, A_MN, B_MN);
   const int nchunks = (K + kKC - 1) / kKC;
+  const int lg_nb = __ffs(BN >> 3) - 1;   // BN is a power of two
   auto issue = [&](int c) {
     const uint32_t sa = sbase + (uint32_t)(c % kStages) * stage_bytes;
-    stage_tile<A_MN>(A, lda, m0, M, c * kKC, K, kBM, sa);
-    stage_tile<B_MN>(B, ldb, n0, N, c * kKC, K, BN, sa + a_bytes);
+    stage_tile<A_MN>(A, lda, m0, M, c * kKC, K, 4, sa);   // 128 rows: 16 row groups
+    stage_tile<B_MN>(B, ldb, n0, N, c * kKC, K, lg_nb, sa + a_bytes);
   };
   // the first kAhead chunks in flight
   for (int c = 0; c < kAhead; ++c) {
@@ -493,8 +496,8 @@ struct Ws {
 
 constexpr int kOutPad = 16;
 // N columns of a CTA tile: 64 for wide products (more CTAs share the
-// epilogue), else N rounded up to a multiple of 16
-int tile_n(int N) { return N >= 64 ? 64 : (N + 15) / 16 * 16; }
+// epilogue), else N rounded up to a power of two of at least 16
+int tile_n(int N) { return N > 32 ? 64 : (N > 16 ? 32 : 16); }
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 

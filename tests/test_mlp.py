@@ -146,11 +146,11 @@ def test_gpu_gradient_matches_oracle(dims):
 
 
 @pytest.mark.gpu
-def test_gpu_gradient_with_split_k_matches_oracle_and_repeats_exactly():
-    """A batch of 1024 splits the K of the products whose reduction runs over
-    the batch (and of the 256-wide hidden products) across CTAs; the partial
-    tiles are added in a fixed order by the last CTA of each tile, so two calls
-    agree bit for bit, and the gradient matches the oracle's."""
+def test_gpu_gradient_at_batch_1024_matches_oracle_and_repeats_exactly():
+    """The surrogate's training batch (1024 rows, hidden width 256): the
+    weight-gradient products reduce over the whole batch (K = 1024, sixteen
+    chunks through the stage ring); the gradient matches the oracle's and two
+    calls agree bit for bit."""
     n_in, hidden, n_out = 16, 256, 8
     g = _Gpu(n_in, hidden, n_out)
     B = 1024
