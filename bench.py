@@ -95,20 +95,23 @@ def smem_bytes_per_network_ministep(n, W):
 
 # Warp-instructions the period kernel executes per network ministep, from ncu
 # captures of the bench's own launches (smsp__inst_executed.sum over the
-# launch's 6,557,430 network ministeps; n=200, k=8, 4096 chains, autotuned
-# shape): the kernel specialised to the effect plan and the library kernel;
-# and per ministep (network and behaviour, 6,146,609 a launch) of the n=1000
-# co-evolution workload's specialised kernel.
-INST_PER_MINISTEP = {("c2", True): 7704.0, ("c2", False): 14212.0, ("c4", True): 30523.0}
+# launch's 6,557,430 network ministeps; n=200, k=8, 4096 chains), keyed by
+# workload, kernel specialised to the effect plan, and warps per chain of the
+# tuned shape (one warp per chain: 41,552,184,346 per launch; two:
+# 45,901,908,023); and per ministep (network and behaviour, 6,146,609 a
+# launch) of the n=1000 co-evolution workload's specialised kernel (16 warps
+# per chain: 186,772,337,633 per launch; 8: 153,974,457,454).
+INST_PER_MINISTEP = {("c2", True, 1): 6337.0, ("c2", True, 2): 7000.0,
+                     ("c4", True, 16): 30387.0, ("c4", True, 8): 25050.0}
 # DRAM bytes of one period-kernel launch of the bench workload (the problem, its
 # tables and the outputs), measured by ncu on the bench's own timed launch
-# (dram__bytes_read.sum 2,669,056 + dram__bytes_write.sum 2,578,944 at 4096
-# chains, specialised kernel).
-DRAM_BYTES_PER_LAUNCH = {("c2", 4096): 2669056.0 + 2578944.0}
+# (dram__bytes_read.sum 4,728,832 + dram__bytes_write.sum 1,488,640 at 4096
+# chains, specialised kernel, one warp per chain).
+DRAM_BYTES_PER_LAUNCH = {("c2", 4096): 4728832.0 + 1488640.0}
 
 
 def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, specialised=True,
-                    chains=0):
+                    chains=0, warps_per_chain=0):
     """The period kernel is latency-bound: its state is on chip (DRAM moves only
     the problem and the outputs) and no pipe is busier than a quarter of its
     peak, so its ceiling is the SMs' instruction issue rate (4 warp-instructions
@@ -119,7 +122,8 @@ def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, spec
     mhz = (clk or {}).get("sm_mhz") or 2070.0
     hz = mhz * 1e6
     rate = net_steps / (kernel_ms / 1e3)
-    ipm = INST_PER_MINISTEP.get((workload, bool(specialised)))
+    ipm = INST_PER_MINISTEP.get((workload, bool(specialised), int(warps_per_chain)),
+                                INST_PER_MINISTEP.get((workload, bool(specialised))))
     peak = 4.0 * sm_count * hz / 1e9
     achieved = rate * ipm / 1e9 if ipm else None
     smem_peak = 128.0 * sm_count * hz / 1e12          # TB/s, 128 B per cycle per SM
@@ -521,7 +525,7 @@ def c4_throughput(args, torch, dev, stream):
     steps = int(G.simulate(m_h)["steps"].sum())
     rate = steps / (float(np.mean(kms)) / 1e3)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    ipm = INST_PER_MINISTEP.get(("c4", True)) if all(spec) else None
+    ipm = INST_PER_MINISTEP.get(("c4", True, int(shape[0]))) if all(spec) else None
     peak = 4.0 * sms * 2070e6 / 1e9
     res = {"workload": f"c4: {WORKLOADS['c4']}; M={M}", "metric": "ministeps/s",
            "unit": "ministeps/s", "value": rate,
@@ -941,7 +945,8 @@ def main():
     clk = clocks.summary(local)
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     roofline = period_roofline(args.workload, n, (n + 31) // 32, k, net_steps, kern_avg_ms, sm_count,
-                               clk, specialised=all(specialised), chains=M)
+                               clk, specialised=all(specialised), chains=M,
+                               warps_per_chain=shape[0])
     line = {
         "metric": "ministeps/s", "value": value, "unit": "ministeps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
