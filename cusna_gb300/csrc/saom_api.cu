@@ -738,8 +738,13 @@ std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, in
   for (int gi = 0; gi < 5; ++gi) {
     const int G = Gs[gi];
     if (force_G && G != force_G) continue;
-    // in-rows, then out-rows move to global scratch when shared memory is short
+    // placements: everything in shared memory; the in-rows in global scratch
+    // (L1-cached; a candidate even when shared memory suffices, as it frees
+    // shared memory for more chains per SM); the out-rows too, only when
+    // neither of the first two fits
+    bool placed = false;
     for (int place = 0; place < 3; ++place) {
+      if (place == 2 && placed) break;
       const bool rows_smem = place < 2, cols_smem = place == 0;
       LaunchShape sh{};
       sh.G = G;
@@ -771,7 +776,7 @@ std::vector<LaunchShape> rank_shapes(int nmax, int Wmax, int kmax, int kbmax, in
         all.push_back({score, x});
         any = true;
       }
-      if (any) break;   // the first placement that fits is the one used for this G
+      placed |= any;
     }
   }
   std::stable_sort(all.begin(), all.end(),
@@ -854,12 +859,24 @@ bool jit_for(const std::vector<Job> &jobs, int spec_mode, JitKernel *jk) {
 }
 
 // the model's two best shapes of each team size, in the model's order
+// Two candidates per team size G, in the model's order: its best shape for
+// that G and the best with the other placement of the in-rows (shared memory
+// or global scratch), or without one its second best.
 std::vector<LaunchShape> tuning_candidates(const std::vector<LaunchShape> &ranked) {
   std::vector<LaunchShape> c;
-  for (const LaunchShape &s : ranked) {
-    int seen = 0;
-    for (const LaunchShape &x : c) seen += x.G == s.G;
-    if (seen < 2) c.push_back(s);
+  for (size_t i = 0; i < ranked.size(); ++i) {
+    const LaunchShape &first = ranked[i];
+    bool seen = false;
+    for (const LaunchShape &x : c) seen |= x.G == first.G;
+    if (seen) continue;
+    c.push_back(first);
+    const LaunchShape *second = nullptr;
+    for (size_t j = i + 1; j < ranked.size() && !second; ++j)
+      if (ranked[j].G == first.G && ranked[j].cols_in_smem != first.cols_in_smem)
+        second = &ranked[j];
+    for (size_t j = i + 1; j < ranked.size() && !second; ++j)
+      if (ranked[j].G == first.G) second = &ranked[j];
+    if (second) c.push_back(*second);
   }
   return c;
 }
