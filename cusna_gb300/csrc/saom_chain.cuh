@@ -309,20 +309,17 @@ __device__ __forceinline__ bool is_nan64(double x) {
 // The score sums are formed per alter group: the 32-alter blocks b (alter j
 // in block j >> 5, on lane j & 31) fall into nsb groups, block b into group
 // b mod nsb, with nsb fixed by n alone. A team of G warps takes groups g,
-// g+G, ...; each group costs one warp reduction, so small networks (up to 16
-// blocks) use few large groups (about four blocks each, at least two), and
-// larger ones a multiple of 4 with up to two blocks per group (shared evenly
-// by teams of up to 16 warps). A lane adds its alters of a group in ascending
+// g+G, ...; each group costs one warp reduction, so networks of up to 16
+// blocks use at most four groups (up to four blocks each; teams of up to four
+// warps share them), and larger ones a multiple of 4 with up to two blocks per
+// group (shared evenly by teams of up to 16 warps). A lane adds its alters of a group in ascending
 // block order into double-float accumulators, one warp reduction per group
 // follows, and the group records are combined in group order: every sum's
 // order depends on n and j only, never on the team size.
 __host__ __device__ __forceinline__ int lse_groups(int nb) {
   // up to 16 blocks: about four blocks per group, at least two groups (so a
   // team of two warps shares the pass); beyond: about two blocks per group
-  if (nb <= 16) {
-    const int g = (nb + 3) / 4;
-    return nb < 2 ? nb : (g < 2 ? 2 : g);
-  }
+  if (nb <= 16) return nb < 4 ? nb : 4;
   const int g = 4 * ((nb + 7) / 8);
   return g < nb ? g : nb;
 }
