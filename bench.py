@@ -97,17 +97,18 @@ def smem_bytes_per_network_ministep(n, W):
 # captures of the bench's own launches (smsp__inst_executed.sum over the
 # launch's 6,557,430 network ministeps; n=200, k=8, 4096 chains), keyed by
 # workload, kernel specialised to the effect plan, and warps per chain of the
-# tuned shape (one warp per chain: 41,552,184,346 per launch; two:
-# 45,901,908,023); and per ministep (network and behaviour, 6,146,609 a
-# launch) of the n=1000 co-evolution workload's specialised kernel (16 warps
-# per chain: 186,772,337,633 per launch; 8: 153,974,457,454).
-INST_PER_MINISTEP = {("c2", True, 1): 6337.0, ("c2", True, 2): 7000.0,
-                     ("c4", True, 16): 30387.0, ("c4", True, 8): 25050.0}
+# tuned shape (one warp per chain, columns in shared memory or in global
+# scratch: 44,515,682,075 per launch), and per ministep (network and
+# behaviour, 6,146,609 a launch) of the n=1000 co-evolution workload's
+# specialised kernel (16 warps per chain: 186,772,337,633 per launch; 8:
+# 153,974,457,454).
+INST_PER_MINISTEP = {("c2", True, 1): 6789.0, ("c4", True, 16): 30387.0, ("c4", True, 8): 25050.0}
 # DRAM bytes of one period-kernel launch of the bench workload (the problem, its
-# tables and the outputs), measured by ncu on the bench's own timed launch
-# (dram__bytes_read.sum 4,728,832 + dram__bytes_write.sum 1,488,640 at 4096
-# chains, specialised kernel, one warp per chain).
-DRAM_BYTES_PER_LAUNCH = {("c2", 4096): 4728832.0 + 1488640.0}
+# tables, the column bitsets' global scratch and the outputs), measured by ncu
+# on the bench's own timed launch (dram__bytes_read.sum 5,991,168 +
+# dram__bytes_write.sum 8,859,392 at 4096 chains, specialised kernel, one warp
+# per chain, 16 chains per CTA).
+DRAM_BYTES_PER_LAUNCH = {("c2", 4096): 5991168.0 + 8859392.0}
 
 
 def period_roofline(workload, n, W, k, net_steps, kernel_ms, sm_count, clk, specialised=True,
