@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "libcusna.h"
+#include "mom_host.h"
 #include "saom_launch.h"
 
 namespace cusna {
@@ -49,111 +50,6 @@ void mom_err(const char *fmt, ...) {
       return CUSNA_ERR_CUDA;                                                \
     }                                                                       \
   } while (0)
-
-// ---- dense linear algebra (p is small: tens of parameters) ------------------
-typedef std::vector<double> Mat;  // row-major p x p
-
-// Inverse by Gauss-Jordan elimination with partial pivoting; false when a
-// pivot vanishes (R's solve() fails there).
-bool invert(const Mat &A, int p, Mat &out) {
-  Mat a = A;
-  out.assign((size_t)p * p, 0.0);
-  for (int i = 0; i < p; ++i) out[(size_t)i * p + i] = 1.0;
-  double scale = 0.0;
-  for (double x : a) scale = std::max(scale, std::fabs(x));
-  if (!(scale > 0.0)) return false;
-  for (int c = 0; c < p; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < p; ++r)
-      if (std::fabs(a[(size_t)r * p + c]) > std::fabs(a[(size_t)piv * p + c])) piv = r;
-    const double pv = a[(size_t)piv * p + c];
-    if (!(std::fabs(pv) > 1e-14 * scale)) return false;
-    if (piv != c)
-      for (int q = 0; q < p; ++q) {
-        std::swap(a[(size_t)piv * p + q], a[(size_t)c * p + q]);
-        std::swap(out[(size_t)piv * p + q], out[(size_t)c * p + q]);
-      }
-    for (int q = 0; q < p; ++q) {
-      a[(size_t)c * p + q] /= pv;
-      out[(size_t)c * p + q] /= pv;
-    }
-    for (int r = 0; r < p; ++r) {
-      if (r == c) continue;
-      const double f = a[(size_t)r * p + c];
-      if (f == 0.0) continue;
-      for (int q = 0; q < p; ++q) {
-        a[(size_t)r * p + q] -= f * a[(size_t)c * p + q];
-        out[(size_t)r * p + q] -= f * out[(size_t)c * p + q];
-      }
-    }
-  }
-  return true;
-}
-
-// Moore-Penrose pseudo-inverse (R/mom.R:15-19: singular values below
-// sqrt(eps) times the largest dropped) by one-sided Jacobi SVD.
-Mat pinv(const Mat &A, int p) {
-  Mat U = A, V((size_t)p * p, 0.0);
-  for (int i = 0; i < p; ++i) V[(size_t)i * p + i] = 1.0;
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0.0;
-    for (int i = 0; i < p - 1; ++i)
-      for (int j = i + 1; j < p; ++j) {
-        double a = 0, b = 0, g = 0;
-        for (int r = 0; r < p; ++r) {
-          const double ui = U[(size_t)r * p + i], uj = U[(size_t)r * p + j];
-          a += ui * ui;
-          b += uj * uj;
-          g += ui * uj;
-        }
-        if (std::fabs(g) <= 1e-300) continue;
-        off = std::max(off, std::fabs(g) / std::sqrt(a * b + 1e-300));
-        const double zeta = (b - a) / (2.0 * g);
-        const double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
-        for (int r = 0; r < p; ++r) {
-          const double ui = U[(size_t)r * p + i], uj = U[(size_t)r * p + j];
-          U[(size_t)r * p + i] = c * ui - s * uj;
-          U[(size_t)r * p + j] = s * ui + c * uj;
-          const double vi = V[(size_t)r * p + i], vj = V[(size_t)r * p + j];
-          V[(size_t)r * p + i] = c * vi - s * vj;
-          V[(size_t)r * p + j] = s * vi + c * vj;
-        }
-      }
-    if (off < 1e-15) break;
-  }
-  std::vector<double> sv(p);
-  double smax = 0.0;
-  for (int j = 0; j < p; ++j) {
-    double s2 = 0;
-    for (int r = 0; r < p; ++r) s2 += U[(size_t)r * p + j] * U[(size_t)r * p + j];
-    sv[j] = std::sqrt(s2);
-    smax = std::max(smax, sv[j]);
-  }
-  const double tol = std::sqrt(2.220446049250313e-16) * smax;
-  Mat out((size_t)p * p, 0.0);
-  for (int j = 0; j < p; ++j) {
-    if (!(sv[j] > tol)) continue;
-    for (int r = 0; r < p; ++r)
-      for (int c = 0; c < p; ++c)
-        out[(size_t)r * p + c] += V[(size_t)r * p + j] * U[(size_t)c * p + j] / (sv[j] * sv[j]);
-  }
-  return out;
-}
-
-// R/mom.R:20-22 (.safe_solve): the inverse, or the pseudo-inverse when solve() fails
-Mat safe_solve(const Mat &A, int p) {
-  Mat inv;
-  if (invert(A, p, inv)) return inv;
-  return pinv(A, p);
-}
-
-std::vector<double> matvec(const Mat &A, const std::vector<double> &x, int p) {
-  std::vector<double> y(p, 0.0);
-  for (int r = 0; r < p; ++r)
-    for (int c = 0; c < p; ++c) y[r] += A[(size_t)r * p + c] * x[c];
-  return y;
-}
 
 // ---- one chain count's plan: the periods on the device ------------------------
 struct DevMem {
@@ -360,54 +256,15 @@ cusna_status simulate_round(const Model &m, Plan &pl, const std::vector<double> 
   return CUSNA_OK;
 }
 
-std::vector<double> col_means(const std::vector<double> &X, int M, int p) {
-  std::vector<double> mu(p, 0.0);
-  for (int c = 0; c < M; ++c)
-    for (int j = 0; j < p; ++j) mu[j] += X[(size_t)c * p + j];
-  for (int j = 0; j < p; ++j) mu[j] /= M;
-  return mu;
-}
+Mat derivative(const Round &R, int p) { return mom_derivative(R.sp, R.scp, R.M, p); }
 
-// score-function derivative summed over periods (R/mom.R:173-182)
-Mat derivative(const Round &R, int p) {
-  Mat D((size_t)p * p, 0.0);
-  const int M = R.M;
-  for (size_t q = 0; q < R.sp.size(); ++q) {
-    const std::vector<double> ms = col_means(R.sp[q], M, p), mc = col_means(R.scp[q], M, p);
-    for (int c = 0; c < M; ++c)
-      for (int a = 0; a < p; ++a) {
-        const double x = R.sp[q][(size_t)c * p + a] - ms[a];
-        if (x == 0.0) continue;
-        for (int b = 0; b < p; ++b) D[(size_t)a * p + b] += x * (R.scp[q][(size_t)c * p + b] - mc[b]);
-      }
-  }
-  for (double &x : D) x /= M;
-  return D;
-}
-
-// diagonalised inverse (R/mom.R:184-187)
-Mat dinv_of(const Mat &D, int p, double w) {
-  Mat A = D;
-  for (int a = 0; a < p; ++a)
-    for (int b = 0; b < p; ++b) A[(size_t)a * p + b] *= (a == b) ? 1.0 : (1.0 - w);
-  return safe_solve(A, p);
-}
-
-// step cap and rate floor (R/mom.R:189-197)
 std::vector<double> guard_step(const Model &m, const std::vector<double> &theta,
                                std::vector<double> step) {
-  for (int j = 0; j < m.p; ++j) {
-    const double cap = std::max(1.0, 0.5 * std::fabs(theta[j]));
-    step[j] = std::min(std::max(step[j], -cap), cap);
-  }
-  const int n_rates = m.cond ? 0 : m.P;
-  for (int j = 0; j < n_rates; ++j)
-    if (theta[j] - step[j] < 0.1 * theta[j]) step[j] = 0.5 * theta[j];
-  return step;
+  return mom_guard_step(theta, std::move(step), m.cond ? 0 : m.P);
 }
 
 std::vector<double> deviation(const Round &R, const Model &m) {
-  std::vector<double> d = col_means(R.stats, R.M, m.p);
+  std::vector<double> d = mom_col_means(R.stats, R.M, m.p);
   for (int j = 0; j < m.p; ++j) d[j] -= m.targets[j];
   return d;
 }
@@ -535,8 +392,8 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
   std::unique_ptr<NvtxRange> range(new NvtxRange("mom phase 1"));
   if ((s = round(n1, true, R)) != CUSNA_OK) return s;
   {
-    const Mat di = dinv_of(derivative(R, p), p, diag_w);
-    std::vector<double> step = matvec(di, deviation(R, m), p);
+    const Mat di = mom_dinv(derivative(R, p), p, diag_w);
+    std::vector<double> step = mom_matvec(di, deviation(R, m), p);
     for (double &x : step) x *= 0.5 * firstg;
     step = guard_step(m, theta, step);
     for (int j = 0; j < p; ++j) theta[j] -= step[j];
@@ -550,11 +407,11 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
   for (int sub = 0; sub < nsub; ++sub) {
     const double gain = firstg * std::pow(0.5, sub);
     if ((s = round(nD, true, R)) != CUSNA_OK) return s;
-    const Mat di = dinv_of(derivative(R, p), p, diag_w);
+    const Mat di = mom_dinv(derivative(R, p), p, diag_w);
     std::vector<double> thav(p, 0.0);
     for (int it = 0; it < n2[sub]; ++it) {
       if ((s = round(batch2, false, R)) != CUSNA_OK) return s;
-      std::vector<double> step = matvec(di, deviation(R, m), p);
+      std::vector<double> step = mom_matvec(di, deviation(R, m), p);
       for (double &x : step) x *= gain;
       step = guard_step(m, theta, step);
       for (int j = 0; j < p; ++j) {
@@ -576,8 +433,8 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
   range.reset(new NvtxRange("mom phase 3"));
   if ((s = round(n3, true, R)) != CUSNA_OK) return s;
   const Mat D = derivative(R, p);
-  const Mat dinv = safe_solve(D, p);
-  const std::vector<double> mu = col_means(R.stats, R.M, p);
+  const Mat dinv = mom_safe_solve(D, p);
+  const std::vector<double> mu = mom_col_means(R.stats, R.M, p);
   Mat msf((size_t)p * p, 0.0);
   for (int c = 0; c < R.M; ++c)
     for (int a = 0; a < p; ++a) {
@@ -587,7 +444,7 @@ extern "C" CUSNA_API cusna_status cusna_mom_estimate(const cusna_saom_problem *p
   for (double &x : msf) x /= (R.M - 1);
   std::vector<double> dev(p);
   for (int j = 0; j < p; ++j) dev[j] = mu[j] - m.targets[j];
-  const std::vector<double> md = matvec(safe_solve(msf, p), dev, p);
+  const std::vector<double> md = mom_matvec(mom_safe_solve(msf, p), dev, p);
   double q2 = 0.0;
   for (int j = 0; j < p; ++j) q2 += dev[j] * md[j];
   // cov = dinv msf dinv^T
