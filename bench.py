@@ -663,8 +663,9 @@ def fran_latency(args):
 def multi_comparison(args):
     """The multi-network simulator (cusna_saom_simulate_multi) and estimator.
     Throughput: M chains of a 2-network period with every cross-effect type,
-    through the C ABI with host buffers (median of 3 calls after 2 warm-up
-    calls), beside the reference CPU engine (cusna_saom_simulate_multi_cpu) on a
+    through the C ABI with host buffers (median of 3 calls after 12 warm-up
+    calls, in which the autotuner tries its candidate shapes), beside the
+    reference CPU engine (cusna_saom_simulate_multi_cpu) on a
     bounded sample of the chains. Fit: mom_estimate_multinet on a synthetic
     2-network panel with the reference test's control settings, over the GPU
     engine and over the CPU engine (the oracle's restatement of the simulator
@@ -681,7 +682,7 @@ def multi_comparison(args):
     for _ in range(3):
         sim.simulate_multi(m)
     sim.specialise_wait(900.0)
-    for _ in range(2):
+    for _ in range(12):
         sim.simulate_multi(m)
     ts = []
     for _ in range(3):

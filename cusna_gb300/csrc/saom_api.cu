@@ -1229,7 +1229,12 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
     set_err("no launch shape fits %d networks of n=%d", D, n);
     return CUSNA_ERR_UNSUPPORTED;
   }
-  const LaunchShape sh = ranked[0];
+  // the autotuner as for single networks, under a key of its own (the
+  // network count in the flags)
+  TuneKey tkey = tune_key(n, W, kmax, 0, 0, tp, gw, tq, M, use_jit);
+  tkey.flags |= (D << 8) | (1 << 7);
+  int trial = -1;
+  const LaunchShape sh = tuner_pick(tkey, tuning_candidates(ranked), &trial);
   Planner pl;
   for (auto &J : jobs) plan_problem(pl, J, false);
   const size_t o_probs = pl.take(sizeof(DevProblem) * D);
@@ -1267,6 +1272,7 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
   CU(cudaMemcpyAsync(at<char>(o_lam), pb->lam, (size_t)M * D * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(at<char>(o_gidx), gidx.data(), (size_t)k * 4, cudaMemcpyHostToDevice, st));
   CU(cudaMemsetAsync(at<char>(o_counter), 0, sizeof(unsigned long long), st));
+  CU(cudaEventRecord(g_ctx.ev0, st));
   if (use_jit)
     CU(launch_multi_jit(jk, sh, at<DevProblem>(o_probs), md, M, at<unsigned long long>(o_counter),
                         o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
@@ -1275,6 +1281,7 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
     CU(launch_multi(sh, at<DevProblem>(o_probs), md, M, at<unsigned long long>(o_counter),
                     o_cols == NONE ? nullptr : at<uint32_t>(o_cols),
                     o_rows == NONE ? nullptr : at<uint32_t>(o_rows), cols_words, st));
+  CU(cudaEventRecord(g_ctx.ev1, st));
   auto get = [&](void *dst, size_t off, size_t bytes) -> cusna_status {
     if (!dst || off == NONE) return CUSNA_OK;
     CU(cudaMemcpyAsync(dst, at<char>(off), bytes, cudaMemcpyDeviceToHost, st));
@@ -1286,6 +1293,11 @@ cusna_status simulate_multi(const cusna_saom_multi_problem *pb, cusna_saom_multi
   if ((s = get(r->steps, o_st, (size_t)M * 4)) != CUSNA_OK) return s;
   if ((s = get(r->a_ends, o_ae, (size_t)M * D * n * n)) != CUSNA_OK) return s;
   CU(cudaStreamSynchronize(st));
+  if (trial >= 0) {
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, g_ctx.ev0, g_ctx.ev1));
+    tuner_record(tkey, trial, ms);
+  }
   return CUSNA_OK;
 }
 
